@@ -1,0 +1,243 @@
+"""Drop-in replacement of the reference Python module ``acoustics3d`` (``DiffBEM`` and ``sphere``).
+
+Same constructor signature and defaults (acoustics3d_cpp/src/acoustics3d.cpp:355-357), same
+method names, argument meaning and return types (acoustics3d.cpp:358-382). Where the reference
+printed to stderr and returned a sentinel, these raise ``AC3DError``. Keyword-only extensions:
+``precision`` ("mixed" = complex FP32 H-matrix with FP64 refinement, "fp64"), ``incident``
+(``("point", xyz)`` default at ``src_pt``, or ``("plane", direction)``).
+
+The work runs on the GPU through ``libac3d.so`` (include/ac3d.h); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as _L
+from ._lib import AC3DError
+
+__all__ = ["DiffBEM", "sphere", "AC3DError"]
+
+_PREC = {"mixed": _L.PREC_MIXED, "fp32": _L.PREC_MIXED, "fp64": _L.PREC_FP64}
+
+
+def _f64(a, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _cplx(buf: np.ndarray) -> np.ndarray:
+    return buf.view(np.complex128).copy()
+
+
+class DiffBEM:
+    """GPU BEM value / gradient of the diffusion coefficient of a mesh (reference ``DiffBEM``)."""
+
+    def __init__(self, cluster_size=64, radius_factor=1.5, freq_bands=(1000,), n_freqs=1, approx_ACA_tol=1e-3,
+                 Q_ACA_tol=1e-3, solver_tol=1e-3, src_pt=(0.0, 100.0, 0.0), listener_radius=50, listener_ds=5,
+                 recompute_matrices=False, *, precision: str = "mixed", incident=None, listener: str = "dense"):
+        L = _L.lib()
+        bands = _f64(list(freq_bands))
+        src = _f64(src_pt, (3,))
+        h = ctypes.c_void_p()
+        rc = L.ac3d_create(ctypes.byref(h), int(cluster_size), float(radius_factor), _L.ptr(bands), len(bands),
+                           int(n_freqs), float(approx_ACA_tol), float(Q_ACA_tol), float(solver_tol), _L.ptr(src),
+                           float(listener_radius), float(listener_ds), int(bool(recompute_matrices)))
+        if rc != _L.OK:
+            raise AC3DError(rc, "invalid DiffBEM parameters or no CUDA device")
+        self._h = h
+        self._bands = list(bands)
+        self.silent = False
+        self.use_actual = False
+        self._Hs: dict[int, int] = {}
+        self._Ps = None
+        self._Es = None
+        self._diff_set = False
+        self.set_precision(precision)
+        self.set_listener_mode(listener)
+        if incident is not None:
+            self.set_incident(*incident)
+
+    # -- lifecycle ----------------------------------------------------------------------------
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _L.lib().ac3d_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def _check(self, rc):
+        _L.check(self._h, rc)
+
+    def _actual_unsupported(self):
+        if self.use_actual:
+            raise NotImplementedError("use_actual (dense QR path) is not provided by the GPU build")
+
+    # -- extensions -----------------------------------------------------------------------------
+    def set_precision(self, precision: str) -> None:
+        self._check(_L.lib().ac3d_set_precision(self._h, _PREC[precision]))
+        self.precision = precision
+
+    def set_listener_mode(self, mode: str) -> None:
+        """"dense": receiver matrix evaluated exactly on the fly (default); "aca": partially pivoted
+        ACA with Q_ACA_tol, as the reference (aca.cpp:84-134)."""
+        m = {"dense": _L.LISTENER_DENSE, "aca": _L.LISTENER_ACA}[mode]
+        self._check(_L.lib().ac3d_set_listener_mode(self._h, m))
+        self.listener = mode
+
+    def set_incident(self, kind: str, vec) -> None:
+        k = {"point": _L.INCIDENT_POINT, "plane": _L.INCIDENT_PLANE}[kind]
+        self._check(_L.lib().ac3d_set_incident(self._h, k, _L.ptr(_f64(vec, (3,)))))
+
+    def set_solver(self, max_iterations: int = 0, inner_tol: float = 1e-4, max_outer: int = 10) -> None:
+        self._check(_L.lib().ac3d_set_solver(self._h, int(max_iterations), float(inner_tol), int(max_outer)))
+
+    def set_listeners(self, listeners) -> None:
+        Ls = _f64(listeners).reshape(-1, 3)
+        self._check(_L.lib().ac3d_set_listeners(self._h, _L.ptr(Ls), len(Ls)))
+
+    def stats(self) -> dict:
+        s = _L.Stats()
+        self._check(_L.lib().ac3d_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    # -- reference API --------------------------------------------------------------------------
+    def set_mesh(self, Ps, Es):
+        """acoustics3d.cpp:36-67: returns (Ps, Es permuted into cluster-tree order)."""
+        Ps = _f64(Ps).reshape(-1, 3)
+        Es = _i32(Es).reshape(-1, 3)
+        out = np.zeros_like(Es)
+        self._check(_L.lib().ac3d_set_mesh(self._h, _L.ptr(Ps), len(Ps), _L.ptr(Es), len(Es), _L.ptr(out)))
+        self._Ps, self._Es = Ps.copy(), out
+        self._diff_set = False
+        if not self.silent:
+            print(f"{len(Ps)} vertices, {len(Es)} elements")
+        return Ps.copy(), out.copy()
+
+    def set_diff_points(self, diff_pts) -> None:
+        """acoustics3d.cpp:69-101."""
+        d = _i32(list(diff_pts))
+        self._check(_L.lib().ac3d_set_diff_points(self._h, _L.ptr(d), len(d)))
+        self._Hs = {}
+        for i in d:
+            self._Hs[int(i)] = len(self._Hs)
+        self._diff_set = True
+
+    def precompute(self, Ps, Es, diff_pts):
+        """acoustics3d.cpp:103-107."""
+        out = self.set_mesh(Ps, Es)
+        self.set_diff_points(diff_pts)
+        return out
+
+    def value(self, x=None) -> float:
+        """acoustics3d.cpp:109-160: band-mean diffusion coefficient (optionally at heights x)."""
+        self._actual_unsupported()
+        c = ctypes.c_double()
+        xx = None if x is None else _f64(x)
+        self._check(_L.lib().ac3d_value(self._h, _L.ptr(xx), ctypes.byref(c)))
+        return c.value
+
+    def band_value(self, freq_band) -> float:
+        """acoustics3d.cpp:162-176."""
+        self._actual_unsupported()
+        c = ctypes.c_double()
+        self._check(_L.lib().ac3d_band_value(self._h, float(freq_band), ctypes.byref(c)))
+        return c.value
+
+    def values(self) -> list:
+        """acoustics3d.cpp:178-197."""
+        self._actual_unsupported()
+        out = np.zeros(len(self._bands))
+        self._check(_L.lib().ac3d_values(self._h, _L.ptr(out)))
+        return [float(v) for v in out]
+
+    def gradient(self, x):
+        """acoustics3d.cpp:199-234: (c, dc/dx), both summed over bands."""
+        self._actual_unsupported()
+        xx = _f64(x)
+        g = np.zeros(len(xx))
+        c = ctypes.c_double()
+        self._check(_L.lib().ac3d_gradient(self._h, _L.ptr(xx), ctypes.byref(c), _L.ptr(g)))
+        return c.value, g
+
+    def pvals(self, frequency, listeners=None) -> np.ndarray:
+        """acoustics3d.cpp:236-280: complex pressures at the receivers."""
+        if listeners is None:
+            n = ctypes.c_int()
+            self._check(_L.lib().ac3d_num_listeners(self._h, ctypes.byref(n)))
+            out = np.zeros(2 * n.value)
+            self._check(_L.lib().ac3d_pressures(self._h, float(frequency), None, 0, _L.ptr(out)))
+        else:
+            Ls = _f64(listeners).reshape(-1, 3)
+            out = np.zeros(2 * len(Ls))
+            self._check(_L.lib().ac3d_pressures(self._h, float(frequency), _L.ptr(Ls), len(Ls), _L.ptr(out)))
+        return _cplx(out)
+
+    def surface_vals(self, frequency) -> np.ndarray:
+        """acoustics3d.cpp:282-315: the surface solution in tree order."""
+        n = 0 if self._Es is None else len(self._Es)
+        out = np.zeros(2 * max(n, 1))
+        self._check(_L.lib().ac3d_surface_values(self._h, float(frequency), _L.ptr(out)))
+        return _cplx(out[:2 * n])
+
+    def get_listeners(self) -> np.ndarray:
+        n = ctypes.c_int()
+        self._check(_L.lib().ac3d_num_listeners(self._h, ctypes.byref(n)))
+        out = np.zeros((n.value, 3))
+        self._check(_L.lib().ac3d_get_listeners(self._h, _L.ptr(out)))
+        return out
+
+    def get_mesh(self, x=None):
+        """acoustics3d.cpp:321-342."""
+        if self._Ps is None:
+            print("Warning! No mesh set. Behavior might not be as expected.")
+            return np.zeros((0, 3)), np.zeros((0, 3), np.int32)
+        Ps = self._Ps.copy()
+        if x is not None:
+            if not self._diff_set:
+                print("Warning! No diff points set. Behavior might not be as expected.")
+            for v, h in self._Hs.items():
+                Ps[v, 1] = x[h] + self._Ps[v, 1]
+        return Ps, self._Es.copy()
+
+    def get_Hs(self) -> dict:
+        return dict(self._Hs)
+
+    def set_band(self, freq_band) -> None:
+        """acoustics3d.cpp:348-351."""
+        self._check(_L.lib().ac3d_set_band(self._h, float(freq_band)))
+        self._bands = [float(freq_band)]
+
+    def set_bands(self, freq_bands) -> None:
+        b = _f64(list(freq_bands))
+        self._check(_L.lib().ac3d_set_bands(self._h, _L.ptr(b), len(b)))
+        self._bands = list(b)
+
+
+def sphere(sphere_mesh, freq, LL=100, lrad=10, actual=False, *, precision: str = "fp64") -> np.ndarray:
+    """sphere.h:28-85: scattered pressure of a plane wave e^{-ikx} on a mesh read from an OBJ path
+    (or given as an (Ps, Es) tuple), at LL receivers on a circle of radius lrad in the xz plane."""
+    if actual:
+        raise NotImplementedError("actual=True (dense QR path) is not provided by the GPU build")
+    if isinstance(sphere_mesh, (tuple, list)):
+        Ps, Es = sphere_mesh
+    else:
+        from .meshes import read_obj
+        Ps, Es = read_obj(sphere_mesh)
+    Ps = _f64(Ps).reshape(-1, 3)
+    Es = _i32(Es).reshape(-1, 3)
+    out = np.zeros(2 * int(LL))
+    rc = _L.lib().ac3d_sphere(_L.ptr(Ps), len(Ps), _L.ptr(Es), len(Es), float(freq), int(LL), float(lrad),
+                              _PREC[precision], _L.ptr(out))
+    if rc != _L.OK:
+        raise AC3DError(rc, "sphere evaluation failed")
+    return _cplx(out)

@@ -1,0 +1,1118 @@
+// Host orchestration and the C-ABI of libac3d.so.
+//
+// Mirrors the reference binding DiffBEM (acoustics3d_cpp/src/acoustics3d.cpp:22-351) and its
+// driver bem3d::gradient (acoustics3d_cpp/src/adjoint.cpp:24-242): set_mesh builds the tree and
+// partition once; every evaluation updates vertex heights, assembles one H-matrix per frequency
+// on the GPU, solves with the device-resident BiCGSTAB, evaluates the receivers, forms the
+// diffusion coefficient and, for the gradient, runs the adjoint solve and shape derivatives.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ac3d.h"
+#include "internal.h"
+#include "krylov.h"
+#include "listener.h"
+
+namespace ac3d {
+
+void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
+  if (e != cudaSuccess) {
+    throw Error(AC3D_ERR_CUDA, std::string(cudaGetErrorName(e)) + ": " + cudaGetErrorString(e) + " (" + what +
+                                   " at " + file + ":" + std::to_string(line) + ")");
+  }
+}
+
+void DevBuf::alloc(size_t n, cudaStream_t stream) {
+  release();
+  s = stream;
+  if (n == 0) n = 16;
+  cudaError_t e = cudaMallocAsync(&p, n, s);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    throw Error(AC3D_ERR_RESOURCE, "device allocation of " + std::to_string(n) + " bytes failed");
+  }
+  AC3D_CUDA(e);
+  bytes = n;
+}
+
+void DevBuf::release() {
+  if (p) cudaFreeAsync(p, s);
+  p = nullptr;
+  bytes = 0;
+}
+
+template <typename T>
+static void upload(DevBuf& d, const std::vector<T>& h, cudaStream_t s) {
+  d.alloc(std::max<size_t>(h.size(), 1) * sizeof(T), s);
+  if (!h.empty()) AC3D_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+static double wavenumber(double f) { return 2 * kPiHost * f / 344.0; }  // helpers.h:8, constants.h:13
+
+// get_frequencies (helpers.cpp:67-83)
+static std::vector<double> frequencies(double band, int n) {
+  if (n == 1) return {band};
+  double bw = std::pow(2.0, 1.0 / 6.0);
+  double lo = std::log(band / bw), hi = std::log(band * bw);
+  double d = (hi - lo) / (n - 1.0);
+  std::vector<double> f;
+  for (int i = 0; i < n; i++) f.push_back(std::exp(lo + i * d));
+  return f;
+}
+
+// compute_listener_pts + spherical_to_cartesian (helpers.cpp:34-65)
+static std::vector<double> hemisphere(double radius, double ds) {
+  std::vector<double> el{0}, az{0};
+  for (double e = ds; e < 91; e += ds)
+    for (double a = 0; a < 360; a += ds) {
+      el.push_back(e);
+      az.push_back(a);
+    }
+  std::vector<double> L;
+  for (size_t i = 0; i < el.size(); i++) {
+    double th = el[i] * kPiHost / 180.0, ph = az[i] * kPiHost / 180.0;
+    L.push_back(radius * std::sin(th) * std::cos(ph));
+    L.push_back(radius * std::cos(th));
+    L.push_back(-radius * std::sin(th) * std::sin(ph));
+  }
+  return L;
+}
+
+struct GpuTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaStream_t s;
+  explicit GpuTimer(cudaStream_t st) : s(st) {
+    AC3D_CUDA(cudaEventCreate(&a));
+    AC3D_CUDA(cudaEventCreate(&b));
+    AC3D_CUDA(cudaEventRecord(a, s));
+  }
+  double stop() {
+    AC3D_CUDA(cudaEventRecord(b, s));
+    AC3D_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    AC3D_CUDA(cudaEventElapsedTime(&ms, a, b));
+    return ms;
+  }
+  ~GpuTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  const void* key_h = nullptr;
+  const void* key_x = nullptr;
+  bool tr = false;
+  int vec64 = 0;
+  ~GraphCache() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+}  // namespace ac3d
+
+using namespace ac3d;
+
+struct ac3d_ctx {
+  // constructor parameters (DiffBEM, acoustics3d.cpp:22-34)
+  int cluster_size = 64;
+  double radius_factor = 1.5;
+  std::vector<double> bands{1000};
+  int n_freqs = 1;
+  double aca_tol = 1e-3, q_tol = 1e-3, solver_tol = 1e-3;
+  double src[3] = {0, 100, 0};
+  int src_kind = AC3D_INCIDENT_POINT;
+  double listener_radius = 50, listener_ds = 5;
+  bool recompute = false;
+  // extensions
+  int prec = AC3D_PREC_MIXED;
+  int listener_mode = AC3D_LISTENER_DENSE;
+  int maxit = 0;           // 0: twice the number of unknowns
+  double inner_tol = 1e-4; // relative tolerance of each FP32 inner solve
+  int max_outer = 10;
+  int chunk = 8;           // BiCGSTAB iterations per captured graph launch
+  int maxk = 100;          // APPROX_ACA_MAX_K (constants.h:16)
+
+  cudaStream_t stream = nullptr;
+  std::string err;
+  ac3d_stats stats{};
+
+  // mesh
+  bool mesh_set = false, diff_set = false;
+  int V = 0, Ne = 0;
+  std::vector<double> Ps0;  // base positions
+  std::vector<int> Es;      // tree order
+  Partition P;
+  DevPartition DP;
+  DevGeometry G;
+  int64_t sum_mn = 0, worst_pool = 0;
+  int64_t pool_hint[2] = {0, 0};
+  std::vector<double> Ls;   // receivers for value/gradient
+  DevBuf Ls_dev;
+  // differentiable points
+  std::vector<int> diff_pts;
+  std::unordered_map<int, int> Hs;
+  std::vector<int> h_off, pair_elem, pair_corner, pair_touch, touch;
+  DevBuf d_h_off, d_pair_elem, d_pair_corner, d_pair_touch, d_touch;
+
+  // work buffers
+  DevBuf kv, partials, kstate, red, b64, x64, r64, ff_scratch, adj_scratch, tmp_recv;
+  KState* h_state = nullptr;  // pinned
+  double* h_red = nullptr;    // pinned
+
+  ~ac3d_ctx() {
+    if (h_state) cudaFreeHost(h_state);
+    if (h_red) cudaFreeHost(h_red);
+  }
+};
+
+namespace {
+
+void require_mesh(ac3d_ctx* c) {
+  if (!c->mesh_set) throw Error(AC3D_ERR_STATE, "No mesh set. Set one using set_mesh or precompute.");
+}
+
+// ------------------------------------------------------------------------------------------
+// Assembly
+// ------------------------------------------------------------------------------------------
+std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
+  cudaStream_t s = c->stream;
+  auto H = std::make_unique<DevHMat>();
+  H->prec = prec;
+  H->k = k;
+  H->maxk = c->maxk;
+  const size_t cs = prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
+  H->near.alloc((size_t)std::max<int64_t>(c->P.near_total, 1) * cs, s);
+  launch_near_assembly(c->G, c->DP, *H, s);
+  const int na = c->DP.na;
+  H->rank.alloc((size_t)std::max(na, 1) * sizeof(int), s);
+  H->t_off.alloc((size_t)(na + 1) * sizeof(int), s);
+  AC3D_CUDA(cudaMemsetAsync(H->rank.p, 0, (size_t)std::max(na, 1) * sizeof(int), s));
+  if (na > 0) {
+    H->term_off.alloc((size_t)na * c->maxk * sizeof(long long), s);
+    H->pool_used.alloc(16, s);
+    int64_t cap = c->pool_hint[prec];
+    if (cap <= 0) cap = std::min<int64_t>(c->worst_pool, 16 * c->sum_mn);
+    cap = std::max<int64_t>(cap, 1024);
+    for (int attempt = 0;; attempt++) {
+      H->pool.alloc((size_t)cap * cs, s);
+      H->pool_cap = cap;
+      AC3D_CUDA(cudaMemsetAsync(H->pool_used.p, 0, 16, s));
+      launch_aca(c->G, c->DP, *H, c->aca_tol, c->P.max_rows, s);
+      unsigned long long hu[2];
+      AC3D_CUDA(cudaMemcpyAsync(hu, H->pool_used.p, 16, cudaMemcpyDeviceToHost, s));
+      AC3D_CUDA(cudaStreamSynchronize(s));
+      int status = (int)(hu[1] & 0xffffffffu);
+      if (!(status & 1)) {
+        H->pool_used_host = (int64_t)hu[0];
+        break;
+      }
+      if (cap >= c->worst_pool || attempt > 8) throw Error(AC3D_ERR_INTERNAL, "ACA pool overflow at worst-case size");
+      cap = std::min<int64_t>(c->worst_pool, std::max<int64_t>(cap * 2, (int64_t)hu[0]));
+    }
+    c->pool_hint[prec] = std::min<int64_t>(c->worst_pool, H->pool_used_host + H->pool_used_host / 8 + 4096);
+    launch_rank_scan(c->DP, *H, s);
+    const size_t tcap = (size_t)std::max<int64_t>(c->P.aca_term_cap, 1);
+    H->tvec.alloc(tcap * (prec == PREC_FP64 ? sizeof(cd) : sizeof(cf)), s);
+    H->tvec64.alloc(tcap * sizeof(cd), s);
+    H->ranks_host.resize(na);
+    AC3D_CUDA(cudaMemcpyAsync(H->ranks_host.data(), H->rank.p, na * sizeof(int), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    int64_t lr = 0;
+    int mx = 0;
+    double sr = 0;
+    for (int b = 0; b < na; b++) {
+      int r = H->ranks_host[b];
+      const int* q = &c->P.approx[4 * b];
+      lr += (int64_t)r * ((q[1] - q[0]) + (q[3] - q[2]));
+      mx = std::max(mx, r);
+      sr += r;
+    }
+    H->lr_entries = lr;
+    c->stats.lr_entries = lr;
+    c->stats.max_rank = mx;
+    c->stats.mean_rank = sr / na;
+  } else {
+    AC3D_CUDA(cudaMemsetAsync(H->t_off.p, 0, sizeof(int), s));
+    H->tvec.alloc(16, s);
+    H->tvec64.alloc(16, s);
+  }
+  c->stats.near_entries = c->P.near_total;
+  c->stats.hmat_bytes = (long long)H->bytes();
+  return H;
+}
+
+// ------------------------------------------------------------------------------------------
+// Solve op(A) x = b (b, x FP64 device vectors of length Ne)
+// ------------------------------------------------------------------------------------------
+struct SolveCache {
+  std::vector<std::unique_ptr<GraphCache>> graphs;
+};
+
+void ensure_work(ac3d_ctx* c) {
+  cudaStream_t s = c->stream;
+  const size_t n = (size_t)c->Ne;
+  c->kv.ensure(8 * n * sizeof(cd), s);
+  const int G = krylov_vec_grid(c->Ne);
+  c->partials.ensure((size_t)std::max(c->DP.nleaf, G) * 5 * sizeof(double) + 64, s);
+  c->kstate.ensure(sizeof(KState), s);
+  c->red.ensure(8 * sizeof(double), s);
+  c->b64.ensure(n * sizeof(cd), s);
+  c->x64.ensure(n * sizeof(cd), s);
+  c->r64.ensure(n * sizeof(cd), s);
+  if (!c->h_state) AC3D_CUDA(cudaMallocHost(&c->h_state, 2 * sizeof(KState)));
+  (void)device_sm_count();  // query outside any stream capture
+  if (!c->h_red) AC3D_CUDA(cudaMallocHost(&c->h_red, 8 * sizeof(double)));
+}
+
+KrylovBufs bufs(ac3d_ctx* c, int vec64) {
+  KrylovBufs B;
+  B.n = c->Ne;
+  const size_t es = vec64 ? sizeof(cd) : sizeof(cf);
+  char* base = (char*)c->kv.p;
+  void** slots[8] = {&B.b, &B.x, &B.r, &B.rhat, &B.p, &B.v, &B.s, &B.t};
+  for (int i = 0; i < 8; i++) *slots[i] = base + (size_t)i * c->Ne * es;
+  B.partials = c->partials.as<double>();
+  B.nparts_r = krylov_vec_grid(c->Ne);
+  B.state = c->kstate.as<KState>();
+  return B;
+}
+
+// Runs BiCGSTAB on the prepared buffers (B.b filled). Returns iterations; done flag in *done.
+int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int vec64, double tol, int* done) {
+  cudaStream_t s = c->stream;
+  const int maxit = c->maxit > 0 ? c->maxit : 2 * c->Ne;
+  krylov_enqueue_init(B, vec64, tol, maxit, s);
+  // capture one chunk of iterations as a graph and replay it until the state reports completion
+  cudaGraph_t graph;
+  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  krylov_enqueue_iterations(B, c->DP, H, tr, vec64, c->chunk, s);
+  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
+  cudaGraphExec_t exec;
+  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  AC3D_CUDA(cudaGraphDestroy(graph));
+  int launched = 0;
+  const int max_launch = maxit / c->chunk + 2;
+  // keep one chunk in flight while the host reads the previous state
+  AC3D_CUDA(cudaGraphLaunch(exec, s));
+  AC3D_CUDA(cudaMemcpyAsync(&c->h_state[0], B.state, sizeof(KState), cudaMemcpyDeviceToHost, s));
+  launched++;
+  cudaEvent_t ev;
+  AC3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  AC3D_CUDA(cudaEventRecord(ev, s));
+  KState st{};
+  while (true) {
+    bool more = launched < max_launch;
+    if (more) {
+      AC3D_CUDA(cudaGraphLaunch(exec, s));
+      AC3D_CUDA(cudaMemcpyAsync(&c->h_state[launched & 1], B.state, sizeof(KState), cudaMemcpyDeviceToHost, s));
+    }
+    AC3D_CUDA(cudaEventSynchronize(ev));
+    st = c->h_state[(launched - 1) & 1];
+    if (st.done || !more) break;
+    launched++;
+    AC3D_CUDA(cudaEventRecord(ev, s));
+  }
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  st = c->h_state[(launched - 1) & 1];
+  if (launched < max_launch) {
+    // the extra chunk in flight was a no-op; reread the final state
+    AC3D_CUDA(cudaMemcpy(&st, B.state, sizeof(KState), cudaMemcpyDeviceToHost));
+  } else {
+    AC3D_CUDA(cudaMemcpy(&st, B.state, sizeof(KState), cudaMemcpyDeviceToHost));
+  }
+  AC3D_CUDA(cudaEventDestroy(ev));
+  AC3D_CUDA(cudaGraphExecDestroy(exec));
+  *done = st.done;
+  c->stats.matvecs += 2 * st.iter;
+  return st.iter;
+}
+
+double reduce_norm2_residual(ac3d_ctx* c, const DevHMat& H, bool tr, const cd* b, const cd* x, cd* r) {
+  cudaStream_t s = c->stream;
+  MatvecEpilogue ep;
+  ep.partials = c->partials.as<double>();
+  launch_matvec(c->DP, H, c->Ne, tr, 1, x, r, b, ep, s);
+  launch_reduce5(c->partials.as<double>(), c->DP.nleaf, c->red.as<double>(), s);
+  AC3D_CUDA(cudaMemcpyAsync(c->h_red, c->red.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  c->stats.matvecs++;
+  return c->h_red[4];
+}
+
+// x = op(A)^{-1} b to relative residual solver_tol (FP64 b, x on device).
+void solve(ac3d_ctx* c, const DevHMat& H, const cd* b, cd* x, bool tr) {
+  cudaStream_t s = c->stream;
+  ensure_work(c);
+  const int n = c->Ne;
+  const double tol = c->solver_tol;
+  int done = 0;
+  if (H.prec == PREC_FP64) {
+    KrylovBufs B = bufs(c, 1);
+    launch_copy64(n, b, B.b, s);
+    int it = run_krylov(c, H, B, tr, 1, tol, &done);
+    launch_copy64(n, B.x, x, s);
+    c->stats.iterations += it;
+    c->stats.outer_steps += 1;
+    // final true residual, FP64
+    double rn2 = reduce_norm2_residual(c, H, tr, b, x, c->r64.as<cd>());
+    int np = launch_norm2_64(n, b, c->partials.as<double>(), s);
+    launch_reduce5(c->partials.as<double>(), np, c->red.as<double>(), s);
+    AC3D_CUDA(cudaMemcpyAsync(c->h_red, c->red.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    double b2 = c->h_red[4];
+    c->stats.rel_residual = b2 > 0 ? std::sqrt(rn2 / b2) : 0.0;
+    if (done != 1) c->stats.converged = 0;
+    return;
+  }
+  // mixed precision: FP32 inner BiCGSTAB inside FP64 iterative refinement
+  KrylovBufs B = bufs(c, 0);
+  launch_zero64(n, x, s);
+  double bn2 = reduce_norm2_residual(c, H, tr, b, x, c->r64.as<cd>());  // r = b - A 0 = b
+  double rn2 = bn2;
+  int outer = 0;
+  while (outer < c->max_outer && rn2 > tol * tol * bn2) {
+    launch_to32(n, c->r64.p, B.b, s);
+    double need = tol * std::sqrt(bn2 / rn2);
+    double tin = std::max(c->inner_tol, 0.3 * need);
+    int it = run_krylov(c, H, B, tr, 0, tin, &done);
+    c->stats.iterations += it;
+    launch_add32(n, x, B.x, s);
+    rn2 = reduce_norm2_residual(c, H, tr, b, x, c->r64.as<cd>());
+    outer++;
+    if (done == 3 && it == 0) break;
+  }
+  c->stats.outer_steps += outer;
+  c->stats.rel_residual = bn2 > 0 ? std::sqrt(rn2 / bn2) : 0.0;
+  if (rn2 > tol * tol * bn2) c->stats.converged = 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// Geometry / mesh
+// ------------------------------------------------------------------------------------------
+void upload_points(ac3d_ctx* c, const std::vector<double>& Ps) {
+  cudaStream_t s = c->stream;
+  c->G.P.ensure(Ps.size() * sizeof(double), s);
+  AC3D_CUDA(cudaMemcpyAsync(c->G.P.p, Ps.data(), Ps.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_geometry(c->G, s);
+}
+
+std::vector<double> heights_to_points(ac3d_ctx* c, const double* x) {
+  std::vector<double> Ps = c->Ps0;
+  if (x)
+    for (const auto& kv : c->Hs) Ps[3 * (size_t)kv.first + 1] = x[kv.second] + c->Ps0[3 * (size_t)kv.first + 1];
+  return Ps;
+}
+
+void upload_receivers(ac3d_ctx* c, const double* L, int n, DevBuf& dst) {
+  std::vector<double> v(4 * (size_t)n);
+  for (int i = 0; i < n; i++) {
+    v[4 * i] = L[3 * i];
+    v[4 * i + 1] = L[3 * i + 1];
+    v[4 * i + 2] = L[3 * i + 2];
+    v[4 * i + 3] = 0;
+  }
+  upload(dst, v, c->stream);
+}
+
+// Receiver matrix by ACA (reference mode, compute_ACA_listener, aca.cpp:84-134).
+struct ListenerLR {
+  DevBuf pool, toff, rank, used, blk, ord, pts, t;
+  int L = 0, iter_lim = 0;
+};
+
+std::unique_ptr<ListenerLR> listener_lr(ac3d_ctx* c, double k, const double* Lh, int L) {
+  cudaStream_t s = c->stream;
+  auto Q = std::make_unique<ListenerLR>();
+  Q->L = L;
+  const int maxk = 5000;  // Q_ACA_MAX_K (constants.h:17)
+  Q->iter_lim = std::max(1, std::min(maxk, std::min(L - 1, c->Ne - 1)));
+  const size_t cs = c->prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
+  const long long cap = (long long)Q->iter_lim * (L + c->Ne);
+  Q->pool.alloc((size_t)cap * cs, s);
+  Q->toff.alloc((size_t)Q->iter_lim * sizeof(long long), s);
+  Q->rank.alloc(sizeof(int), s);
+  Q->used.alloc(16, s);
+  Q->t.alloc((size_t)Q->iter_lim * sizeof(cd), s);
+  AC3D_CUDA(cudaMemsetAsync(Q->used.p, 0, 16, s));
+  upload(Q->blk, std::vector<int>{0, L, 0, c->Ne}, s);
+  upload(Q->ord, std::vector<int>{0}, s);
+  if (c->prec == PREC_FP64) {
+    std::vector<double> v(4 * (size_t)L);
+    for (int i = 0; i < L; i++)
+      for (int d = 0; d < 3; d++) v[4 * i + d] = Lh[3 * i + d];
+    upload(Q->pts, v, s);
+  } else {
+    std::vector<float> v(4 * (size_t)L, 0.f);
+    for (int i = 0; i < L; i++)
+      for (int d = 0; d < 3; d++) v[4 * i + d] = (float)Lh[3 * i + d];
+    upload(Q->pts, v, s);
+  }
+  launch_listener_aca(c->G, c->prec, Q->pts.p, L, k, c->q_tol, maxk, Q->pool.p, cap,
+                      Q->used.as<unsigned long long>(), Q->toff.as<long long>(), Q->rank.as<int>(),
+                      (int*)(Q->used.as<unsigned long long>() + 1), Q->blk.as<int4>(), Q->ord.as<int>(), s);
+  return Q;
+}
+
+void listener_apply(ac3d_ctx* c, const ListenerLR& Q, const cd* in, cd* out, bool trans) {
+  launch_lr_apply(c->prec, Q.pool.p, Q.toff.as<long long>(), Q.rank.as<int>(), Q.iter_lim, Q.L, c->Ne, in,
+                  trans ? 1 : 0, Q.t.as<cd>(), out, c->stream);
+}
+
+// One frequency: assemble, solve -b, receivers. Keeps H if `keep`.
+std::unique_ptr<DevHMat> forward_one(ac3d_ctx* c, double f, const double4* recv, const double* Lh, int L, cd* x_out,
+                                     cd* y_out, bool keep, std::unique_ptr<ListenerLR>* q_keep = nullptr) {
+  cudaStream_t s = c->stream;
+  const double k = wavenumber(f);
+  GpuTimer ta(s);
+  auto H = assemble(c, k, c->prec);
+  c->stats.ms_assemble += ta.stop();
+  ensure_work(c);
+  // b = -incident field (the system is (K - I/2) x = -b, adjoint.cpp:95)
+  GpuTimer ts(s);
+  launch_rhs(c->G, 1, k, c->src_kind, c->src, c->b64.p, s);
+  launch_negate64(c->Ne, c->b64.p, s);
+  solve(c, *H, c->b64.as<cd>(), x_out, false);
+  c->stats.solves++;
+  c->stats.ms_solve += ts.stop();
+  if (y_out) {
+    GpuTimer tl(s);
+    if (c->listener_mode == AC3D_LISTENER_ACA) {
+      auto Q = listener_lr(c, k, Lh, L);
+      listener_apply(c, *Q, x_out, y_out, false);
+      if (q_keep) *q_keep = std::move(Q);
+    } else {
+      launch_far_field(c->G, c->prec, recv, L, k, x_out, y_out, c->ff_scratch, s);
+    }
+    c->stats.ms_listener += tl.stop();
+  }
+  if (!keep) H.reset();
+  return H;
+}
+
+// bem3d::gradient (adjoint.cpp:24-242) for one band at the geometry currently on the device.
+double band_eval(ac3d_ctx* c, double band, bool forward_only, double* grad_dev) {
+  cudaStream_t s = c->stream;
+  const int L = (int)c->Ls.size() / 3;
+  const int n = c->Ne;
+  auto freqs = frequencies(band, c->n_freqs);
+  const int F = (int)freqs.size();
+  DevBuf xs, ys, yt, u, coef, vf, adjb, lmb;
+  xs.alloc((size_t)F * n * sizeof(cd), s);
+  ys.alloc((size_t)F * L * sizeof(cd), s);
+  yt.alloc((size_t)L * sizeof(double), s);
+  u.alloc((size_t)L * sizeof(double), s);
+  coef.alloc(16, s);
+  AC3D_CUDA(cudaMemsetAsync(yt.p, 0, (size_t)L * sizeof(double), s));
+  std::vector<std::unique_ptr<DevHMat>> saved(F);
+  std::vector<std::unique_ptr<ListenerLR>> savedQ(F);
+  const bool keep = !forward_only && !c->recompute;
+  for (int fi = 0; fi < F; fi++) {
+    cd* xf = xs.as<cd>() + (size_t)fi * n;
+    cd* yf = ys.as<cd>() + (size_t)fi * L;
+    saved[fi] = forward_one(c, freqs[fi], c->Ls_dev.as<double4>(), c->Ls.data(), L, xf, yf, keep,
+                            keep ? &savedQ[fi] : nullptr);
+    launch_accum_abs(yf, L, yt.as<double>(), s);
+  }
+  launch_compute_u(yt.as<double>(), L, u.as<double>(), coef.as<double>(), s);
+  double cval = 0;
+  AC3D_CUDA(cudaMemcpyAsync(&cval, coef.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  if (forward_only) return cval;
+
+  GpuTimer tadj(s);
+  vf.alloc((size_t)L * sizeof(cd), s);
+  adjb.alloc((size_t)n * sizeof(cd), s);
+  lmb.alloc((size_t)n * sizeof(cd), s);
+  for (int fi = 0; fi < F; fi++) {
+    const double k = wavenumber(freqs[fi]);
+    cd* xf = xs.as<cd>() + (size_t)fi * n;
+    cd* yf = ys.as<cd>() + (size_t)fi * L;
+    launch_vf(u.as<double>(), yf, L, vf.as<cd>(), s);
+    if (c->listener_mode == AC3D_LISTENER_ACA) {
+      std::unique_ptr<ListenerLR> Q = std::move(savedQ[fi]);
+      if (!Q) Q = listener_lr(c, k, c->Ls.data(), L);  // recompute (adjoint.cpp:177-178)
+      listener_apply(c, *Q, vf.as<cd>(), adjb.as<cd>(), true);
+    } else {
+      launch_far_field_t(c->G, c->prec, c->Ls_dev.as<double4>(), L, k, vf.as<cd>(), adjb.as<cd>(), s);
+    }
+    std::unique_ptr<DevHMat> H = std::move(saved[fi]);
+    if (!H) H = assemble(c, k, c->prec);  // recompute_matrices (adjoint.cpp:173-195)
+    solve(c, *H, adjb.as<cd>(), lmb.as<cd>(), true);
+    c->stats.solves++;
+    H.reset();
+    AdjointArgs a{};
+    a.prec = c->prec;
+    a.k = k;
+    a.npairs = (int)c->pair_elem.size();
+    a.pair_elem = c->d_pair_elem.as<int>();
+    a.pair_corner = c->d_pair_corner.as<int>();
+    a.ntouch = (int)c->touch.size();
+    a.touch_elem = c->d_touch.as<int>();
+    a.pair_touch = c->d_pair_touch.as<int>();
+    a.recv = c->Ls_dev.as<double4>();
+    a.L = L;
+    a.vf = vf.as<cd>();
+    a.x = xf;
+    a.lmb = lmb.as<cd>();
+    a.rhs_kind = c->src_kind;
+    for (int d = 0; d < 3; d++) a.rhs_v[d] = c->src[d];
+    a.h_off = c->d_h_off.as<int>();
+    a.HH = (int)c->h_off.size() - 1;
+    a.grad = grad_dev;
+    launch_adjoint_terms(c->G, a, c->adj_scratch, s);
+  }
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  c->stats.ms_adjoint += tadj.stop();
+  return cval;
+}
+
+void reset_stats(ac3d_ctx* c) {
+  ac3d_stats z{};
+  z.n_elements = c->Ne;
+  z.n_direct = c->DP.nd;
+  z.n_approx = c->DP.na;
+  z.n_leaves = c->DP.nleaf;
+  z.converged = 1;
+  c->stats = z;
+}
+
+template <typename F>
+int guard(ac3d_ctx* c, F&& f) {
+  if (!c) return AC3D_ERR_ARG;
+  try {
+    c->err.clear();
+    auto t0 = std::chrono::steady_clock::now();
+    f();
+    c->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return AC3D_OK;
+  } catch (const Error& e) {
+    c->err = e.what();
+    if (e.code == AC3D_ERR_CUDA) cudaGetLastError();
+    return e.code;
+  } catch (const std::exception& e) {
+    c->err = e.what();
+    return AC3D_ERR_INTERNAL;
+  }
+}
+
+}  // namespace
+
+// ============================================================================================
+// C-ABI
+// ============================================================================================
+extern "C" {
+
+const char* ac3d_version(void) { return "acoustic_reliefs_gb300 0.1 (sm_103a)"; }
+
+int ac3d_create(ac3d_ctx** out, int cluster_size, double radius_factor, const double* freq_bands, int n_bands,
+                int n_freqs, double approx_aca_tol, double q_aca_tol, double solver_tol, const double* src_pt,
+                double listener_radius, double listener_ds, int recompute_matrices) {
+  if (!out) return AC3D_ERR_ARG;
+  *out = nullptr;
+  if (cluster_size < 1 || cluster_size > 256 || n_freqs < 1 || n_bands < 0 || (n_bands > 0 && !freq_bands) ||
+      listener_ds <= 0 || !(solver_tol > 0) || !(approx_aca_tol >= 0))
+    return AC3D_ERR_ARG;
+  ac3d_ctx* c = new ac3d_ctx;
+  c->cluster_size = cluster_size;
+  c->radius_factor = radius_factor;
+  c->bands.assign(freq_bands, freq_bands + n_bands);
+  c->n_freqs = n_freqs;
+  c->aca_tol = approx_aca_tol;
+  c->q_tol = q_aca_tol;
+  c->solver_tol = solver_tol;
+  if (src_pt)
+    for (int d = 0; d < 3; d++) c->src[d] = src_pt[d];
+  c->listener_radius = listener_radius;
+  c->listener_ds = listener_ds;
+  c->recompute = recompute_matrices != 0;
+  c->Ls = hemisphere(listener_radius, listener_ds);
+  int rc = guard(c, [&] {
+    AC3D_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    int dev = 0;
+    AC3D_CUDA(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    AC3D_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t thr = UINT64_MAX;
+    AC3D_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    upload_receivers(c, c->Ls.data(), (int)c->Ls.size() / 3, c->Ls_dev);
+    AC3D_CUDA(cudaStreamSynchronize(c->stream));
+  });
+  if (rc != AC3D_OK) {
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return AC3D_OK;
+}
+
+void ac3d_destroy(ac3d_ctx* c) {
+  if (!c) return;
+  try {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+  } catch (...) {
+  }
+  cudaStream_t s = c->stream;
+  {
+    // release device buffers before the stream goes away
+    DevBuf* bufs[] = {&c->kv, &c->partials, &c->kstate, &c->red, &c->b64, &c->x64, &c->r64, &c->ff_scratch,
+                      &c->adj_scratch, &c->tmp_recv, &c->Ls_dev, &c->d_h_off, &c->d_pair_elem, &c->d_pair_corner,
+                      &c->d_pair_touch, &c->d_touch};
+    for (DevBuf* b : bufs) b->release();
+    c->DP = DevPartition();
+    c->G = DevGeometry();
+  }
+  if (s) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  delete c;
+}
+
+const char* ac3d_last_error(const ac3d_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int ac3d_set_precision(ac3d_ctx* c, int p) {
+  if (!c || (p != AC3D_PREC_MIXED && p != AC3D_PREC_FP64)) return AC3D_ERR_ARG;
+  c->prec = p;
+  return AC3D_OK;
+}
+
+int ac3d_set_incident(ac3d_ctx* c, int kind, const double* v) {
+  if (!c || !v || (kind != AC3D_INCIDENT_POINT && kind != AC3D_INCIDENT_PLANE)) return AC3D_ERR_ARG;
+  c->src_kind = kind;
+  double nrm = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  for (int d = 0; d < 3; d++) c->src[d] = kind == AC3D_INCIDENT_PLANE ? v[d] / nrm : v[d];
+  return AC3D_OK;
+}
+
+int ac3d_set_listener_mode(ac3d_ctx* c, int mode) {
+  if (!c || (mode != AC3D_LISTENER_DENSE && mode != AC3D_LISTENER_ACA)) return AC3D_ERR_ARG;
+  c->listener_mode = mode;
+  return AC3D_OK;
+}
+
+int ac3d_set_solver(ac3d_ctx* c, int max_iterations, double inner_tol, int max_outer) {
+  if (!c || max_iterations < 0 || !(inner_tol > 0 && inner_tol < 1) || max_outer < 1) return AC3D_ERR_ARG;
+  c->maxit = max_iterations;
+  c->inner_tol = inner_tol;
+  c->max_outer = max_outer;
+  return AC3D_OK;
+}
+
+int ac3d_set_listeners(ac3d_ctx* c, const double* Ls, int L) {
+  if (!c || !Ls || L < 2) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    c->Ls.assign(Ls, Ls + 3 * (size_t)L);
+    upload_receivers(c, Ls, L, c->Ls_dev);
+    AC3D_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int Ne, int32_t* Es_out) {
+  if (!c || !Ps || !Es || V < 3 || Ne < 1) return AC3D_ERR_ARG;
+  for (int i = 0; i < 3 * Ne; i++)
+    if (Es[i] < 0 || Es[i] >= V) {
+      c->err = "element index out of range";
+      return AC3D_ERR_ARG;
+    }
+  for (int i = 0; i < 3 * V; i++)
+    if (!std::isfinite(Ps[i])) {
+      c->err = "non-finite vertex coordinate";
+      return AC3D_ERR_ARG;
+    }
+  return guard(c, [&] {
+    cudaStream_t s = c->stream;
+    c->mesh_set = false;
+    c->diff_set = false;
+    c->V = V;
+    c->Ne = Ne;
+    c->Ps0.assign(Ps, Ps + 3 * (size_t)V);
+    // centroids in the input order (compute_centers, helpers.cpp:7-14)
+    std::vector<double> C(3 * (size_t)Ne);
+    for (int e = 0; e < Ne; e++)
+      for (int d = 0; d < 3; d++)
+        C[3 * e + d] = (Ps[3 * Es[3 * e] + d] + Ps[3 * Es[3 * e + 1] + d] + Ps[3 * Es[3 * e + 2] + d]) / 3;
+    build_partition(C.data(), Ne, c->cluster_size, c->radius_factor, c->P);
+    if (c->P.max_leaf > 256) throw Error(AC3D_ERR_ARG, "leaf clusters above 256 elements are not supported");
+    c->Es.resize(3 * (size_t)Ne);
+    for (int i = 0; i < Ne; i++)
+      for (int d = 0; d < 3; d++) c->Es[3 * i + d] = Es[3 * c->P.order[i] + d];
+    build_leaf_lists(c->P, c->maxk);
+    // ClusterTree::check (clustertree.cpp:33-47) on the reordered centroids
+    for (int e = 0; e < Ne; e++)
+      for (int d = 0; d < 3; d++)
+        C[3 * e + d] =
+            (Ps[3 * c->Es[3 * e] + d] + Ps[3 * c->Es[3 * e + 1] + d] + Ps[3 * c->Es[3 * e + 2] + d]) / 3;
+    c->P.tree_ok = true;
+    for (const TreeNode& nd : c->P.nodes)
+      for (int i = nd.s; i < nd.e; i++) {
+        double dx = C[3 * i] - nd.c[0], dy = C[3 * i + 1] - nd.c[1], dz = C[3 * i + 2] - nd.c[2];
+        if (!(std::sqrt(dx * dx + dy * dy + dz * dz) <= nd.r + 1e-6)) c->P.tree_ok = false;
+      }
+    // device partition
+    DevPartition& DP = c->DP;
+    DP.nleaf = (int)c->P.leaf_start.size() - 1;
+    DP.nd = (int)c->P.direct.size() / 4;
+    DP.na = (int)c->P.approx.size() / 4;
+    upload(DP.blocks_d, c->P.direct, s);
+    upload(DP.blocks_a, c->P.approx, s);
+    upload(DP.leaf_start, c->P.leaf_start, s);
+    upload(DP.fw_near_ptr, c->P.fw_near_ptr, s);
+    upload(DP.fw_near, c->P.fw_near, s);
+    upload(DP.fw_lr_ptr, c->P.fw_lr_ptr, s);
+    upload(DP.fw_lr, c->P.fw_lr, s);
+    upload(DP.tr_near_ptr, c->P.tr_near_ptr, s);
+    upload(DP.tr_near, c->P.tr_near, s);
+    upload(DP.tr_lr_ptr, c->P.tr_lr_ptr, s);
+    upload(DP.tr_lr, c->P.tr_lr, s);
+    std::vector<long long> no(c->P.near_off.begin(), c->P.near_off.end());
+    upload(DP.near_off, no, s);
+    upload(DP.aca_order, c->P.aca_order, s);
+    c->sum_mn = 0;
+    c->worst_pool = 0;
+    for (int b = 0; b < DP.na; b++) {
+      const int* q = &c->P.approx[4 * b];
+      int m = q[1] - q[0], n = q[3] - q[2];
+      c->sum_mn += m + n;
+      c->worst_pool += (int64_t)std::max(0, std::min(c->maxk, std::min(m - 1, n - 1))) * (m + n);
+    }
+    c->pool_hint[0] = c->pool_hint[1] = 0;
+    // geometry
+    c->G.ne = Ne;
+    c->G.nv = V;
+    upload(c->G.E, c->Es, s);
+    upload_points(c, c->Ps0);
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    c->mesh_set = true;
+    reset_stats(c);
+    if (Es_out) std::memcpy(Es_out, c->Es.data(), c->Es.size() * sizeof(int32_t));
+  });
+}
+
+int ac3d_set_diff_points(ac3d_ctx* c, const int32_t* pts, int HH) {
+  if (!c || (HH > 0 && !pts) || HH < 0) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    cudaStream_t s = c->stream;
+    c->Hs.clear();
+    c->diff_pts.assign(pts, pts + HH);
+    int h = 0;
+    for (int i = 0; i < HH; i++) {
+      if (pts[i] < 0 || pts[i] >= c->V) throw Error(AC3D_ERR_ARG, "differentiable point index out of range");
+      c->Hs[pts[i]] = h++;  // later duplicates overwrite, as std::unordered_map::operator[] does
+    }
+    // incidence lists (acoustics3d.cpp:79-98): for each element j, corners 0..2
+    std::vector<std::vector<std::pair<int, int>>> lists(HH);
+    for (int j = 0; j < c->Ne; j++)
+      for (int o = 0; o < 3; o++) {
+        auto it = c->Hs.find(c->Es[3 * j + o]);
+        if (it != c->Hs.end()) lists[it->second].push_back({j, o});
+      }
+    c->h_off.assign(HH + 1, 0);
+    c->pair_elem.clear();
+    c->pair_corner.clear();
+    for (int i = 0; i < HH; i++) {
+      for (auto& pr : lists[i]) {
+        c->pair_elem.push_back(pr.first);
+        c->pair_corner.push_back(pr.second);
+      }
+      c->h_off[i + 1] = (int)c->pair_elem.size();
+    }
+    std::vector<int> tid(c->Ne, -1);
+    c->touch.clear();
+    c->pair_touch.resize(c->pair_elem.size());
+    for (size_t t = 0; t < c->pair_elem.size(); t++) {
+      int e = c->pair_elem[t];
+      if (tid[e] < 0) {
+        tid[e] = (int)c->touch.size();
+        c->touch.push_back(e);
+      }
+      c->pair_touch[t] = tid[e];
+    }
+    upload(c->d_h_off, c->h_off, s);
+    upload(c->d_pair_elem, c->pair_elem, s);
+    upload(c->d_pair_corner, c->pair_corner, s);
+    upload(c->d_pair_touch, c->pair_touch, s);
+    upload(c->d_touch, c->touch, s);
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    c->diff_set = true;
+  });
+}
+
+int ac3d_set_band(ac3d_ctx* c, double fb) {
+  if (!c) return AC3D_ERR_ARG;
+  c->bands.assign(1, fb);
+  return AC3D_OK;
+}
+
+int ac3d_set_bands(ac3d_ctx* c, const double* fb, int n) {
+  if (!c || n < 1 || !fb) return AC3D_ERR_ARG;
+  c->bands.assign(fb, fb + n);
+  return AC3D_OK;
+}
+
+int ac3d_num_listeners(const ac3d_ctx* c, int* L) {
+  if (!c || !L) return AC3D_ERR_ARG;
+  *L = (int)c->Ls.size() / 3;
+  return AC3D_OK;
+}
+
+int ac3d_get_listeners(const ac3d_ctx* c, double* out) {
+  if (!c || !out) return AC3D_ERR_ARG;
+  std::memcpy(out, c->Ls.data(), c->Ls.size() * sizeof(double));
+  return AC3D_OK;
+}
+
+int ac3d_set_points(ac3d_ctx* c, const double* Ps) {
+  if (!c || !Ps) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    c->Ps0.assign(Ps, Ps + 3 * (size_t)c->V);
+    upload_points(c, c->Ps0);
+  });
+}
+
+int ac3d_pressures(ac3d_ctx* c, double f, const double* Ls, int L, double* out) {
+  if (!c || !out || !(f > 0) || (Ls && L < 1)) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    reset_stats(c);
+    cudaStream_t s = c->stream;
+    upload_points(c, c->Ps0);
+    const double4* recv = c->Ls_dev.as<double4>();
+    const double* Lh = c->Ls.data();
+    int nL = (int)c->Ls.size() / 3;
+    if (Ls) {
+      Lh = Ls;
+      upload_receivers(c, Ls, L, c->tmp_recv);
+      recv = c->tmp_recv.as<double4>();
+      nL = L;
+    }
+    ensure_work(c);
+    DevBuf y;
+    y.alloc((size_t)nL * sizeof(cd), s);
+    forward_one(c, f, recv, Lh, nL, c->x64.as<cd>(), y.as<cd>(), false);
+    AC3D_CUDA(cudaMemcpyAsync(out, y.p, (size_t)nL * sizeof(cd), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+  });
+}
+
+int ac3d_surface_values(ac3d_ctx* c, double f, double* out) {
+  if (!c || !out || !(f > 0)) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    reset_stats(c);
+    cudaStream_t s = c->stream;
+    upload_points(c, c->Ps0);
+    ensure_work(c);
+    forward_one(c, f, nullptr, nullptr, 0, c->x64.as<cd>(), nullptr, false);
+    AC3D_CUDA(cudaMemcpyAsync(out, c->x64.p, (size_t)c->Ne * sizeof(cd), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+  });
+}
+
+int ac3d_band_value(ac3d_ctx* c, double fb, double* cv) {
+  if (!c || !cv) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    reset_stats(c);
+    upload_points(c, c->Ps0);
+    *cv = band_eval(c, fb, true, nullptr);
+  });
+}
+
+int ac3d_values(ac3d_ctx* c, double* out) {
+  if (!c || !out) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    reset_stats(c);
+    upload_points(c, c->Ps0);
+    for (size_t b = 0; b < c->bands.size(); b++) out[b] = band_eval(c, c->bands[b], true, nullptr);
+  });
+}
+
+int ac3d_value(ac3d_ctx* c, const double* x, double* cv) {
+  if (!c || !cv) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    reset_stats(c);
+    upload_points(c, heights_to_points(c, x));
+    double acc = 0;
+    for (double fb : c->bands) acc += band_eval(c, fb, true, nullptr);
+    *cv = acc / (double)c->bands.size();
+  });
+}
+
+int ac3d_gradient(ac3d_ctx* c, const double* x, double* cv, double* grad) {
+  if (!c || !x || !cv || !grad) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    if (!c->diff_set)
+      throw Error(AC3D_ERR_STATE, "No differentiable points set. Set them using set_diff_pts or precompute.");
+    reset_stats(c);
+    cudaStream_t s = c->stream;
+    upload_points(c, heights_to_points(c, x));
+    const int HH = (int)c->h_off.size() - 1;
+    DevBuf g;
+    g.alloc((size_t)std::max(HH, 1) * sizeof(double), s);
+    AC3D_CUDA(cudaMemsetAsync(g.p, 0, (size_t)std::max(HH, 1) * sizeof(double), s));
+    double acc = 0;
+    for (double fb : c->bands) acc += band_eval(c, fb, false, g.as<double>());
+    AC3D_CUDA(cudaMemcpyAsync(grad, g.p, (size_t)HH * sizeof(double), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    *cv = acc;
+  });
+}
+
+int ac3d_value_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, void* stream) {
+  if (!c || !c_dev) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    cudaStream_t us = (cudaStream_t)stream;
+    cudaStream_t s = c->stream;
+    cudaEvent_t ev;
+    AC3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    AC3D_CUDA(cudaEventRecord(ev, us));
+    AC3D_CUDA(cudaStreamWaitEvent(s, ev, 0));
+    std::vector<double> x;
+    if (x_dev) {
+      const int HH = (int)c->diff_pts.size();
+      x.resize(HH);
+      AC3D_CUDA(cudaMemcpyAsync(x.data(), x_dev, HH * sizeof(double), cudaMemcpyDeviceToHost, s));
+      AC3D_CUDA(cudaStreamSynchronize(s));
+    }
+    reset_stats(c);
+    upload_points(c, heights_to_points(c, x_dev ? x.data() : nullptr));
+    double acc = 0;
+    for (double fb : c->bands) acc += band_eval(c, fb, true, nullptr);
+    acc /= (double)c->bands.size();
+    AC3D_CUDA(cudaMemcpyAsync(c_dev, &acc, sizeof(double), cudaMemcpyHostToDevice, s));
+    AC3D_CUDA(cudaEventRecord(ev, s));
+    AC3D_CUDA(cudaStreamWaitEvent(us, ev, 0));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    AC3D_CUDA(cudaEventDestroy(ev));
+  });
+}
+
+int ac3d_gradient_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, double* g_dev, void* stream) {
+  if (!c || !x_dev || !c_dev || !g_dev) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    if (!c->diff_set)
+      throw Error(AC3D_ERR_STATE, "No differentiable points set. Set them using set_diff_pts or precompute.");
+    cudaStream_t us = (cudaStream_t)stream;
+    cudaStream_t s = c->stream;
+    cudaEvent_t ev;
+    AC3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    AC3D_CUDA(cudaEventRecord(ev, us));
+    AC3D_CUDA(cudaStreamWaitEvent(s, ev, 0));
+    const int HH = (int)c->h_off.size() - 1;
+    std::vector<double> x(HH);
+    AC3D_CUDA(cudaMemcpyAsync(x.data(), x_dev, HH * sizeof(double), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    reset_stats(c);
+    upload_points(c, heights_to_points(c, x.data()));
+    AC3D_CUDA(cudaMemsetAsync(g_dev, 0, (size_t)HH * sizeof(double), s));
+    double acc = 0;
+    for (double fb : c->bands) acc += band_eval(c, fb, false, g_dev);
+    AC3D_CUDA(cudaMemcpyAsync(c_dev, &acc, sizeof(double), cudaMemcpyHostToDevice, s));
+    AC3D_CUDA(cudaEventRecord(ev, s));
+    AC3D_CUDA(cudaStreamWaitEvent(us, ev, 0));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    AC3D_CUDA(cudaEventDestroy(ev));
+  });
+}
+
+int ac3d_sphere(const double* Ps, int V, const int32_t* Es, int Ne, double freq, int LL, double lrad, int precision,
+                double* out) {
+  if (!Ps || !Es || !out || LL < 1) return AC3D_ERR_ARG;
+  const double band = freq;
+  const double src[3] = {1.0, 0.0, 0.0};
+  ac3d_ctx* c = nullptr;
+  // sphere.h:32,43,51: leaf 128, factor 1.5, tolerances 1e-10
+  int rc = ac3d_create(&c, 128, 1.5, &band, 1, 1, 1e-10, 1e-10, 1e-10, src, 1.0, 5.0, 0);
+  if (rc) return rc;
+  std::vector<int32_t> Eo(3 * (size_t)Ne);
+  std::vector<double> L(3 * (size_t)LL, 0.0);
+  for (int l = 0; l < LL; l++) {  // sphere.h:58-63
+    double th = (double)l / (double)LL * 2 * kPiHost;
+    L[3 * l] = lrad * std::cos(th);
+    L[3 * l + 2] = -lrad * std::sin(th);
+  }
+  if (!(rc = ac3d_set_precision(c, precision)) && !(rc = ac3d_set_incident(c, AC3D_INCIDENT_PLANE, src)) &&
+      !(rc = ac3d_set_mesh(c, Ps, V, Es, Ne, Eo.data())))
+    rc = ac3d_pressures(c, freq, L.data(), LL, out);
+  ac3d_destroy(c);
+  return rc;
+}
+
+struct ac3d_partition {
+  ac3d::Partition P;
+};
+
+int ac3d_partition_build(const double* Ps, int V, const int32_t* Es, int Ne, int cluster_size, double radius_factor,
+                         ac3d_partition** out) {
+  if (!Ps || !Es || !out || V < 3 || Ne < 1 || cluster_size < 1) return AC3D_ERR_ARG;
+  for (int i = 0; i < 3 * Ne; i++)
+    if (Es[i] < 0 || Es[i] >= V) return AC3D_ERR_ARG;
+  try {
+    auto* p = new ac3d_partition;
+    std::vector<double> C(3 * (size_t)Ne);
+    for (int e = 0; e < Ne; e++)
+      for (int d = 0; d < 3; d++)
+        C[3 * e + d] = (Ps[3 * Es[3 * e] + d] + Ps[3 * Es[3 * e + 1] + d] + Ps[3 * Es[3 * e + 2] + d]) / 3;
+    build_partition(C.data(), Ne, cluster_size, radius_factor, p->P);
+    // ClusterTree::check on the reordered centroids
+    std::vector<double> Cr(3 * (size_t)Ne);
+    for (int i = 0; i < Ne; i++)
+      for (int d = 0; d < 3; d++) Cr[3 * i + d] = C[3 * p->P.order[i] + d];
+    for (const TreeNode& nd : p->P.nodes)
+      for (int i = nd.s; i < nd.e; i++) {
+        double dx = Cr[3 * i] - nd.c[0], dy = Cr[3 * i + 1] - nd.c[1], dz = Cr[3 * i + 2] - nd.c[2];
+        if (!(std::sqrt(dx * dx + dy * dy + dz * dz) <= nd.r + 1e-6)) p->P.tree_ok = false;
+      }
+    *out = p;
+    return AC3D_OK;
+  } catch (...) {
+    return AC3D_ERR_INTERNAL;
+  }
+}
+
+int ac3d_partition_counts(const ac3d_partition* p, int* nd, int* na, int* nl, int* ok) {
+  if (!p) return AC3D_ERR_ARG;
+  if (nd) *nd = (int)p->P.direct.size() / 4;
+  if (na) *na = (int)p->P.approx.size() / 4;
+  if (nl) *nl = (int)p->P.leaf_start.size() - 1;
+  if (ok) *ok = p->P.tree_ok ? 1 : 0;
+  return AC3D_OK;
+}
+
+int ac3d_partition_get(const ac3d_partition* p, int32_t* order, int32_t* direct, int32_t* approx, int32_t* leaves) {
+  if (!p) return AC3D_ERR_ARG;
+  if (order) std::copy(p->P.order.begin(), p->P.order.end(), order);
+  if (direct) std::copy(p->P.direct.begin(), p->P.direct.end(), direct);
+  if (approx) std::copy(p->P.approx.begin(), p->P.approx.end(), approx);
+  if (leaves) std::copy(p->P.leaf_start.begin(), p->P.leaf_start.end(), leaves);
+  return AC3D_OK;
+}
+
+void ac3d_partition_free(ac3d_partition* p) { delete p; }
+
+int ac3d_get_stats(const ac3d_ctx* c, ac3d_stats* out) {
+  if (!c || !out) return AC3D_ERR_ARG;
+  *out = c->stats;
+  return AC3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,343 @@
+// H-matrix assembly on the GPU: near-field quadrature and partially pivoted ACA.
+//
+// Near field (compute_block, integrate.cpp:87-100; hmatrix.cpp:20-44): one CTA per dense block,
+// one thread per entry, 6-point rule, displacement formed in FP64. Storage is column-major per
+// block (entry (r, c) at c * m + r), blocks packed back to back.
+//
+// ACA (compute_ACA_block, aca.cpp:38-82, with argmax rules aca.cpp:9-36): one CTA per admissible
+// block. The sequence of the reference is kept exactly: first row pivot 0; v = row - U(i,:) V;
+// column pivot j = first index of max |v|^2; V row = v / v_j (v itself when v_j == 0 and the zero
+// guard is on); u = column - U V(:, j); err += |u|^2 |v|^2 + 2 sum_q |u^T U_q| |v V_q^T| (plain,
+// non-conjugated products); stop when sqrt(|u|^2 |v|^2 / err) <= eps, dropping the converging
+// term; next row pivot = first max of |u|^2 over rows not used yet. Each rank-1 term (u | v) is
+// bump-allocated from one pool with an atomic counter, so storage is proportional to the actual
+// ranks; the pool offset of term q of block b is term_off[b * maxk + q].
+#include "common.cuh"
+#include "internal.h"
+#include "listener.h"
+
+#include <algorithm>
+
+namespace ac3d {
+
+namespace {
+constexpr int kAcaThreads = 256;
+constexpr int kAcaWarps = kAcaThreads / 32;
+}  // namespace
+
+template <typename R>
+__global__ void __launch_bounds__(256) near_kernel(GeoView<R> G, const int4* __restrict__ blocks,
+                                                   const long long* __restrict__ near_off, R k, cplx<R>* out) {
+  const int b = blockIdx.x;
+  const int4 q = blocks[b];
+  const int m = q.y - q.x, n = q.w - q.z;
+  cplx<R>* dst = out + near_off[b];
+  const int mn = m * n;
+  for (int t = threadIdx.x; t < mn; t += blockDim.x) {
+    int c = t / m, r = t - c * m;
+    dst[t] = entry_near<R>(k, G, G.cen[q.x + r], q.z + c);
+  }
+}
+
+// Block-wide argmax of (value, index): larger value wins, smaller index on ties. Threads start
+// from (-1, 0) and skip NaN values, which reproduces a sequential scan with a strict `>` from -1.
+template <typename R>
+__device__ __forceinline__ void block_argmax(R& val, int& idx, R* sv, int* si) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    R ov = __shfl_xor_sync(0xffffffffu, val, o);
+    int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ov > val || (ov == val && oi < idx)) {
+      val = ov;
+      idx = oi;
+    }
+  }
+  if (lane == 0) {
+    sv[w] = val;
+    si[w] = idx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    R bv = sv[0];
+    int bi = si[0];
+    for (int i = 1; i < kAcaWarps; i++)
+      if (sv[i] > bv || (sv[i] == bv && si[i] < bi)) {
+        bv = sv[i];
+        bi = si[i];
+      }
+    sv[0] = bv;
+    si[0] = bi;
+  }
+  __syncthreads();
+  val = sv[0];
+  idx = si[0];
+  __syncthreads();
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sd) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sd[w] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kAcaWarps; i++) s += sd[i];
+    sd[0] = s;
+  }
+  __syncthreads();
+  s = sd[0];
+  __syncthreads();
+  return s;
+}
+
+template <typename R, typename P4>
+struct AcaArgs {
+  GeoView<R> G;
+  const int4* blocks;
+  const int* order;
+  const P4* rowpts;
+  R k;
+  double eps;
+  int maxk;
+  int zero_guard;
+  int iter_cap;
+  cplx<R>* pool;
+  long long pool_cap;
+  unsigned long long* pool_used;
+  long long* term_off;
+  int* rank;
+  int* status;
+};
+
+template <typename R, typename P4>
+__global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ R s_rv[kAcaWarps];
+  __shared__ int s_ri[kAcaWarps];
+  __shared__ double s_d[kAcaWarps];
+  __shared__ long long s_base;
+  __shared__ int s_flag;
+
+  const int b = A.order[blockIdx.x];
+  const int4 q = A.blocks[b];
+  const int rs = q.x, cs = q.z, m = q.y - q.x, n = q.w - q.z;
+  int iter_lim = min(A.maxk, min(m - 1, n - 1));
+  if (iter_lim < 0) iter_lim = 0;
+  if (iter_lim > A.iter_cap) iter_lim = A.iter_cap;  // host guarantees iter_cap >= every iter_lim
+
+  cplx<R>* uq = (cplx<R>*)smem_raw;
+  cplx<R>* vq = uq + A.iter_cap;
+  long long* toff = (long long*)(vq + A.iter_cap);
+  unsigned* used = (unsigned*)(toff + A.iter_cap);
+
+  const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  for (int w = tid; w < (m + 31) / 32; w += T) used[w] = 0;
+  __syncthreads();
+  if (tid == 0) used[0] = 1u;
+  double err = 0;  // meaningful in thread 0
+  int i = 0, iter = 0;
+  __syncthreads();
+
+  while (iter < iter_lim) {
+    // --- allocate the storage of term `iter` ---------------------------------------------
+    if (tid == 0) {
+      unsigned long long need = (unsigned long long)(m + n);
+      unsigned long long base = atomicAdd(A.pool_used, need);
+      s_flag = (base + need > (unsigned long long)A.pool_cap) ? 1 : 0;
+      s_base = (long long)base;
+      if (s_flag) atomicOr(A.status, 1);
+    }
+    __syncthreads();
+    if (s_flag) break;
+    cplx<R>* unew = A.pool + s_base;
+    cplx<R>* vnew = unew + m;
+    for (int p = tid; p < iter; p += T) uq[p] = A.pool[toff[p] + i];
+    __syncthreads();
+
+    // --- row residual v = M(i, :) - U(i, :) V ---------------------------------------------
+    const P4 pi = A.rowpts[rs + i];
+    R best = R(-1);
+    int bidx = 0;
+    for (int c = tid; c < n; c += T) {
+      cplx<R> v = entry_far<R>(A.k, A.G, pi, cs + c);
+      for (int p = 0; p < iter; p++) cfms(v, uq[p], A.pool[toff[p] + m + c]);
+      vnew[c] = v;
+      R a = abs2(v);
+      if (a > best) {
+        best = a;
+        bidx = c;
+      }
+    }
+    block_argmax<R>(best, bidx, s_rv, s_ri);
+    const int j = bidx;
+    const cplx<R> vj = vnew[j];
+    for (int p = tid; p < iter; p += T) vq[p] = A.pool[toff[p] + m + j];
+    __syncthreads();
+    const bool keep = A.zero_guard && vj.re == R(0) && vj.im == R(0);
+    double vn = 0;
+    for (int c = tid; c < n; c += T) {
+      cplx<R> v = vnew[c];
+      if (!keep) v = cdiv(v, vj);
+      vnew[c] = v;
+      vn += (double)abs2(v);
+    }
+
+    // --- column residual u = M(:, j) - U V(:, j) ------------------------------------------
+    double un = 0;
+    for (int r = tid; r < m; r += T) {
+      cplx<R> u = entry_far<R>(A.k, A.G, A.rowpts[rs + r], cs + j);
+      for (int p = 0; p < iter; p++) cfms(u, A.pool[toff[p] + r], vq[p]);
+      unew[r] = u;
+      un += (double)abs2(u);
+    }
+    __syncthreads();
+
+    // --- cross terms sum_q |u^T U_q| |v V_q^T| (one warp per earlier term) ------------------
+    double dots = 0;
+    for (int p = warp; p < iter; p += kAcaWarps) {
+      const cplx<R>* Up = A.pool + toff[p];
+      const cplx<R>* Vp = Up + m;
+      cplx<R> ud(0, 0), vd(0, 0);
+      for (int r = lane; r < m; r += 32) cfma(ud, unew[r], Up[r]);
+      for (int c = lane; c < n; c += 32) cfma(vd, vnew[c], Vp[c]);
+      double udr = warp_sum((double)ud.re), udi = warp_sum((double)ud.im);
+      double vdr = warp_sum((double)vd.re), vdi = warp_sum((double)vd.im);
+      if (lane == 0) dots += sqrt(udr * udr + udi * udi) * sqrt(vdr * vdr + vdi * vdi);
+    }
+    un = block_sum(un, s_d);
+    vn = block_sum(vn, s_d);
+    dots = block_sum(dots, s_d);
+    if (tid == 0) {
+      err += un * vn + 2 * dots;
+      s_flag = (sqrt(un * vn / err) <= A.eps) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_flag) break;
+
+    // --- next row pivot: first max |u|^2 over unused rows --------------------------------
+    best = R(-1);
+    bidx = 0;
+    for (int r = tid; r < m; r += T) {
+      if ((used[r >> 5] >> (r & 31)) & 1u) continue;
+      R a = abs2(unew[r]);
+      if (a > best) {
+        best = a;
+        bidx = r;
+      }
+    }
+    block_argmax<R>(best, bidx, s_rv, s_ri);
+    i = bidx;
+    if (tid == 0) {
+      used[i >> 5] |= 1u << (i & 31);
+      toff[iter] = s_base;
+      A.term_off[(long long)b * A.maxk + iter] = s_base;
+    }
+    iter++;
+    __syncthreads();
+  }
+  if (tid == 0) A.rank[b] = iter;
+}
+
+__global__ void rank_scan_kernel(const int* __restrict__ rank, int na, int* t_off) {
+  __shared__ int sums[1024];
+  const int tid = threadIdx.x;
+  const int chunk = (na + 1023) / 1024;
+  const int s = min(na, tid * chunk), e = min(na, s + chunk);
+  int acc = 0;
+  for (int i = s; i < e; i++) acc += rank[i];
+  sums[tid] = acc;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    int v = tid >= o ? sums[tid - o] : 0;
+    __syncthreads();
+    sums[tid] += v;
+    __syncthreads();
+  }
+  int base = tid ? sums[tid - 1] : 0;
+  for (int i = s; i < e; i++) {
+    t_off[i] = base;
+    base += rank[i];
+  }
+  if (tid == 1023) t_off[na] = sums[1023];
+}
+
+template <typename R>
+GeoView<R> geo_view(const DevGeometry& G);
+template <>
+GeoView<float> geo_view<float>(const DevGeometry& G) {
+  return {G.cen.as<double4>(), G.va.as<double4>(), G.eg32.as<ElemGeo<float>>(), G.cen32.as<float4>(),
+          G.va32.as<float4>(), G.ne};
+}
+template <>
+GeoView<double> geo_view<double>(const DevGeometry& G) {
+  return {G.cen.as<double4>(), G.va.as<double4>(), G.eg64.as<ElemGeo<double>>(), G.cen32.as<float4>(),
+          G.va32.as<float4>(), G.ne};
+}
+
+void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s) {
+  if (DP.nd == 0) return;
+  if (H.prec == PREC_FP64)
+    near_kernel<double><<<DP.nd, 256, 0, s>>>(geo_view<double>(G), DP.blocks_d.as<int4>(),
+                                              DP.near_off.as<long long>(), H.k, H.near.as<cd>());
+  else
+    near_kernel<float><<<DP.nd, 256, 0, s>>>(geo_view<float>(G), DP.blocks_d.as<int4>(),
+                                             DP.near_off.as<long long>(), (float)H.k, H.near.as<cf>());
+  AC3D_CUDA(cudaGetLastError());
+}
+
+template <typename R, typename P4>
+static void aca_launch_t(const AcaArgs<R, P4>& a, int nblocks, int max_rows, cudaStream_t s) {
+  size_t smem = (size_t)a.iter_cap * (2 * sizeof(cplx<R>) + sizeof(long long)) + (size_t)((max_rows + 31) / 32) * 4;
+  if (smem > 48 * 1024) {
+    if (smem > 227 * 1024) throw Error(4, "ACA block too large for shared memory");
+    AC3D_CUDA(cudaFuncSetAttribute(aca_kernel<R, P4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  aca_kernel<R, P4><<<nblocks, kAcaThreads, smem, s>>>(a);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s) {
+  if (DP.na == 0) return;
+  int iter_cap = H.maxk;
+  if (H.prec == PREC_FP64) {
+    AcaArgs<double, double4> a{geo_view<double>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
+                               G.cen.as<double4>(), H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cd>(),
+                               H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
+                               H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
+    aca_launch_t(a, DP.na, max_rows, s);
+  } else {
+    AcaArgs<float, float4> a{geo_view<float>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
+                             G.cen32.as<float4>(), (float)H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cf>(),
+                             H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
+                             H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
+    aca_launch_t(a, DP.na, max_rows, s);
+  }
+}
+
+void launch_rank_scan(const DevPartition& DP, DevHMat& H, cudaStream_t s) {
+  rank_scan_kernel<<<1, 1024, 0, s>>>(H.rank.as<int>(), DP.na, H.t_off.as<int>());
+  AC3D_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------------------------------
+// Listener ACA (compute_ACA_listener, aca.cpp:84-134): one block of L receivers x Ne elements,
+// maxk 5000, no zero guard. Rows are receiver points.
+// ------------------------------------------------------------------------------------------
+void launch_listener_aca(const DevGeometry& G, int prec, const void* pts, int L, double k, double eps, int maxk,
+                         void* pool, long long pool_cap, unsigned long long* used, long long* term_off, int* rank,
+                         int* status, const int4* block, const int* order, cudaStream_t s) {
+  int iter_lim = std::min(maxk, std::min(L - 1, G.ne - 1));
+  if (iter_lim < 1) iter_lim = 1;
+  if (prec == PREC_FP64) {
+    AcaArgs<double, double4> a{geo_view<double>(G), block, order, (const double4*)pts, k, eps, maxk, 0, iter_lim,
+                               (cd*)pool, pool_cap, used, term_off, rank, status};
+    aca_launch_t(a, 1, L, s);
+  } else {
+    AcaArgs<float, float4> a{geo_view<float>(G), block, order, (const float4*)pts, (float)k, eps, maxk, 0,
+                             iter_lim, (cf*)pool, pool_cap, used, term_off, rank, status};
+    aca_launch_t(a, 1, L, s);
+  }
+}
+
+}  // namespace ac3d

@@ -1,0 +1,163 @@
+// Internal declarations shared by the host orchestration (api.cpp, tree.cpp) and the CUDA
+// translation units. Nothing here is part of the public C-ABI (include/ac3d.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace ac3d {
+
+constexpr double kPiHost = 3.14159265358979323846;
+
+// ------------------------------------------------------------------------------------------
+// Errors: host code throws; the C-ABI converts to status codes + a per-context message.
+// ------------------------------------------------------------------------------------------
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* what, const char* file, int line);
+#define AC3D_CUDA(x) ::ac3d::cuda_check((x), #x, __FILE__, __LINE__)
+
+// ------------------------------------------------------------------------------------------
+// Device buffer (stream-ordered allocation on the owning context's stream).
+// ------------------------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaStream_t s = nullptr;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept { *this = std::move(o); }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      bytes = o.bytes;
+      s = o.s;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t n, cudaStream_t stream);
+  void ensure(size_t n, cudaStream_t stream) {
+    if (n > bytes) alloc(n, stream);
+  }
+  void release();
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+// ------------------------------------------------------------------------------------------
+// Cluster tree and block partition (host; ClusterTree, clustertree.cpp:49-137)
+// ------------------------------------------------------------------------------------------
+struct TreeNode {
+  double c[3];
+  double r;
+  int s, e;
+  int left, right;
+  bool leaf;
+};
+
+struct Partition {
+  int ne = 0;
+  std::vector<int> order;              // tree position -> original element index
+  std::vector<TreeNode> nodes;
+  std::vector<int> direct;             // 4 ints per near block (rs, re, cs, ce)
+  std::vector<int> approx;             // 4 ints per admissible block
+  std::vector<int> leaf_start;         // leaf ranges, ascending (nleaf + 1 entries)
+  // Per-leaf work lists (CSR), forward (row leaves) and transposed (column leaves).
+  std::vector<int> fw_near_ptr, fw_near;   // near blocks whose rows are the leaf
+  std::vector<int> fw_lr_ptr, fw_lr;       // admissible blocks whose rows contain the leaf
+  std::vector<int> tr_near_ptr, tr_near;   // near blocks whose columns are the leaf
+  std::vector<int> tr_lr_ptr, tr_lr;       // admissible blocks whose columns contain the leaf
+  std::vector<int64_t> near_off;       // element offset of each near block (column-major storage)
+  int64_t near_total = 0;
+  std::vector<int> aca_order;          // admissible blocks by decreasing m + n
+  int max_rows = 0;                    // largest admissible block row count
+  int64_t aca_term_cap = 0;            // sum over blocks of min(maxk, m-1, n-1)
+  int max_leaf = 0;
+  bool tree_ok = true;
+};
+
+void build_partition(const double* C, int ne, int leaf_size, double factor, Partition& P);
+void build_leaf_lists(Partition& P, int maxk);
+
+// ------------------------------------------------------------------------------------------
+// Device views
+// ------------------------------------------------------------------------------------------
+struct DevPartition {
+  int nleaf = 0, nd = 0, na = 0;
+  DevBuf blocks_d, blocks_a;            // int4
+  DevBuf leaf_start;                    // int (nleaf + 1)
+  DevBuf fw_near_ptr, fw_near, fw_lr_ptr, fw_lr;
+  DevBuf tr_near_ptr, tr_near, tr_lr_ptr, tr_lr;
+  DevBuf near_off;                      // int64
+  DevBuf aca_order;                     // int
+};
+
+// Element geometry on device (recomputed from vertex positions for every height update).
+struct DevGeometry {
+  int ne = 0, nv = 0;
+  DevBuf P;          // double (nv x 3)
+  DevBuf E;          // int (ne x 3), tree order
+  DevBuf cen, va;    // double4
+  DevBuf cen32, va32;  // float4
+  DevBuf eg32;       // ElemGeo<float>
+  DevBuf eg64;       // ElemGeo<double>
+};
+
+enum Precision { PREC_MIXED = 0, PREC_FP64 = 1 };
+
+// An assembled H-matrix of (K - I/2) at one wavenumber.
+struct DevHMat {
+  int prec = PREC_MIXED;  // storage: complex FP32 (mixed) or complex FP64
+  double k = 0;
+  int maxk = 100;
+  DevBuf near;            // complex storage of all near blocks
+  DevBuf pool;            // rank-1 terms (u | v) of all admissible blocks
+  DevBuf term_off;        // int64 [na * maxk] offset of each term in the pool
+  DevBuf rank;            // int [na]
+  DevBuf t_off;           // int [na + 1] prefix of ranks
+  DevBuf tvec;            // intermediate V x per term (complex, vector precision)
+  DevBuf tvec64;          // FP64 intermediate for refinement residuals
+  DevBuf pool_used;       // unsigned long long
+  int64_t pool_cap = 0;
+  int64_t pool_used_host = 0;
+  std::vector<int> ranks_host;
+  int64_t lr_entries = 0; // sum r (m + n)
+  size_t bytes() const { return near.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + tvec.bytes + tvec64.bytes; }
+};
+
+// ------------------------------------------------------------------------------------------
+// Kernel launchers (implemented in the .cu files)
+// ------------------------------------------------------------------------------------------
+void launch_geometry(DevGeometry& G, cudaStream_t s);
+void launch_rhs(const DevGeometry& G, int prec_vec64, double k, int kind, const double* v3, void* out, cudaStream_t s);
+
+void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s);
+void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s);
+void launch_rank_scan(const DevPartition& DP, DevHMat& H, cudaStream_t s);
+
+// Matvec y = op(A) x with op = identity or plain transpose. vec: 0 = complex FP32 vectors,
+// 1 = complex FP64 vectors. residual: y = b - op(A) x instead (b given).
+struct MatvecEpilogue {
+  // optional fused dot products over the produced vector y (FP64 partials per CTA)
+  const void* dot_a = nullptr;  // if set: partial sum conj(dot_a) . y
+  const void* dot_b = nullptr;  // if set: partial sum conj(y) . dot_b  (and |y|^2)
+  double* partials = nullptr;   // per-CTA partials [grid x 6]
+};
+void launch_matvec(const DevPartition& DP, const DevHMat& H, int ne, bool transposed, int vec64,
+                   const void* x, void* y, const void* b_minus, const MatvecEpilogue& ep, cudaStream_t s);
+int matvec_grid(const DevPartition& DP, bool transposed);
+int device_sm_count();
+
+}  // namespace ac3d

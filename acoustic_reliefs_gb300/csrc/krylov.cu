@@ -1,0 +1,352 @@
+// Device-resident BiCGSTAB (van der Vorst 1992), the solver the reference runs through
+// Eigen::BiCGSTAB with an identity preconditioner and zero initial guess (adjoint.cpp:92-95,
+// 190-209; acoustics3d.cpp:266-269). Stop rule: |r|^2 <= tol^2 |b|^2 on the recursively updated
+// residual, checked before every iteration; at most `maxit` iterations.
+//
+// All scalars live in a device struct; dot products are FP64 and reduced in a fixed order
+// (per-CTA partials, then one CTA), so a solve is bit-reproducible. Every kernel returns at once
+// when the state says the solve has finished, which lets the host replay a captured graph of a
+// fixed number of iterations until the flag is set.
+#include "common.cuh"
+#include "internal.h"
+#include "krylov.h"
+
+namespace ac3d {
+
+namespace {
+constexpr int kVecThreads = 256;
+constexpr int kVecWarps = kVecThreads / 32;
+}  // namespace
+
+__device__ __forceinline__ void block_sums(double* d, int nd, double (*sd)[5]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = 0; i < nd; i++) d[i] = warp_sum(d[i]);
+  if (lane == 0)
+    for (int i = 0; i < nd; i++) sd[w][i] = d[i];
+  __syncthreads();
+}
+
+__device__ __forceinline__ void write_partials(double* d, double* partials) {
+  __shared__ double sd[kVecWarps][5];
+  block_sums(d, 5, sd);
+  if (threadIdx.x < 5) {
+    double s = 0;
+    for (int w = 0; w < kVecWarps; w++) s += sd[w][threadIdx.x];
+    partials[(size_t)blockIdx.x * 5 + threadIdx.x] = s;
+  }
+}
+
+// Fixed-order reduction of `n` partial 5-vectors by one CTA; result in out[5] (all threads).
+__device__ __forceinline__ void reduce_partials(const double* partials, int n, double* out) {
+  __shared__ double sd[kVecWarps][5];
+  double d[5] = {0, 0, 0, 0, 0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    for (int c = 0; c < 5; c++) d[c] += partials[(size_t)i * 5 + c];
+  block_sums(d, 5, sd);
+  for (int c = 0; c < 5; c++) {
+    double s = 0;
+    for (int w = 0; w < kVecWarps; w++) s += sd[w][c];
+    out[c] = s;
+  }
+  __syncthreads();
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(kVecThreads) k_init(int n, const cplx<VT>* __restrict__ b, cplx<VT>* x,
+                                                      cplx<VT>* r, cplx<VT>* rhat, cplx<VT>* p, cplx<VT>* v,
+                                                      double* partials) {
+  double d[5] = {0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    cplx<VT> bi = b[i];
+    x[i] = cplx<VT>();
+    r[i] = bi;
+    rhat[i] = bi;
+    p[i] = cplx<VT>();
+    v[i] = cplx<VT>();
+    double a2 = (double)bi.re * bi.re + (double)bi.im * bi.im;
+    d[0] += a2;
+    d[4] += a2;
+  }
+  write_partials(d, partials);
+}
+
+__global__ void k_scalar_init(KState* st, const double* partials, int n, double tol, int maxit) {
+  double s[5];
+  reduce_partials(partials, n, s);
+  if (threadIdx.x == 0) {
+    st->bnorm2 = s[4];
+    st->rnorm2 = s[4];
+    st->rhat2 = s[4];
+    st->tol2 = tol * tol * s[4];
+    st->rho_re = st->alpha_re = st->omega_re = 1.0;
+    st->rho_im = st->alpha_im = st->omega_im = 0.0;
+    st->rho_old_re = 1.0;
+    st->rho_old_im = 0.0;
+    st->beta_re = st->beta_im = 0.0;
+    st->iter = 0;
+    st->maxit = maxit;
+    st->done = s[4] == 0.0 ? 1 : 0;
+    st->restart = 0;
+    st->restarts = 0;
+  }
+}
+
+__device__ __forceinline__ void cdivd(double ar, double ai, double br, double bi, double& cr, double& ci) {
+  double s = fabs(br) + fabs(bi);
+  double xr = br / s, xi = bi / s, yr = ar / s, yi = ai / s;
+  double d = xr * xr + xi * xi;
+  cr = (yr * xr + yi * xi) / d;
+  ci = (yi * xr - yr * xi) / d;
+}
+
+// Start of an iteration: convergence test, rho = (rhat, r), beta.
+__global__ void k_scalar_rho(KState* st, const double* partials, int n) {
+  if (st->done) return;
+  double s[5];
+  reduce_partials(partials, n, s);
+  if (threadIdx.x != 0) return;
+  double rr = s[4];
+  st->rnorm2 = rr;
+  st->restart = 0;
+  if (!(rr > st->tol2)) {
+    st->done = 1;
+    return;
+  }
+  if (st->iter >= st->maxit) {
+    st->done = 2;
+    return;
+  }
+  double rho_re = s[0], rho_im = s[1];
+  double rho_old_re = st->rho_re, rho_old_im = st->rho_im;
+  // breakdown: the shadow residual has become orthogonal to r -> restart with rhat = r
+  if (rho_re * rho_re + rho_im * rho_im <= 1e-24 * st->rhat2 * rr) {
+    st->restart = 1;
+    st->restarts++;
+    st->rhat2 = rr;
+    st->rho_re = rr;
+    st->rho_im = 0.0;
+    st->rho_old_re = 1.0;
+    st->rho_old_im = 0.0;
+    st->alpha_re = st->omega_re = 1.0;
+    st->alpha_im = st->omega_im = 0.0;
+    st->beta_re = st->beta_im = 0.0;
+    return;
+  }
+  st->rho_old_re = rho_old_re;
+  st->rho_old_im = rho_old_im;
+  st->rho_re = rho_re;
+  st->rho_im = rho_im;
+  // beta = (rho / rho_old) (alpha / omega)
+  double q1r, q1i, q2r, q2i;
+  cdivd(rho_re, rho_im, rho_old_re, rho_old_im, q1r, q1i);
+  cdivd(st->alpha_re, st->alpha_im, st->omega_re, st->omega_im, q2r, q2i);
+  st->beta_re = q1r * q2r - q1i * q2i;
+  st->beta_im = q1r * q2i + q1i * q2r;
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(kVecThreads) k_p(const KState* st, int n, const cplx<VT>* __restrict__ r,
+                                                   cplx<VT>* p, cplx<VT>* v, cplx<VT>* rhat) {
+  if (st->done) return;
+  const bool restart = st->restart != 0;
+  const VT br = (VT)st->beta_re, bi = (VT)st->beta_im, wr = (VT)st->omega_re, wi = (VT)st->omega_im;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    cplx<VT> ri = r[i];
+    if (restart) {
+      rhat[i] = ri;
+      p[i] = ri;
+      v[i] = cplx<VT>();
+    } else {
+      cplx<VT> pi = p[i], vi = v[i];
+      // p = r + beta (p - omega v)
+      VT tr = pi.re - (wr * vi.re - wi * vi.im);
+      VT ti = pi.im - (wr * vi.im + wi * vi.re);
+      p[i] = cplx<VT>(ri.re + br * tr - bi * ti, ri.im + br * ti + bi * tr);
+    }
+  }
+}
+
+// alpha = rho / (rhat, v); partials from the matvec epilogue (slots 0, 1).
+__global__ void k_scalar_alpha(KState* st, const double* partials, int n) {
+  if (st->done) return;
+  double s[5];
+  reduce_partials(partials, n, s);
+  if (threadIdx.x != 0) return;
+  if (s[0] == 0.0 && s[1] == 0.0) {
+    st->done = 3;
+    return;
+  }
+  cdivd(st->rho_re, st->rho_im, s[0], s[1], st->alpha_re, st->alpha_im);
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(kVecThreads) k_s(const KState* st, int n, const cplx<VT>* __restrict__ r,
+                                                   const cplx<VT>* __restrict__ v, cplx<VT>* s) {
+  if (st->done) return;
+  const VT ar = (VT)st->alpha_re, ai = (VT)st->alpha_im;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    cplx<VT> ri = r[i], vi = v[i];
+    s[i] = cplx<VT>(ri.re - (ar * vi.re - ai * vi.im), ri.im - (ar * vi.im + ai * vi.re));
+  }
+}
+
+// omega = (t, s) / (t, t); partials from the matvec epilogue (slots 2, 3 and 4).
+__global__ void k_scalar_omega(KState* st, const double* partials, int n) {
+  if (st->done) return;
+  double s[5];
+  reduce_partials(partials, n, s);
+  if (threadIdx.x != 0) return;
+  if (s[4] > 0.0) {
+    st->omega_re = s[2] / s[4];
+    st->omega_im = s[3] / s[4];
+  } else {
+    st->omega_re = st->omega_im = 0.0;
+  }
+  st->iter++;
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(kVecThreads) k_xr(const KState* st, int n, cplx<VT>* x, const cplx<VT>* __restrict__ p,
+                                                    const cplx<VT>* __restrict__ s, cplx<VT>* r,
+                                                    const cplx<VT>* __restrict__ t, const cplx<VT>* __restrict__ rhat,
+                                                    double* partials) {
+  if (st->done) return;
+  const VT ar = (VT)st->alpha_re, ai = (VT)st->alpha_im, wr = (VT)st->omega_re, wi = (VT)st->omega_im;
+  double d[5] = {0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    cplx<VT> pi = p[i], si = s[i], ti = t[i], xi = x[i], hi = rhat[i];
+    xi.re += (ar * pi.re - ai * pi.im) + (wr * si.re - wi * si.im);
+    xi.im += (ar * pi.im + ai * pi.re) + (wr * si.im + wi * si.re);
+    x[i] = xi;
+    cplx<VT> ri(si.re - (wr * ti.re - wi * ti.im), si.im - (wr * ti.im + wi * ti.re));
+    r[i] = ri;
+    d[0] += (double)hi.re * ri.re + (double)hi.im * ri.im;
+    d[1] += (double)hi.re * ri.im - (double)hi.im * ri.re;
+    d[4] += (double)ri.re * ri.re + (double)ri.im * ri.im;
+  }
+  write_partials(d, partials);
+}
+
+// ------------------------------------------------------------------------------------------
+// Refinement helpers (mixed precision): FP64 residual -> FP32 right-hand side, x64 += d32.
+// ------------------------------------------------------------------------------------------
+__global__ void k_to32(int n, const cd* __restrict__ a, cf* b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = cf((float)a[i].re, (float)a[i].im);
+}
+__global__ void k_add32(int n, cd* x, const cf* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i].re += (double)d[i].re;
+    x[i].im += (double)d[i].im;
+  }
+}
+__global__ void k_copy64(int n, const cd* __restrict__ a, cd* b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+__global__ void k_zero64(int n, cd* b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = cd();
+}
+__global__ void k_negate64(int n, cd* a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    a[i].re = -a[i].re;
+    a[i].im = -a[i].im;
+  }
+}
+__global__ void __launch_bounds__(kVecThreads) k_norm2_64(int n, const cd* __restrict__ a, double* partials) {
+  double d[5] = {0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    d[4] += a[i].re * a[i].re + a[i].im * a[i].im;
+  write_partials(d, partials);
+}
+__global__ void k_reduce5(const double* partials, int n, double* out) {
+  double s[5];
+  reduce_partials(partials, n, s);
+  if (threadIdx.x < 5) out[threadIdx.x] = s[threadIdx.x];
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------
+static int vec_grid(int n) {
+  int g = (n + kVecThreads - 1) / kVecThreads;
+  return g < 1 ? 1 : (g > 1184 ? 1184 : g);
+}
+
+template <typename VT>
+static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, cudaStream_t s) {
+  const int n = B.n, G = vec_grid(n);
+  const int vec64 = sizeof(VT) == 8;
+  KState* st = B.state;
+  k_scalar_rho<<<1, kVecThreads, 0, s>>>(st, B.partials, B.nparts_r);
+  k_p<VT><<<G, kVecThreads, 0, s>>>(st, n, (const cplx<VT>*)B.r, (cplx<VT>*)B.p, (cplx<VT>*)B.v, (cplx<VT>*)B.rhat);
+  MatvecEpilogue e1;
+  e1.dot_a = B.rhat;
+  e1.partials = B.partials;
+  launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s);
+  k_scalar_alpha<<<1, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf);
+  k_s<VT><<<G, kVecThreads, 0, s>>>(st, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v, (cplx<VT>*)B.s);
+  MatvecEpilogue e2;
+  e2.dot_b = B.s;
+  e2.partials = B.partials;
+  launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s);
+  k_scalar_omega<<<1, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf);
+  k_xr<VT><<<G, kVecThreads, 0, s>>>(st, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p, (const cplx<VT>*)B.s,
+                                     (cplx<VT>*)B.r, (const cplx<VT>*)B.t, (const cplx<VT>*)B.rhat, B.partials);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+void krylov_enqueue_init(const KrylovBufs& B, int vec64, double tol, int maxit, cudaStream_t s) {
+  const int n = B.n, G = vec_grid(n);
+  if (vec64)
+    k_init<double><<<G, kVecThreads, 0, s>>>(n, (const cd*)B.b, (cd*)B.x, (cd*)B.r, (cd*)B.rhat, (cd*)B.p,
+                                             (cd*)B.v, B.partials);
+  else
+    k_init<float><<<G, kVecThreads, 0, s>>>(n, (const cf*)B.b, (cf*)B.x, (cf*)B.r, (cf*)B.rhat, (cf*)B.p,
+                                            (cf*)B.v, B.partials);
+  k_scalar_init<<<1, kVecThreads, 0, s>>>(B.state, B.partials, G, tol, maxit);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+void krylov_enqueue_iterations(const KrylovBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, int vec64,
+                               int count, cudaStream_t s) {
+  for (int i = 0; i < count; i++) {
+    if (vec64)
+      enqueue_iteration<double>(B, DP, H, tr, s);
+    else
+      enqueue_iteration<float>(B, DP, H, tr, s);
+  }
+}
+
+int krylov_vec_grid(int n) { return vec_grid(n); }
+
+void launch_to32(int n, const void* a, void* b, cudaStream_t s) {
+  k_to32<<<vec_grid(n), kVecThreads, 0, s>>>(n, (const cd*)a, (cf*)b);
+  AC3D_CUDA(cudaGetLastError());
+}
+void launch_add32(int n, void* x, const void* d, cudaStream_t s) {
+  k_add32<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)x, (const cf*)d);
+  AC3D_CUDA(cudaGetLastError());
+}
+void launch_copy64(int n, const void* a, void* b, cudaStream_t s) {
+  k_copy64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (const cd*)a, (cd*)b);
+  AC3D_CUDA(cudaGetLastError());
+}
+void launch_zero64(int n, void* b, cudaStream_t s) {
+  k_zero64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)b);
+  AC3D_CUDA(cudaGetLastError());
+}
+void launch_negate64(int n, void* a, cudaStream_t s) {
+  k_negate64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)a);
+  AC3D_CUDA(cudaGetLastError());
+}
+int launch_norm2_64(int n, const void* a, double* partials, cudaStream_t s) {
+  k_norm2_64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (const cd*)a, partials);
+  AC3D_CUDA(cudaGetLastError());
+  return vec_grid(n);
+}
+void launch_reduce5(const double* partials, int n, double* out, cudaStream_t s) {
+  k_reduce5<<<1, kVecThreads, 0, s>>>(partials, n, out);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+}  // namespace ac3d

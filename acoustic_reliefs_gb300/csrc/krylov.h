@@ -1,0 +1,46 @@
+// Device-resident BiCGSTAB interface (internal).
+#pragma once
+
+#include "internal.h"
+
+namespace ac3d {
+
+// Solver scalars, kept on the device for the whole solve.
+struct KState {
+  double rho_re, rho_im, rho_old_re, rho_old_im;
+  double alpha_re, alpha_im, omega_re, omega_im;
+  double beta_re, beta_im;
+  double bnorm2, rnorm2, tol2, rhat2;
+  int iter, maxit;
+  int done;      // 0 running, 1 converged, 2 iteration limit, 3 breakdown (rhat . v == 0)
+  int restart;   // this iteration restarts with rhat = r
+  int restarts;
+  int pad;
+};
+
+// Device vectors of one solve (complex, FP32 or FP64 according to the solve).
+struct KrylovBufs {
+  int n = 0;
+  void *b = nullptr, *x = nullptr, *r = nullptr, *rhat = nullptr, *p = nullptr, *v = nullptr, *s = nullptr,
+       *t = nullptr;
+  double* partials = nullptr;  // >= max(nleaf, vector grid) x 5
+  int nparts_r = 0;            // number of partials feeding the rho step (vector grid)
+  KState* state = nullptr;
+};
+
+void krylov_enqueue_init(const KrylovBufs& B, int vec64, double tol, int maxit, cudaStream_t s);
+void krylov_enqueue_iterations(const KrylovBufs& B, const DevPartition& DP, const DevHMat& H, bool transposed,
+                               int vec64, int count, cudaStream_t s);
+int krylov_vec_grid(int n);
+
+void launch_matvec_ex(const DevPartition& DP, const DevHMat& H, bool transposed, int vec64, const void* x, void* y,
+                      const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s);
+void launch_to32(int n, const void* a, void* b, cudaStream_t s);
+void launch_add32(int n, void* x, const void* d, cudaStream_t s);
+void launch_copy64(int n, const void* a, void* b, cudaStream_t s);
+void launch_zero64(int n, void* b, cudaStream_t s);
+void launch_negate64(int n, void* a, cudaStream_t s);
+int launch_norm2_64(int n, const void* a, double* partials, cudaStream_t s);
+void launch_reduce5(const double* partials, int n, double* out, cudaStream_t s);
+
+}  // namespace ac3d

@@ -1,0 +1,136 @@
+/* C-ABI of libac3d.so: the GB300 BEM hot path behind the reference's `acoustics3d` binding.
+ *
+ * Each entry point replaces one method of the reference binding class DiffBEM
+ * (acoustics3d_cpp/src/acoustics3d.cpp, bound at :353-383) or the free function `sphere`
+ * (acoustics3d_cpp/include/sphere.h:28-85); the citation is given beside each declaration.
+ * Arguments are plain pointers and sizes. Vertex positions are (V, 3) float64 row-major,
+ * connectivity (Ne, 3) int32 row-major, complex outputs interleaved float64 (re, im).
+ *
+ * Every function returns AC3D_OK (0) or an error code; ac3d_last_error() gives the message.
+ * Where the reference printed to std::cerr and returned a sentinel (acoustics3d.cpp:110-113,
+ * 133-136, 200-207, 241-243), these return AC3D_ERR_STATE. A context owns one CUDA stream and
+ * is not reentrant; use one context per host thread.
+ */
+#ifndef AC3D_H
+#define AC3D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AC3D_OK 0
+#define AC3D_ERR_ARG 1        /* invalid argument */
+#define AC3D_ERR_STATE 2      /* mesh / differentiable points not set */
+#define AC3D_ERR_INTERNAL 3
+#define AC3D_ERR_RESOURCE 4   /* device memory or shared-memory limits */
+#define AC3D_ERR_CUDA 5
+#define AC3D_ERR_NOT_CONVERGED 6 /* solver hit its iteration limit (results still written) */
+
+#define AC3D_PREC_MIXED 0     /* complex FP32 blocks, FP64 dots and iterative refinement */
+#define AC3D_PREC_FP64 1      /* everything complex FP64 */
+
+#define AC3D_INCIDENT_POINT 0 /* point source e^{-ikr}/(4 pi r) at the given point */
+#define AC3D_INCIDENT_PLANE 1 /* plane wave e^{-ik d.x} along the given unit vector */
+
+#define AC3D_LISTENER_DENSE 0 /* receiver matrix evaluated exactly on the fly */
+#define AC3D_LISTENER_ACA 1   /* receiver matrix by ACA with Q_ACA_tol, as the reference */
+
+typedef struct ac3d_ctx ac3d_ctx;
+
+/* Statistics of the most recent call. */
+typedef struct ac3d_stats {
+  int n_elements, n_direct, n_approx, n_leaves;
+  long long near_entries, lr_entries; /* stored complex entries */
+  double mean_rank;
+  int max_rank;
+  long long hmat_bytes;     /* device bytes of the last H-matrix */
+  int solves;               /* linear solves in the call */
+  int iterations;           /* BiCGSTAB iterations, summed over solves and refinement steps */
+  int outer_steps;          /* refinement steps (mixed precision) summed over solves */
+  int matvecs;
+  double rel_residual;      /* final |b - A x| / |b| of the last solve (FP64) */
+  int converged;            /* 1 if every solve met solver_tol */
+  double ms_assemble, ms_solve, ms_listener, ms_adjoint, ms_total;
+} ac3d_stats;
+
+/* DiffBEM(cluster_size, radius_factor, freq_bands, n_freqs, approx_ACA_tol, Q_ACA_tol,
+ *         solver_tol, src_pt, listener_radius, listener_ds, recompute_matrices)
+ * -- acoustics3d.cpp:22-34 (constructor), defaults at :355-357. */
+int ac3d_create(ac3d_ctx** ctx, int cluster_size, double radius_factor, const double* freq_bands, int n_bands,
+                int n_freqs, double approx_aca_tol, double q_aca_tol, double solver_tol, const double* src_pt,
+                double listener_radius, double listener_ds, int recompute_matrices);
+void ac3d_destroy(ac3d_ctx* ctx);
+const char* ac3d_last_error(const ac3d_ctx* ctx);
+
+/* Options with no reference counterpart (the reference is FP64, point source, ACA receivers). */
+int ac3d_set_precision(ac3d_ctx* ctx, int precision);
+int ac3d_set_incident(ac3d_ctx* ctx, int kind, const double* v3);
+int ac3d_set_listener_mode(ac3d_ctx* ctx, int mode);
+int ac3d_set_solver(ac3d_ctx* ctx, int max_iterations, double inner_tol, int max_outer);
+/* Replace the receivers used by value / values / band_value / gradient (default: the
+ * hemisphere of compute_listener_pts, helpers.cpp:52-65). */
+int ac3d_set_listeners(ac3d_ctx* ctx, const double* Ls, int L);
+
+/* set_mesh(Ps, Es) -> (Ps, Es reordered) -- acoustics3d.cpp:36-67. Es_out (Ne x 3) receives the
+ * tree-ordered connectivity; Ps is not permuted. */
+int ac3d_set_mesh(ac3d_ctx* ctx, const double* Ps, int V, const int32_t* Es, int Ne, int32_t* Es_out);
+/* set_diff_points(diff_pts) -- acoustics3d.cpp:69-101. */
+int ac3d_set_diff_points(ac3d_ctx* ctx, const int32_t* diff_pts, int HH);
+/* set_band(freq_band) -- acoustics3d.cpp:348-351; ac3d_set_bands replaces the whole list. */
+int ac3d_set_band(ac3d_ctx* ctx, double freq_band);
+int ac3d_set_bands(ac3d_ctx* ctx, const double* freq_bands, int n_bands);
+
+/* get_listeners() -- acoustics3d.cpp:317-319. */
+int ac3d_num_listeners(const ac3d_ctx* ctx, int* L);
+int ac3d_get_listeners(const ac3d_ctx* ctx, double* Ls_out);
+/* Replace all vertex positions (same topology; the block partition of set_mesh is kept, as the
+ * reference keeps it across height updates, acoustics3d.cpp:139-146). */
+int ac3d_set_points(ac3d_ctx* ctx, const double* Ps);
+
+/* pvals(frequency[, listeners]) -- acoustics3d.cpp:236-280. Ls may be NULL (context receivers);
+ * out receives L complex pressures. */
+int ac3d_pressures(ac3d_ctx* ctx, double frequency, const double* Ls, int L, double* out);
+/* surface_vals(frequency) -- acoustics3d.cpp:282-315; out receives Ne complex values. */
+int ac3d_surface_values(ac3d_ctx* ctx, double frequency, double* out);
+/* band_value(freq_band) -- acoustics3d.cpp:162-176. */
+int ac3d_band_value(ac3d_ctx* ctx, double freq_band, double* c);
+/* values() -- acoustics3d.cpp:178-197; out receives one coefficient per band. */
+int ac3d_values(ac3d_ctx* ctx, double* out);
+/* value() / value(x) -- acoustics3d.cpp:109-160: mean over bands; x (HH heights) may be NULL. */
+int ac3d_value(ac3d_ctx* ctx, const double* x, double* c);
+/* gradient(x) -> (c, dc/dx) -- acoustics3d.cpp:199-234: c and gradient summed over bands. */
+int ac3d_gradient(ac3d_ctx* ctx, const double* x, double* c, double* grad);
+/* Same as ac3d_value / ac3d_gradient with x, c and grad in device memory; the work is ordered
+ * after `stream` (a cudaStream_t) and `stream` waits for its completion. */
+int ac3d_value_dev(ac3d_ctx* ctx, const double* x_dev, double* c_dev, void* stream);
+int ac3d_gradient_dev(ac3d_ctx* ctx, const double* x_dev, double* c_dev, double* grad_dev, void* stream);
+
+/* sphere(sphere_mesh, freq, LL, lrad, actual=false) -- sphere.h:28-85, with the mesh passed as
+ * arrays instead of an OBJ path: leaf 128, factor 1.5, ACA and solver tolerance 1e-10, plane
+ * wave e^{-ikx}, LL receivers on a circle of radius lrad in the xz plane. */
+int ac3d_sphere(const double* Ps, int V, const int32_t* Es, int Ne, double freq, int LL, double lrad, int precision,
+                double* out);
+
+int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
+
+/* Host-only cluster tree and block partition (ClusterTree, clustertree.cpp:49-137, as used by
+ * set_mesh, acoustics3d.cpp:43-58). No GPU work: for inspection and tests. */
+typedef struct ac3d_partition ac3d_partition;
+int ac3d_partition_build(const double* Ps, int V, const int32_t* Es, int Ne, int cluster_size, double radius_factor,
+                         ac3d_partition** out);
+/* counts: n_direct, n_approx, n_leaves, tree_ok (1 if every centroid lies inside its node radius) */
+int ac3d_partition_counts(const ac3d_partition* p, int* n_direct, int* n_approx, int* n_leaves, int* tree_ok);
+/* order (Ne): tree position -> input element; direct (4 n_direct), approx (4 n_approx): blocks
+ * (row start, row end, column start, column end) in traversal order; leaves (n_leaves + 1). */
+int ac3d_partition_get(const ac3d_partition* p, int32_t* order, int32_t* direct, int32_t* approx, int32_t* leaves);
+void ac3d_partition_free(ac3d_partition* p);
+/* Library version string. */
+const char* ac3d_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AC3D_H */
