@@ -24,6 +24,7 @@ SIGNATURES = {
     "ac3d_version": (ctypes.c_char_p, []),
     "ac3d_create": (_I, [ctypes.POINTER(_P), _I, _D, _P, _I, _I, _D, _D, _D, _P, _D, _D, _I]),
     "ac3d_destroy": (None, [_P]),
+    "ac3d_select_device": (_I, [_I]),
     "ac3d_last_error": (ctypes.c_char_p, [_P]),
     "ac3d_set_precision": (_I, [_P, _I]),
     "ac3d_set_incident": (_I, [_P, _I, _P]),
@@ -38,6 +39,7 @@ SIGNATURES = {
     "ac3d_get_listeners": (_I, [_P, _P]),
     "ac3d_set_points": (_I, [_P, _P]),
     "ac3d_pressures": (_I, [_P, _D, _P, _I, _P]),
+    "ac3d_pressures_dev": (_I, [_P, _D, _P, _I, _P, _P]),
     "ac3d_surface_values": (_I, [_P, _D, _P]),
     "ac3d_band_value": (_I, [_P, _D, _P]),
     "ac3d_values": (_I, [_P, _P]),
@@ -47,6 +49,7 @@ SIGNATURES = {
     "ac3d_gradient_dev": (_I, [_P, _P, _P, _P, _P]),
     "ac3d_sphere": (_I, [_P, _I, _P, _I, _D, _I, _D, _I, _P]),
     "ac3d_get_stats": (_I, [_P, _P]),
+    "ac3d_matvec_timing": (_I, [_P, _I, _I, _P, _P]),
     "ac3d_partition_build": (_I, [_P, _I, _P, _I, _I, _D, ctypes.POINTER(_P)]),
     "ac3d_partition_counts": (_I, [_P, _P, _P, _P, _P]),
     "ac3d_partition_get": (_I, [_P, _P, _P, _P, _P]),
@@ -62,7 +65,7 @@ class Stats(ctypes.Structure):
                 ("solves", _I), ("iterations", _I), ("outer_steps", _I), ("matvecs", _I),
                 ("rel_residual", _D), ("converged", _I),
                 ("ms_assemble", _D), ("ms_solve", _D), ("ms_listener", _D), ("ms_adjoint", _D),
-                ("ms_total", _D)]
+                ("ms_total", _D), ("kernel_launches", ctypes.c_longlong)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -42,8 +42,13 @@ class DiffBEM:
 
     def __init__(self, cluster_size=64, radius_factor=1.5, freq_bands=(1000,), n_freqs=1, approx_ACA_tol=1e-3,
                  Q_ACA_tol=1e-3, solver_tol=1e-3, src_pt=(0.0, 100.0, 0.0), listener_radius=50, listener_ds=5,
-                 recompute_matrices=False, *, precision: str = "mixed", incident=None, listener: str = "dense"):
+                 recompute_matrices=False, *, precision: str = "mixed", incident=None, listener: str = "dense",
+                 device: int | None = None):
         L = _L.lib()
+        if device is not None:
+            rc = L.ac3d_select_device(int(device))
+            if rc != _L.OK:
+                raise AC3DError(rc, f"cannot select CUDA device {device}")
         bands = _f64(list(freq_bands))
         src = _f64(src_pt, (3,))
         h = ctypes.c_void_p()
@@ -98,12 +103,20 @@ class DiffBEM:
         k = {"point": _L.INCIDENT_POINT, "plane": _L.INCIDENT_PLANE}[kind]
         self._check(_L.lib().ac3d_set_incident(self._h, k, _L.ptr(_f64(vec, (3,)))))
 
-    def set_solver(self, max_iterations: int = 0, inner_tol: float = 1e-4, max_outer: int = 10) -> None:
+    def set_solver(self, max_iterations: int = 0, inner_tol: float = 1e-6, max_outer: int = 10) -> None:
         self._check(_L.lib().ac3d_set_solver(self._h, int(max_iterations), float(inner_tol), int(max_outer)))
 
     def set_listeners(self, listeners) -> None:
         Ls = _f64(listeners).reshape(-1, 3)
         self._check(_L.lib().ac3d_set_listeners(self._h, _L.ptr(Ls), len(Ls)))
+
+    def matvec_timing(self, iters: int = 50, transposed: bool = False):
+        """(ms per H-matvec, algorithmic bytes per matvec) on the H-matrix of the last solve."""
+        ms = ctypes.c_double()
+        nb = ctypes.c_longlong()
+        self._check(_L.lib().ac3d_matvec_timing(self._h, int(iters), int(transposed), ctypes.byref(ms),
+                                                ctypes.byref(nb)))
+        return ms.value, nb.value
 
     def stats(self) -> dict:
         s = _L.Stats()
@@ -168,6 +181,19 @@ class DiffBEM:
         c = ctypes.c_double()
         self._check(_L.lib().ac3d_gradient(self._h, _L.ptr(xx), ctypes.byref(c), _L.ptr(g)))
         return c.value, g
+
+    def pvals_dev(self, frequency, out_ptr: int, listeners_ptr: int | None = None, n_listeners: int = 0,
+                  stream: int = 0) -> None:
+        """Pressures into device memory (out_ptr: L complex128), receivers optionally in device
+        memory (listeners_ptr: L x 3 float64), ordered on the CUDA stream handle `stream`."""
+        self._check(_L.lib().ac3d_pressures_dev(self._h, float(frequency), ctypes.c_void_p(listeners_ptr or 0),
+                                                int(n_listeners), ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream)))
+
+    def set_points(self, Ps) -> None:
+        """Replace all vertex positions (same topology, partition kept)."""
+        P = _f64(Ps).reshape(-1, 3)
+        self._check(_L.lib().ac3d_set_points(self._h, _L.ptr(P)))
+        self._Ps = P.copy()
 
     def pvals(self, frequency, listeners=None) -> np.ndarray:
         """acoustics3d.cpp:236-280: complex pressures at the receivers."""

@@ -206,12 +206,16 @@ static void adjoint_t(const DevGeometry& G, const AdjointArgs& a, DevBuf& scratc
   cd* s1 = (cd*)((char*)scratch.p + ((bytesA + 15) / 16) * 16);
   cd* s2 = s1 + (size_t)a.ntouch * S1;
   GeoView<R> gv = geo_view<R>(G);
+  note_launch();
   derA_kernel<R><<<(a.npairs * 32 + kAdjThreads - 1) / kAdjThreads, kAdjThreads, 0, s>>>(gv, a, outA);
   AC3D_CUDA(cudaGetLastError());
+  note_launch();
   derB_s1_kernel<R><<<dim3(tiles1, S1), kAdjThreads, 0, s>>>(gv, a, s1, S1);
   AC3D_CUDA(cudaGetLastError());
+  note_launch();
   derB_s2_kernel<R><<<dim3(tiles2, S2), kAdjThreads, 0, s>>>(gv, a, s2, S2);
   AC3D_CUDA(cudaGetLastError());
+  note_launch();
   adj_combine_kernel<<<(a.HH + 127) / 128, 128, 0, s>>>(a, G.cen.as<double4>(), outA, s1, s2, S1, S2);
   AC3D_CUDA(cudaGetLastError());
 }

@@ -23,6 +23,8 @@
 
 namespace ac3d {
 
+std::atomic<long long> g_kernel_launches{0};
+
 void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
   if (e != cudaSuccess) {
     throw Error(AC3D_ERR_CUDA, std::string(cudaGetErrorName(e)) + ": " + cudaGetErrorString(e) + " (" + what +
@@ -137,7 +139,7 @@ struct ac3d_ctx {
   int prec = AC3D_PREC_MIXED;
   int listener_mode = AC3D_LISTENER_DENSE;
   int maxit = 0;           // 0: twice the number of unknowns
-  double inner_tol = 1e-4; // relative tolerance of each FP32 inner solve
+  double inner_tol = 1e-6; // floor of the relative tolerance of each FP32 inner solve
   int max_outer = 10;
   int chunk = 8;           // BiCGSTAB iterations per captured graph launch
   int maxk = 100;          // APPROX_ACA_MAX_K (constants.h:16)
@@ -166,6 +168,8 @@ struct ac3d_ctx {
 
   // work buffers
   DevBuf kv, partials, kstate, red, b64, x64, r64, ff_scratch, adj_scratch, tmp_recv;
+  std::unique_ptr<DevHMat> last_H;  // H-matrix of the latest forward solve (matvec timing)
+  bool geom_base = false;           // the device geometry holds Ps0 (no heights applied)
   KState* h_state = nullptr;  // pinned
   double* h_red = nullptr;    // pinned
 
@@ -220,8 +224,10 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
       cap = std::min<int64_t>(c->worst_pool, std::max<int64_t>(cap * 2, (int64_t)hu[0]));
     }
     c->pool_hint[prec] = std::min<int64_t>(c->worst_pool, H->pool_used_host + H->pool_used_host / 8 + 4096);
-    launch_rank_scan(c->DP, *H, s);
     const size_t tcap = (size_t)std::max<int64_t>(c->P.aca_term_cap, 1);
+    H->task_b.alloc(tcap * sizeof(int), s);
+    H->task_off.alloc(tcap * sizeof(long long), s);
+    launch_rank_scan(c->DP, *H, s);
     H->tvec.alloc(tcap * (prec == PREC_FP64 ? sizeof(cd) : sizeof(cf)), s);
     H->tvec64.alloc(tcap * sizeof(cd), s);
     H->ranks_host.resize(na);
@@ -294,9 +300,12 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   krylov_enqueue_init(B, vec64, tol, maxit, s);
   // capture one chunk of iterations as a graph and replay it until the state reports completion
   cudaGraph_t graph;
+  const long long before = g_kernel_launches.load();
   AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   krylov_enqueue_iterations(B, c->DP, H, tr, vec64, c->chunk, s);
   AC3D_CUDA(cudaStreamEndCapture(s, &graph));
+  const long long nodes = g_kernel_launches.load() - before;
+  g_kernel_launches.fetch_sub(nodes);  // captured, not launched
   cudaGraphExec_t exec;
   AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   AC3D_CUDA(cudaGraphDestroy(graph));
@@ -304,6 +313,7 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   const int max_launch = maxit / c->chunk + 2;
   // keep one chunk in flight while the host reads the previous state
   AC3D_CUDA(cudaGraphLaunch(exec, s));
+  note_launch(nodes);
   AC3D_CUDA(cudaMemcpyAsync(&c->h_state[0], B.state, sizeof(KState), cudaMemcpyDeviceToHost, s));
   launched++;
   cudaEvent_t ev;
@@ -314,6 +324,7 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
     bool more = launched < max_launch;
     if (more) {
       AC3D_CUDA(cudaGraphLaunch(exec, s));
+      note_launch(nodes);
       AC3D_CUDA(cudaMemcpyAsync(&c->h_state[launched & 1], B.state, sizeof(KState), cudaMemcpyDeviceToHost, s));
     }
     AC3D_CUDA(cudaEventSynchronize(ev));
@@ -404,6 +415,13 @@ void upload_points(ac3d_ctx* c, const std::vector<double>& Ps) {
   c->G.P.ensure(Ps.size() * sizeof(double), s);
   AC3D_CUDA(cudaMemcpyAsync(c->G.P.p, Ps.data(), Ps.size() * sizeof(double), cudaMemcpyHostToDevice, s));
   launch_geometry(c->G, s);
+}
+
+void ensure_base_geometry(ac3d_ctx* c) {
+  if (!c->geom_base) {
+    upload_points(c, c->Ps0);
+    c->geom_base = true;
+  }
 }
 
 std::vector<double> heights_to_points(ac3d_ctx* c, const double* x) {
@@ -592,8 +610,10 @@ int guard(ac3d_ctx* c, F&& f) {
   try {
     c->err.clear();
     auto t0 = std::chrono::steady_clock::now();
+    const long long l0 = g_kernel_launches.load();
     f();
     c->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    c->stats.kernel_launches = g_kernel_launches.load() - l0;
     return AC3D_OK;
   } catch (const Error& e) {
     c->err = e.what();
@@ -657,25 +677,31 @@ int ac3d_create(ac3d_ctx** out, int cluster_size, double radius_factor, const do
 
 void ac3d_destroy(ac3d_ctx* c) {
   if (!c) return;
-  try {
-    if (c->stream) cudaStreamSynchronize(c->stream);
-  } catch (...) {
-  }
   cudaStream_t s = c->stream;
-  {
-    // release device buffers before the stream goes away
-    DevBuf* bufs[] = {&c->kv, &c->partials, &c->kstate, &c->red, &c->b64, &c->x64, &c->r64, &c->ff_scratch,
-                      &c->adj_scratch, &c->tmp_recv, &c->Ls_dev, &c->d_h_off, &c->d_pair_elem, &c->d_pair_corner,
-                      &c->d_pair_touch, &c->d_touch};
-    for (DevBuf* b : bufs) b->release();
-    c->DP = DevPartition();
-    c->G = DevGeometry();
-  }
+  if (s) cudaStreamSynchronize(s);
+  // every device buffer is released on the context stream, so all of them go before the stream
+  c->last_H.reset();
+  DevBuf* bufs[] = {&c->kv, &c->partials, &c->kstate, &c->red, &c->b64, &c->x64, &c->r64, &c->ff_scratch,
+                    &c->adj_scratch, &c->tmp_recv, &c->Ls_dev, &c->d_h_off, &c->d_pair_elem, &c->d_pair_corner,
+                    &c->d_pair_touch, &c->d_touch};
+  for (DevBuf* b : bufs) b->release();
+  c->DP = DevPartition();
+  c->G = DevGeometry();
   if (s) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
+    c->stream = nullptr;
   }
   delete c;
+}
+
+int ac3d_select_device(int device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return AC3D_ERR_ARG;
+  }
+  return cudaSetDevice(device) == cudaSuccess ? AC3D_OK : AC3D_ERR_CUDA;
 }
 
 const char* ac3d_last_error(const ac3d_ctx* c) { return c ? c->err.c_str() : "null context"; }
@@ -791,6 +817,7 @@ int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int N
     c->G.nv = V;
     upload(c->G.E, c->Es, s);
     upload_points(c, c->Ps0);
+    c->geom_base = true;
     AC3D_CUDA(cudaStreamSynchronize(s));
     c->mesh_set = true;
     reset_stats(c);
@@ -878,6 +905,7 @@ int ac3d_set_points(ac3d_ctx* c, const double* Ps) {
     require_mesh(c);
     c->Ps0.assign(Ps, Ps + 3 * (size_t)c->V);
     upload_points(c, c->Ps0);
+    c->geom_base = true;
   });
 }
 
@@ -887,7 +915,7 @@ int ac3d_pressures(ac3d_ctx* c, double f, const double* Ls, int L, double* out) 
     require_mesh(c);
     reset_stats(c);
     cudaStream_t s = c->stream;
-    upload_points(c, c->Ps0);
+    ensure_base_geometry(c);
     const double4* recv = c->Ls_dev.as<double4>();
     const double* Lh = c->Ls.data();
     int nL = (int)c->Ls.size() / 3;
@@ -900,9 +928,42 @@ int ac3d_pressures(ac3d_ctx* c, double f, const double* Ls, int L, double* out) 
     ensure_work(c);
     DevBuf y;
     y.alloc((size_t)nL * sizeof(cd), s);
-    forward_one(c, f, recv, Lh, nL, c->x64.as<cd>(), y.as<cd>(), false);
+    c->last_H.reset();
+    c->last_H = forward_one(c, f, recv, Lh, nL, c->x64.as<cd>(), y.as<cd>(), true);
     AC3D_CUDA(cudaMemcpyAsync(out, y.p, (size_t)nL * sizeof(cd), cudaMemcpyDeviceToHost, s));
     AC3D_CUDA(cudaStreamSynchronize(s));
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+  });
+}
+
+int ac3d_pressures_dev(ac3d_ctx* c, double f, const double* Ls_dev, int L, double* out_dev, void* stream) {
+  if (!c || !out_dev || !(f > 0) || (Ls_dev && L < 1)) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    if (c->listener_mode == AC3D_LISTENER_ACA && Ls_dev)
+      throw Error(AC3D_ERR_ARG, "receiver ACA mode needs host receivers (use ac3d_pressures)");
+    reset_stats(c);
+    cudaStream_t us = (cudaStream_t)stream;
+    cudaStream_t s = c->stream;
+    cudaEvent_t ev;
+    AC3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    AC3D_CUDA(cudaEventRecord(ev, us));
+    AC3D_CUDA(cudaStreamWaitEvent(s, ev, 0));
+    ensure_base_geometry(c);
+    const double4* recv = c->Ls_dev.as<double4>();
+    int nL = (int)c->Ls.size() / 3;
+    if (Ls_dev) {
+      c->tmp_recv.ensure((size_t)L * sizeof(double4), s);
+      launch_pack_points(Ls_dev, L, c->tmp_recv.p, s);
+      recv = c->tmp_recv.as<double4>();
+      nL = L;
+    }
+    ensure_work(c);
+    c->last_H.reset();
+    c->last_H = forward_one(c, f, recv, c->Ls.data(), nL, c->x64.as<cd>(), (cd*)out_dev, true);
+    AC3D_CUDA(cudaEventRecord(ev, s));
+    AC3D_CUDA(cudaStreamWaitEvent(us, ev, 0));
+    AC3D_CUDA(cudaEventDestroy(ev));
     if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
   });
 }
@@ -913,9 +974,10 @@ int ac3d_surface_values(ac3d_ctx* c, double f, double* out) {
     require_mesh(c);
     reset_stats(c);
     cudaStream_t s = c->stream;
-    upload_points(c, c->Ps0);
+    ensure_base_geometry(c);
     ensure_work(c);
-    forward_one(c, f, nullptr, nullptr, 0, c->x64.as<cd>(), nullptr, false);
+    c->last_H.reset();
+    c->last_H = forward_one(c, f, nullptr, nullptr, 0, c->x64.as<cd>(), nullptr, true);
     AC3D_CUDA(cudaMemcpyAsync(out, c->x64.p, (size_t)c->Ne * sizeof(cd), cudaMemcpyDeviceToHost, s));
     AC3D_CUDA(cudaStreamSynchronize(s));
     if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
@@ -927,7 +989,7 @@ int ac3d_band_value(ac3d_ctx* c, double fb, double* cv) {
   return guard(c, [&] {
     require_mesh(c);
     reset_stats(c);
-    upload_points(c, c->Ps0);
+    ensure_base_geometry(c);
     *cv = band_eval(c, fb, true, nullptr);
   });
 }
@@ -937,7 +999,7 @@ int ac3d_values(ac3d_ctx* c, double* out) {
   return guard(c, [&] {
     require_mesh(c);
     reset_stats(c);
-    upload_points(c, c->Ps0);
+    ensure_base_geometry(c);
     for (size_t b = 0; b < c->bands.size(); b++) out[b] = band_eval(c, c->bands[b], true, nullptr);
   });
 }
@@ -948,6 +1010,7 @@ int ac3d_value(ac3d_ctx* c, const double* x, double* cv) {
     require_mesh(c);
     reset_stats(c);
     upload_points(c, heights_to_points(c, x));
+    c->geom_base = x == nullptr;
     double acc = 0;
     for (double fb : c->bands) acc += band_eval(c, fb, true, nullptr);
     *cv = acc / (double)c->bands.size();
@@ -963,6 +1026,7 @@ int ac3d_gradient(ac3d_ctx* c, const double* x, double* cv, double* grad) {
     reset_stats(c);
     cudaStream_t s = c->stream;
     upload_points(c, heights_to_points(c, x));
+    c->geom_base = false;
     const int HH = (int)c->h_off.size() - 1;
     DevBuf g;
     g.alloc((size_t)std::max(HH, 1) * sizeof(double), s);
@@ -994,6 +1058,7 @@ int ac3d_value_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, void* stream
     }
     reset_stats(c);
     upload_points(c, heights_to_points(c, x_dev ? x.data() : nullptr));
+    c->geom_base = x_dev == nullptr;
     double acc = 0;
     for (double fb : c->bands) acc += band_eval(c, fb, true, nullptr);
     acc /= (double)c->bands.size();
@@ -1023,6 +1088,7 @@ int ac3d_gradient_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, double* g
     AC3D_CUDA(cudaStreamSynchronize(s));
     reset_stats(c);
     upload_points(c, heights_to_points(c, x.data()));
+    c->geom_base = false;
     AC3D_CUDA(cudaMemsetAsync(g_dev, 0, (size_t)HH * sizeof(double), s));
     double acc = 0;
     for (double fb : c->bands) acc += band_eval(c, fb, false, g_dev);
@@ -1108,6 +1174,41 @@ int ac3d_partition_get(const ac3d_partition* p, int32_t* order, int32_t* direct,
 }
 
 void ac3d_partition_free(ac3d_partition* p) { delete p; }
+
+int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long long* bytes) {
+  if (!c || iters < 1 || !ms || !bytes) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    if (!c->last_H) throw Error(AC3D_ERR_STATE, "no H-matrix: call ac3d_pressures first");
+    cudaStream_t s = c->stream;
+    const DevHMat& H = *c->last_H;
+    ensure_work(c);
+    const int vec64 = H.prec == PREC_FP64 ? 1 : 0;
+    KrylovBufs B = bufs(c, vec64);
+    // x = the last solution rounded to the vector precision, y = scratch
+    if (vec64)
+      launch_copy64(c->Ne, c->x64.p, B.p, s);
+    else
+      launch_to32(c->Ne, c->x64.p, B.p, s);
+    MatvecEpilogue ep;
+    launch_matvec(c->DP, H, c->Ne, transposed != 0, vec64, B.p, B.v, nullptr, ep, s);  // warm-up
+    cudaEvent_t e0, e1;
+    AC3D_CUDA(cudaEventCreate(&e0));
+    AC3D_CUDA(cudaEventCreate(&e1));
+    AC3D_CUDA(cudaEventRecord(e0, s));
+    for (int i = 0; i < iters; i++)
+      launch_matvec(c->DP, H, c->Ne, transposed != 0, vec64, (i & 1) ? B.v : B.p, (i & 1) ? B.t : B.v, nullptr, ep,
+                    s);
+    AC3D_CUDA(cudaEventRecord(e1, s));
+    AC3D_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    AC3D_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / iters;
+    const long long es = vec64 ? 16 : 8;
+    *bytes = (c->P.near_total + H.lr_entries) * es + 2LL * c->Ne * es;
+  });
+}
 
 int ac3d_get_stats(const ac3d_ctx* c, ac3d_stats* out) {
   if (!c || !out) return AC3D_ERR_ARG;

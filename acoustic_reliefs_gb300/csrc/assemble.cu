@@ -137,22 +137,28 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
   if (tid == 0) used[0] = 1u;
   double err = 0;  // meaningful in thread 0
   int i = 0, iter = 0;
+  int nst = 0;           // stored (nonzero) terms; a term with u == 0 or v == 0 is exactly zero in
+                         // every later residual, cross term and product, so it is not stored
+  bool need_alloc = true;
   __syncthreads();
 
   while (iter < iter_lim) {
-    // --- allocate the storage of term `iter` ---------------------------------------------
-    if (tid == 0) {
-      unsigned long long need = (unsigned long long)(m + n);
-      unsigned long long base = atomicAdd(A.pool_used, need);
-      s_flag = (base + need > (unsigned long long)A.pool_cap) ? 1 : 0;
-      s_base = (long long)base;
-      if (s_flag) atomicOr(A.status, 1);
+    // --- storage of the current term (a slot is reused after a zero term) -------------------
+    if (need_alloc) {
+      if (tid == 0) {
+        unsigned long long need = (unsigned long long)(m + n);
+        unsigned long long base = atomicAdd(A.pool_used, need);
+        s_flag = (base + need > (unsigned long long)A.pool_cap) ? 1 : 0;
+        s_base = (long long)base;
+        if (s_flag) atomicOr(A.status, 1);
+      }
+      __syncthreads();
+      if (s_flag) break;
+      need_alloc = false;
     }
-    __syncthreads();
-    if (s_flag) break;
     cplx<R>* unew = A.pool + s_base;
     cplx<R>* vnew = unew + m;
-    for (int p = tid; p < iter; p += T) uq[p] = A.pool[toff[p] + i];
+    for (int p = tid; p < nst; p += T) uq[p] = A.pool[toff[p] + i];
     __syncthreads();
 
     // --- row residual v = M(i, :) - U(i, :) V ---------------------------------------------
@@ -161,7 +167,7 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
     int bidx = 0;
     for (int c = tid; c < n; c += T) {
       cplx<R> v = entry_far<R>(A.k, A.G, pi, cs + c);
-      for (int p = 0; p < iter; p++) cfms(v, uq[p], A.pool[toff[p] + m + c]);
+      for (int p = 0; p < nst; p++) cfms(v, uq[p], A.pool[toff[p] + m + c]);
       vnew[c] = v;
       R a = abs2(v);
       if (a > best) {
@@ -172,7 +178,7 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
     block_argmax<R>(best, bidx, s_rv, s_ri);
     const int j = bidx;
     const cplx<R> vj = vnew[j];
-    for (int p = tid; p < iter; p += T) vq[p] = A.pool[toff[p] + m + j];
+    for (int p = tid; p < nst; p += T) vq[p] = A.pool[toff[p] + m + j];
     __syncthreads();
     const bool keep = A.zero_guard && vj.re == R(0) && vj.im == R(0);
     double vn = 0;
@@ -180,22 +186,22 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
       cplx<R> v = vnew[c];
       if (!keep) v = cdiv(v, vj);
       vnew[c] = v;
-      vn += (double)abs2(v);
+      vn += (double)v.re * (double)v.re + (double)v.im * (double)v.im;
     }
 
     // --- column residual u = M(:, j) - U V(:, j) ------------------------------------------
     double un = 0;
     for (int r = tid; r < m; r += T) {
       cplx<R> u = entry_far<R>(A.k, A.G, A.rowpts[rs + r], cs + j);
-      for (int p = 0; p < iter; p++) cfms(u, A.pool[toff[p] + r], vq[p]);
+      for (int p = 0; p < nst; p++) cfms(u, A.pool[toff[p] + r], vq[p]);
       unew[r] = u;
-      un += (double)abs2(u);
+      un += (double)u.re * (double)u.re + (double)u.im * (double)u.im;
     }
     __syncthreads();
 
-    // --- cross terms sum_q |u^T U_q| |v V_q^T| (one warp per earlier term) ------------------
+    // --- cross terms sum_q |u^T U_q| |v V_q^T| (one warp per earlier stored term) -----------
     double dots = 0;
-    for (int p = warp; p < iter; p += kAcaWarps) {
+    for (int p = warp; p < nst; p += kAcaWarps) {
       const cplx<R>* Up = A.pool + toff[p];
       const cplx<R>* Vp = Up + m;
       cplx<R> ud(0, 0), vd(0, 0);
@@ -214,6 +220,7 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
     }
     __syncthreads();
     if (s_flag) break;
+    const bool zero_term = (un == 0.0) || (vn == 0.0);
 
     // --- next row pivot: first max |u|^2 over unused rows --------------------------------
     best = R(-1);
@@ -230,13 +237,19 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
     i = bidx;
     if (tid == 0) {
       used[i >> 5] |= 1u << (i & 31);
-      toff[iter] = s_base;
-      A.term_off[(long long)b * A.maxk + iter] = s_base;
+      if (!zero_term) {
+        toff[nst] = s_base;
+        A.term_off[(long long)b * A.maxk + nst] = s_base;
+      }
+    }
+    if (!zero_term) {
+      nst++;
+      need_alloc = true;
     }
     iter++;
     __syncthreads();
   }
-  if (tid == 0) A.rank[b] = iter;
+  if (tid == 0) A.rank[b] = nst;
 }
 
 __global__ void rank_scan_kernel(const int* __restrict__ rank, int na, int* t_off) {
@@ -277,6 +290,7 @@ GeoView<double> geo_view<double>(const DevGeometry& G) {
 
 void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s) {
   if (DP.nd == 0) return;
+  note_launch();
   if (H.prec == PREC_FP64)
     near_kernel<double><<<DP.nd, 256, 0, s>>>(geo_view<double>(G), DP.blocks_d.as<int4>(),
                                               DP.near_off.as<long long>(), H.k, H.near.as<cd>());
@@ -293,6 +307,7 @@ static void aca_launch_t(const AcaArgs<R, P4>& a, int nblocks, int max_rows, cud
     if (smem > 227 * 1024) throw Error(4, "ACA block too large for shared memory");
     AC3D_CUDA(cudaFuncSetAttribute(aca_kernel<R, P4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
+  note_launch();
   aca_kernel<R, P4><<<nblocks, kAcaThreads, smem, s>>>(a);
   AC3D_CUDA(cudaGetLastError());
 }
@@ -315,8 +330,26 @@ void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double
   }
 }
 
+// Flat list of stored terms for the matvec: task t -> (block, pool offset of the term).
+__global__ void task_map_kernel(const int* __restrict__ rank, const int* __restrict__ t_off,
+                                const long long* __restrict__ term_off, int na, int maxk, int* task_b,
+                                long long* task_off) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= na) return;
+  const int r = rank[b], o = t_off[b];
+  for (int q = 0; q < r; q++) {
+    task_b[o + q] = b;
+    task_off[o + q] = term_off[(long long)b * maxk + q];
+  }
+}
+
 void launch_rank_scan(const DevPartition& DP, DevHMat& H, cudaStream_t s) {
+  note_launch();
   rank_scan_kernel<<<1, 1024, 0, s>>>(H.rank.as<int>(), DP.na, H.t_off.as<int>());
+  AC3D_CUDA(cudaGetLastError());
+  note_launch();
+  task_map_kernel<<<(DP.na + 255) / 256, 256, 0, s>>>(H.rank.as<int>(), H.t_off.as<int>(), H.term_off.as<long long>(),
+                                                       DP.na, H.maxk, H.task_b.as<int>(), H.task_off.as<long long>());
   AC3D_CUDA(cudaGetLastError());
 }
 

@@ -64,6 +64,7 @@ void launch_geometry(DevGeometry& G, cudaStream_t s) {
   G.eg32.ensure(ne * sizeof(ElemGeo<float>), s);
   G.eg64.ensure(ne * sizeof(ElemGeo<double>), s);
   int T = 256;
+  note_launch();
   geometry_kernel<<<(G.ne + T - 1) / T, T, 0, s>>>(G.P.as<double>(), G.E.as<int>(), G.ne, G.cen.as<double4>(),
                                                    G.va.as<double4>(), G.cen32.as<float4>(), G.va32.as<float4>(),
                                                    G.eg32.as<ElemGeo<float>>(), G.eg64.as<ElemGeo<double>>());
@@ -99,10 +100,22 @@ __global__ void rhs_kernel(const double4* __restrict__ cen, int ne, double k, in
 void launch_rhs(const DevGeometry& G, int vec64, double k, int kind, const double* v3, void* out, cudaStream_t s) {
   int T = 256;
   int nb = (G.ne + T - 1) / T;
+  note_launch();
   if (vec64)
     rhs_kernel<double><<<nb, T, 0, s>>>(G.cen.as<double4>(), G.ne, k, kind, v3[0], v3[1], v3[2], (cd*)out);
   else
     rhs_kernel<float><<<nb, T, 0, s>>>(G.cen.as<double4>(), G.ne, k, kind, v3[0], v3[1], v3[2], (cf*)out);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+__global__ void pack_points_kernel(const double* __restrict__ p, int n, double4* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_double4(p[3 * i], p[3 * i + 1], p[3 * i + 2], 0.0);
+}
+
+void launch_pack_points(const double* p, int n, void* out, cudaStream_t s) {
+  note_launch();
+  pack_points_kernel<<<(n + 255) / 256, 256, 0, s>>>(p, n, (double4*)out);
   AC3D_CUDA(cudaGetLastError());
 }
 

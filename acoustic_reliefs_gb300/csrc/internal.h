@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -12,6 +13,10 @@
 namespace ac3d {
 
 constexpr double kPiHost = 3.14159265358979323846;
+
+// Kernels launched by this library (process-wide); graph replays add their captured node count.
+extern std::atomic<long long> g_kernel_launches;
+inline void note_launch(long long n = 1) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ------------------------------------------------------------------------------------------
 // Errors: host code throws; the C-ABI converts to status codes + a per-context message.
@@ -127,6 +132,8 @@ struct DevHMat {
   DevBuf term_off;        // int64 [na * maxk] offset of each term in the pool
   DevBuf rank;            // int [na]
   DevBuf t_off;           // int [na + 1] prefix of ranks
+  DevBuf task_b;          // int [sum ranks] block of each stored term
+  DevBuf task_off;        // int64 [sum ranks] pool offset of each stored term
   DevBuf tvec;            // intermediate V x per term (complex, vector precision)
   DevBuf tvec64;          // FP64 intermediate for refinement residuals
   DevBuf pool_used;       // unsigned long long
@@ -134,13 +141,17 @@ struct DevHMat {
   int64_t pool_used_host = 0;
   std::vector<int> ranks_host;
   int64_t lr_entries = 0; // sum r (m + n)
-  size_t bytes() const { return near.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + tvec.bytes + tvec64.bytes; }
+  size_t bytes() const {
+    return near.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
+           tvec.bytes + tvec64.bytes;
+  }
 };
 
 // ------------------------------------------------------------------------------------------
 // Kernel launchers (implemented in the .cu files)
 // ------------------------------------------------------------------------------------------
 void launch_geometry(DevGeometry& G, cudaStream_t s);
+void launch_pack_points(const double* p, int n, void* out, cudaStream_t s);
 void launch_rhs(const DevGeometry& G, int prec_vec64, double k, int kind, const double* v3, void* out, cudaStream_t s);
 
 void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s);

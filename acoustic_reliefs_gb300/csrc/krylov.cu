@@ -277,19 +277,25 @@ static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const
   const int n = B.n, G = vec_grid(n);
   const int vec64 = sizeof(VT) == 8;
   KState* st = B.state;
+  note_launch();
   k_scalar_rho<<<1, kVecThreads, 0, s>>>(st, B.partials, B.nparts_r);
+  note_launch();
   k_p<VT><<<G, kVecThreads, 0, s>>>(st, n, (const cplx<VT>*)B.r, (cplx<VT>*)B.p, (cplx<VT>*)B.v, (cplx<VT>*)B.rhat);
   MatvecEpilogue e1;
   e1.dot_a = B.rhat;
   e1.partials = B.partials;
   launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s);
+  note_launch();
   k_scalar_alpha<<<1, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf);
+  note_launch();
   k_s<VT><<<G, kVecThreads, 0, s>>>(st, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v, (cplx<VT>*)B.s);
   MatvecEpilogue e2;
   e2.dot_b = B.s;
   e2.partials = B.partials;
   launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s);
+  note_launch();
   k_scalar_omega<<<1, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf);
+  note_launch();
   k_xr<VT><<<G, kVecThreads, 0, s>>>(st, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p, (const cplx<VT>*)B.s,
                                      (cplx<VT>*)B.r, (const cplx<VT>*)B.t, (const cplx<VT>*)B.rhat, B.partials);
   AC3D_CUDA(cudaGetLastError());
@@ -297,12 +303,14 @@ static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const
 
 void krylov_enqueue_init(const KrylovBufs& B, int vec64, double tol, int maxit, cudaStream_t s) {
   const int n = B.n, G = vec_grid(n);
+  note_launch();
   if (vec64)
     k_init<double><<<G, kVecThreads, 0, s>>>(n, (const cd*)B.b, (cd*)B.x, (cd*)B.r, (cd*)B.rhat, (cd*)B.p,
                                              (cd*)B.v, B.partials);
   else
     k_init<float><<<G, kVecThreads, 0, s>>>(n, (const cf*)B.b, (cf*)B.x, (cf*)B.r, (cf*)B.rhat, (cf*)B.p,
                                             (cf*)B.v, B.partials);
+  note_launch();
   k_scalar_init<<<1, kVecThreads, 0, s>>>(B.state, B.partials, G, tol, maxit);
   AC3D_CUDA(cudaGetLastError());
 }
@@ -320,31 +328,38 @@ void krylov_enqueue_iterations(const KrylovBufs& B, const DevPartition& DP, cons
 int krylov_vec_grid(int n) { return vec_grid(n); }
 
 void launch_to32(int n, const void* a, void* b, cudaStream_t s) {
+  note_launch();
   k_to32<<<vec_grid(n), kVecThreads, 0, s>>>(n, (const cd*)a, (cf*)b);
   AC3D_CUDA(cudaGetLastError());
 }
 void launch_add32(int n, void* x, const void* d, cudaStream_t s) {
+  note_launch();
   k_add32<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)x, (const cf*)d);
   AC3D_CUDA(cudaGetLastError());
 }
 void launch_copy64(int n, const void* a, void* b, cudaStream_t s) {
+  note_launch();
   k_copy64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (const cd*)a, (cd*)b);
   AC3D_CUDA(cudaGetLastError());
 }
 void launch_zero64(int n, void* b, cudaStream_t s) {
+  note_launch();
   k_zero64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)b);
   AC3D_CUDA(cudaGetLastError());
 }
 void launch_negate64(int n, void* a, cudaStream_t s) {
+  note_launch();
   k_negate64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)a);
   AC3D_CUDA(cudaGetLastError());
 }
 int launch_norm2_64(int n, const void* a, double* partials, cudaStream_t s) {
+  note_launch();
   k_norm2_64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (const cd*)a, partials);
   AC3D_CUDA(cudaGetLastError());
   return vec_grid(n);
 }
 void launch_reduce5(const double* partials, int n, double* out, cudaStream_t s) {
+  note_launch();
   k_reduce5<<<1, kVecThreads, 0, s>>>(partials, n, out);
   AC3D_CUDA(cudaGetLastError());
 }

@@ -124,11 +124,13 @@ void launch_far_field(const DevGeometry& G, int prec, const double4* recv, int L
   const int S = std::max(1, std::min(64, (G.ne + 2047) / 2048));
   scratch.ensure((size_t)L * S * sizeof(cd), s);
   dim3 grid((L + kFFRecv - 1) / kFFRecv, S);
+  note_launch();
   if (prec == PREC_FP64)
     far_kernel<double><<<grid, kFFThreads, 0, s>>>(geo_view<double>(G), recv, L, k, x, scratch.as<cd>(), S);
   else
     far_kernel<float><<<grid, kFFThreads, 0, s>>>(geo_view<float>(G), recv, L, (float)k, x, scratch.as<cd>(), S);
   AC3D_CUDA(cudaGetLastError());
+  note_launch();
   far_reduce_kernel<<<(L + 127) / 128, 128, 0, s>>>(scratch.as<cd>(), L, S, y);
   AC3D_CUDA(cudaGetLastError());
 }
@@ -136,6 +138,7 @@ void launch_far_field(const DevGeometry& G, int prec, const double4* recv, int L
 void launch_far_field_t(const DevGeometry& G, int prec, const double4* recv, int L, double k, const cd* vf, cd* out,
                         cudaStream_t s) {
   const int nb = (G.ne + kFFThreads - 1) / kFFThreads;
+  note_launch();
   if (prec == PREC_FP64)
     far_t_kernel<double><<<nb, kFFThreads, 0, s>>>(geo_view<double>(G), recv, L, k, vf, out);
   else
@@ -237,24 +240,31 @@ void launch_lr_apply(int prec, const void* pool, const long long* toff, const in
   const int nb = std::max(1, (iter_lim * 32 + 255) / 256);
   const int len = trans ? ne : L;
   if (prec == PREC_FP64) {
+    note_launch();
     lr_dot_kernel<double><<<nb, 256, 0, s>>>((const cd*)pool, toff, rank, L, ne, x, trans, t);
+    note_launch();
     lr_expand_kernel<double><<<(len + 255) / 256, 256, 0, s>>>((const cd*)pool, toff, rank, L, ne, t, trans, out);
   } else {
+    note_launch();
     lr_dot_kernel<float><<<nb, 256, 0, s>>>((const cf*)pool, toff, rank, L, ne, x, trans, t);
+    note_launch();
     lr_expand_kernel<float><<<(len + 255) / 256, 256, 0, s>>>((const cf*)pool, toff, rank, L, ne, t, trans, out);
   }
   AC3D_CUDA(cudaGetLastError());
 }
 
 void launch_accum_abs(const cd* y, int L, double* yt, cudaStream_t s) {
+  note_launch();
   accum_abs_kernel<<<(L + 255) / 256, 256, 0, s>>>(y, L, yt);
   AC3D_CUDA(cudaGetLastError());
 }
 void launch_compute_u(const double* yt, int L, double* u, double* coef, cudaStream_t s) {
+  note_launch();
   compute_u_kernel<<<1, 1024, 0, s>>>(yt, L, u, coef);
   AC3D_CUDA(cudaGetLastError());
 }
 void launch_vf(const double* u, const cd* y, int L, cd* vf, cudaStream_t s) {
+  note_launch();
   vf_kernel<<<(L + 255) / 256, 256, 0, s>>>(u, y, L, vf);
   AC3D_CUDA(cudaGetLastError());
 }

@@ -26,6 +26,8 @@ struct MvView {
   const int* t_off;
   const long long* term_off;
   const long long* near_off;
+  const int* task_b;
+  const long long* task_off;
   const int* leaf_start;
   const int* near_ptr;
   const int* near_items;
@@ -33,6 +35,15 @@ struct MvView {
   const int* lr_items;
   int na, nleaf, maxk;
 };
+
+// acc (ar, ai) += a * x with the product formed in the accumulator precision
+template <typename AT, typename A, typename X>
+__device__ __forceinline__ void cmac(AT& ar, AT& ai, const A& a, const X& x) {
+  ar = fma((AT)a.re, (AT)x.re, ar);
+  ar = fma(-(AT)a.im, (AT)x.im, ar);
+  ai = fma((AT)a.re, (AT)x.im, ai);
+  ai = fma((AT)a.im, (AT)x.re, ai);
+}
 
 template <typename MT, typename VT, typename AT>
 __global__ void __launch_bounds__(256) mv_phase1(MvView V, const cplx<MT>* __restrict__ pool,
@@ -44,20 +55,10 @@ __global__ void __launch_bounds__(256) mv_phase1(MvView V, const cplx<MT>* __res
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int task = gw; task < total; task += nw) {
-    // block b with t_off[b] <= task < t_off[b + 1]
-    int lo = 0, hi = V.na - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (V.t_off[mid] <= task)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const int b = lo;
-    const int q = task - V.t_off[b];
+    const int b = V.task_b[task];
+    const cplx<MT>* vec = pool + V.task_off[task];
     const int4 blk = V.blocks_a[b];
     const int m = blk.y - blk.x, n = blk.w - blk.z;
-    const cplx<MT>* vec = pool + V.term_off[(long long)b * V.maxk + q];
     const cplx<VT>* xs;
     int len;
     if (!transposed) {
@@ -70,26 +71,15 @@ __global__ void __launch_bounds__(256) mv_phase1(MvView V, const cplx<MT>* __res
     }
     AT ar = 0, ai = 0, br = 0, bi = 0;
     int i = lane;
-    for (; i + 32 < len; i += 64) {
-      cplx<MT> a0 = vec[i], a1 = vec[i + 32];
-      cplx<VT> x0 = xs[i], x1 = xs[i + 32];
-      ar = fma((AT)a0.re, (AT)x0.re, ar);
-      ar = fma(-(AT)a0.im, (AT)x0.im, ar);
-      ai = fma((AT)a0.re, (AT)x0.im, ai);
-      ai = fma((AT)a0.im, (AT)x0.re, ai);
-      br = fma((AT)a1.re, (AT)x1.re, br);
-      br = fma(-(AT)a1.im, (AT)x1.im, br);
-      bi = fma((AT)a1.re, (AT)x1.im, bi);
-      bi = fma((AT)a1.im, (AT)x1.re, bi);
+    for (; i + 96 < len; i += 128) {
+      cplx<MT> a0 = vec[i], a1 = vec[i + 32], a2 = vec[i + 64], a3 = vec[i + 96];
+      cplx<VT> x0 = xs[i], x1 = xs[i + 32], x2 = xs[i + 64], x3 = xs[i + 96];
+      cmac<AT>(ar, ai, a0, x0);
+      cmac<AT>(br, bi, a1, x1);
+      cmac<AT>(ar, ai, a2, x2);
+      cmac<AT>(br, bi, a3, x3);
     }
-    if (i < len) {
-      cplx<MT> a0 = vec[i];
-      cplx<VT> x0 = xs[i];
-      ar = fma((AT)a0.re, (AT)x0.re, ar);
-      ar = fma(-(AT)a0.im, (AT)x0.im, ar);
-      ai = fma((AT)a0.re, (AT)x0.im, ai);
-      ai = fma((AT)a0.im, (AT)x0.re, ai);
-    }
+    for (; i < len; i += 32) cmac<AT>(ar, ai, vec[i], xs[i]);
     ar = warp_sum(ar + br);
     ai = warp_sum(ai + bi);
     if (lane == 0) tvec[task] = cplx<AT>(ar, ai);
@@ -131,26 +121,16 @@ __global__ void __launch_bounds__(kGatherThreads) mv_gather(MvView V, const cplx
         if (active) {
           int c = 0;
           AT br = 0, bi = 0;
-          for (; c + 1 < n; c += 2) {
-            cplx<MT> d0 = D[(size_t)c * R + row], d1 = D[(size_t)(c + 1) * R + row];
-            cplx<VT> x0 = xs[c], x1 = xs[c + 1];
-            accr = fma((AT)d0.re, (AT)x0.re, accr);
-            accr = fma(-(AT)d0.im, (AT)x0.im, accr);
-            acci = fma((AT)d0.re, (AT)x0.im, acci);
-            acci = fma((AT)d0.im, (AT)x0.re, acci);
-            br = fma((AT)d1.re, (AT)x1.re, br);
-            br = fma(-(AT)d1.im, (AT)x1.im, br);
-            bi = fma((AT)d1.re, (AT)x1.im, bi);
-            bi = fma((AT)d1.im, (AT)x1.re, bi);
+          const cplx<MT>* Dr = D + row;
+          for (; c + 3 < n; c += 4) {
+            cplx<MT> d0 = Dr[(size_t)c * R], d1 = Dr[(size_t)(c + 1) * R], d2 = Dr[(size_t)(c + 2) * R],
+                     d3 = Dr[(size_t)(c + 3) * R];
+            cmac<AT>(accr, acci, d0, xs[c]);
+            cmac<AT>(br, bi, d1, xs[c + 1]);
+            cmac<AT>(accr, acci, d2, xs[c + 2]);
+            cmac<AT>(br, bi, d3, xs[c + 3]);
           }
-          if (c < n) {
-            cplx<MT> d0 = D[(size_t)c * R + row];
-            cplx<VT> x0 = xs[c];
-            accr = fma((AT)d0.re, (AT)x0.re, accr);
-            accr = fma(-(AT)d0.im, (AT)x0.im, accr);
-            acci = fma((AT)d0.re, (AT)x0.im, acci);
-            acci = fma((AT)d0.im, (AT)x0.re, acci);
-          }
+          for (; c < n; c++) cmac<AT>(accr, acci, Dr[(size_t)c * R], xs[c]);
           accr += br;
           acci += bi;
         }
@@ -176,17 +156,23 @@ __global__ void __launch_bounds__(kGatherThreads) mv_gather(MvView V, const cplx
       const int4 blk = V.blocks_a[b];
       const int rk = V.rank[b];
       const cplx<AT>* tb = tvec + V.t_off[b];
-      const long long* to = V.term_off + (long long)b * V.maxk;
       const int off = TRANS ? (blk.y - blk.x) + (ls - blk.z) : (ls - blk.x);
       if (active) {
-        for (int q = 0; q < rk; q++) {
-          cplx<MT> u = pool[to[q] + off + row];
-          cplx<AT> t = tb[q];
-          accr = fma((AT)u.re, t.re, accr);
-          accr = fma(-(AT)u.im, t.im, accr);
-          acci = fma((AT)u.re, t.im, acci);
-          acci = fma((AT)u.im, t.re, acci);
+        const long long* tob = V.task_off + V.t_off[b];
+        const cplx<MT>* base = pool + off + row;
+        int q = 0;
+        AT br = 0, bi = 0;
+        for (; q + 3 < rk; q += 4) {
+          const long long o0 = tob[q], o1 = tob[q + 1], o2 = tob[q + 2], o3 = tob[q + 3];
+          cplx<MT> u0 = base[o0], u1 = base[o1], u2 = base[o2], u3 = base[o3];
+          cmac<AT>(accr, acci, u0, tb[q]);
+          cmac<AT>(br, bi, u1, tb[q + 1]);
+          cmac<AT>(accr, acci, u2, tb[q + 2]);
+          cmac<AT>(br, bi, u3, tb[q + 3]);
         }
+        for (; q < rk; q++) cmac<AT>(accr, acci, base[tob[q]], tb[q]);
+        accr += br;
+        acci += bi;
       }
     }
     part[g][row] = cplx<AT>(accr, acci);
@@ -246,6 +232,8 @@ static MvView mv_view(const DevPartition& DP, const DevHMat& H, bool tr) {
   v.t_off = H.t_off.as<int>();
   v.term_off = H.term_off.as<long long>();
   v.near_off = DP.near_off.as<long long>();
+  v.task_b = H.task_b.as<int>();
+  v.task_off = H.task_off.as<long long>();
   v.leaf_start = DP.leaf_start.as<int>();
   v.near_ptr = tr ? DP.tr_near_ptr.as<int>() : DP.fw_near_ptr.as<int>();
   v.near_items = tr ? DP.tr_near.as<int>() : DP.fw_near.as<int>();
@@ -272,10 +260,12 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
                  const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s) {
   MvView v = mv_view(DP, H, tr);
   if (DP.na > 0) {
+    note_launch();
     mv_phase1<MT, VT, AT><<<device_sm_count() * 4, 256, 0, s>>>(v, H.pool.as<cplx<MT>>(), (const cplx<VT>*)x,
                                                         (cplx<AT>*)tvec, tr ? 1 : 0, done);
     AC3D_CUDA(cudaGetLastError());
   }
+  note_launch();
   if (tr)
     mv_gather<MT, VT, AT, true><<<DP.nleaf, kGatherThreads, 0, s>>>(
         v, H.near.as<cplx<MT>>(), H.pool.as<cplx<MT>>(), (const cplx<AT>*)tvec, (const cplx<VT>*)x, (cplx<VT>*)y,

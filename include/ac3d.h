@@ -53,6 +53,7 @@ typedef struct ac3d_stats {
   double rel_residual;      /* final |b - A x| / |b| of the last solve (FP64) */
   int converged;            /* 1 if every solve met solver_tol */
   double ms_assemble, ms_solve, ms_listener, ms_adjoint, ms_total;
+  long long kernel_launches; /* kernels this library launched in the call (graph nodes counted) */
 } ac3d_stats;
 
 /* DiffBEM(cluster_size, radius_factor, freq_bands, n_freqs, approx_ACA_tol, Q_ACA_tol,
@@ -62,6 +63,10 @@ int ac3d_create(ac3d_ctx** ctx, int cluster_size, double radius_factor, const do
                 int n_freqs, double approx_aca_tol, double q_aca_tol, double solver_tol, const double* src_pt,
                 double listener_radius, double listener_ds, int recompute_matrices);
 void ac3d_destroy(ac3d_ctx* ctx);
+/* Selects the CUDA device used by contexts created afterwards on the calling host thread
+ * (the library carries its own CUDA runtime, so another runtime's current device does not
+ * carry over). No reference counterpart: the reference is CPU-only. */
+int ac3d_select_device(int device);
 const char* ac3d_last_error(const ac3d_ctx* ctx);
 
 /* Options with no reference counterpart (the reference is FP64, point source, ACA receivers). */
@@ -92,6 +97,10 @@ int ac3d_set_points(ac3d_ctx* ctx, const double* Ps);
 /* pvals(frequency[, listeners]) -- acoustics3d.cpp:236-280. Ls may be NULL (context receivers);
  * out receives L complex pressures. */
 int ac3d_pressures(ac3d_ctx* ctx, double frequency, const double* Ls, int L, double* out);
+/* Same as ac3d_pressures with receivers (L x 3 float64) and output (L complex) in device memory,
+ * ordered after `stream` (a cudaStream_t), which waits for completion. Ls_dev may be NULL
+ * (context receivers). No host copies of inputs or outputs. */
+int ac3d_pressures_dev(ac3d_ctx* ctx, double frequency, const double* Ls_dev, int L, double* out_dev, void* stream);
 /* surface_vals(frequency) -- acoustics3d.cpp:282-315; out receives Ne complex values. */
 int ac3d_surface_values(ac3d_ctx* ctx, double frequency, double* out);
 /* band_value(freq_band) -- acoustics3d.cpp:162-176. */
@@ -114,6 +123,11 @@ int ac3d_sphere(const double* Ps, int V, const int32_t* Es, int Ne, double freq,
                 double* out);
 
 int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
+/* Times `iters` back-to-back H-matrix matvecs (y = op(A) x, inner-solve precision) on the
+ * H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, with CUDA events on the
+ * context stream. Outputs the mean milliseconds per matvec and the algorithmic bytes per matvec:
+ * stored matrix entries x entry size + 16 Ne (read x, write y). No reference counterpart. */
+int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_matvec, long long* bytes);
 
 /* Host-only cluster tree and block partition (ClusterTree, clustertree.cpp:49-137, as used by
  * set_mesh, acoustics3d.cpp:43-58). No GPU work: for inspection and tests. */

@@ -67,10 +67,10 @@ def test_repeatable_bitwise(gpu_lib):
     assert np.array_equal(y1, y2)
 
 
-def small_diffbem(oracle_lib, precision, recompute=False, listener="dense"):
+def small_diffbem(oracle_lib, precision, recompute=False, listener="dense", tol=1e-6):
     R = cases.meshes.relief(0.3, 0.3, 0.05, 10, 2, 10, 0, cases.meshes.smooth_heightmap(16, 2))
-    kw = dict(cluster_size=16, radius_factor=1.5, freq_bands=[1000.0, 2000.0], n_freqs=3, approx_ACA_tol=1e-6,
-              Q_ACA_tol=1e-6, solver_tol=1e-9, src_pt=(0.0, 100.0, 0.0), listener_radius=50, listener_ds=15,
+    kw = dict(cluster_size=16, radius_factor=1.5, freq_bands=[1000.0, 2000.0], n_freqs=3, approx_ACA_tol=tol,
+              Q_ACA_tol=tol, solver_tol=1e-9, src_pt=(0.0, 100.0, 0.0), listener_radius=50, listener_ds=15,
               recompute_matrices=recompute)
     gpu = DiffBEM(**kw, precision=precision, listener=listener)
     gpu.silent = True
@@ -105,7 +105,11 @@ def test_gradient_vs_oracle(oracle_lib, gpu_lib, precision, recompute, listener)
 
 
 def test_gradient_vs_finite_differences(oracle_lib, gpu_lib):
-    gpu, orc, R = small_diffbem(oracle_lib, "fp64")
+    """Central differences (h = 1e-5 m) of the coefficient against the adjoint gradient. ACA pivots
+    may switch between x + h and x - h, and such a switch moves c by about the ACA tolerance, which
+    the difference quotient amplifies by 1/2h; the forward model is therefore made smooth with an
+    ACA tolerance of 1e-12 (the low-rank factors then reproduce their blocks to rounding)."""
+    gpu, orc, R = small_diffbem(oracle_lib, "fp64", tol=1e-12)
     gpu.set_band(1000.0)
     x = np.random.default_rng(7).uniform(0, 0.02, size=len(R.diff_pts))
     c, g = gpu.gradient(x)
