@@ -195,8 +195,11 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
   H->k = k;
   H->maxk = c->maxk;
   const size_t cs = prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
-  H->near.alloc((size_t)std::max<int64_t>(c->P.near_total, 1) * cs, s);
+  H->near.alloc((size_t)std::max<int64_t>(c->P.near_total, 2) * cs, s);
+  AC3D_CUDA(cudaMemsetAsync(H->near.p, 0, (size_t)std::max<int64_t>(c->P.near_total, 2) * cs, s));
   launch_near_assembly(c->G, c->DP, *H, s);
+  H->err.alloc(16, s);
+  AC3D_CUDA(cudaMemsetAsync(H->err.p, 0, 16, s));
   const int na = c->DP.na;
   H->rank.alloc((size_t)std::max(na, 1) * sizeof(int), s);
   H->t_off.alloc((size_t)(na + 1) * sizeof(int), s);
@@ -225,6 +228,7 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     }
     c->pool_hint[prec] = std::min<int64_t>(c->worst_pool, H->pool_used_host + H->pool_used_host / 8 + 4096);
     const size_t tcap = (size_t)std::max<int64_t>(c->P.aca_term_cap, 1);
+    H->task_cap = (int64_t)tcap;
     H->task_b.alloc(tcap * sizeof(int), s);
     H->task_off.alloc(tcap * sizeof(long long), s);
     launch_rank_scan(c->DP, *H, s);
@@ -245,12 +249,58 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     }
     H->lr_entries = lr;
     c->stats.lr_entries = lr;
+    // per-leaf segments (U by row leaf, V by column leaf), then the pool is released
+    int64_t sum_rn = 0, kf = 0, kt = 0;
+    for (int b = 0; b < na; b++) sum_rn += (int64_t)H->ranks_host[b] * (c->P.approx[4 * b + 3] - c->P.approx[4 * b + 2]);
+    const int nleaf = c->DP.nleaf;
+    int64_t segf = 0, segt = 0;
+    for (int l = 0; l < nleaf; l++) {
+      const int Rl = c->P.leaf_start[l + 1] - c->P.leaf_start[l];
+      int K = 0;
+      for (int it = c->P.fw_lr_ptr[l]; it < c->P.fw_lr_ptr[l + 1]; it++) K += H->ranks_host[c->P.fw_lr[it]];
+      K += K & 1;
+      kf += K;
+      segf += (int64_t)K * Rl;
+      K = 0;
+      for (int it = c->P.tr_lr_ptr[l]; it < c->P.tr_lr_ptr[l + 1]; it++) K += H->ranks_host[c->P.tr_lr[it]];
+      K += K & 1;
+      kt += K;
+      segt += (int64_t)K * Rl;
+    }
+    H->kseg_f.alloc((size_t)(nleaf + 1) * sizeof(int), s);
+    H->kseg_t.alloc((size_t)(nleaf + 1) * sizeof(int), s);
+    H->seg_f.alloc((size_t)(nleaf + 1) * sizeof(long long), s);
+    H->seg_t.alloc((size_t)(nleaf + 1) * sizeof(long long), s);
+    H->useg.alloc((size_t)std::max<int64_t>(segf, 2) * cs, s);
+    H->vseg.alloc((size_t)std::max<int64_t>(segt, 2) * cs, s);
+    H->uidx.alloc((size_t)std::max<int64_t>(kf, 1) * sizeof(int), s);
+    H->vidx.alloc((size_t)std::max<int64_t>(kt, 1) * sizeof(int), s);
+    H->kpos_f.alloc((size_t)std::max<size_t>(c->P.fw_lr.size(), 1) * sizeof(int), s);
+    H->kpos_t.alloc((size_t)std::max<size_t>(c->P.tr_lr.size(), 1) * sizeof(int), s);
+    H->pbuf.alloc((size_t)std::max<int64_t>(std::max(kf, kt), 1) * sizeof(cd), s);
+    launch_pack(c->DP, *H, false, s);
+    launch_pack(c->DP, *H, true, s);
+    H->pool.release();
+    H->term_off.release();
+    (void)sum_rn;
     c->stats.max_rank = mx;
     c->stats.mean_rank = sr / na;
   } else {
     AC3D_CUDA(cudaMemsetAsync(H->t_off.p, 0, sizeof(int), s));
     H->tvec.alloc(16, s);
     H->tvec64.alloc(16, s);
+    for (DevBuf* kb : {&H->kseg_f, &H->kseg_t}) {
+      kb->alloc((size_t)(c->DP.nleaf + 1) * sizeof(int), s);
+      AC3D_CUDA(cudaMemsetAsync(kb->p, 0, (size_t)(c->DP.nleaf + 1) * sizeof(int), s));
+    }
+    for (DevBuf* sb : {&H->seg_f, &H->seg_t}) {
+      sb->alloc((size_t)(c->DP.nleaf + 1) * sizeof(long long), s);
+      AC3D_CUDA(cudaMemsetAsync(sb->p, 0, (size_t)(c->DP.nleaf + 1) * sizeof(long long), s));
+    }
+    H->useg.alloc(32, s);
+    H->vseg.alloc(32, s);
+    H->uidx.alloc(16, s);
+    H->vidx.alloc(16, s);
   }
   c->stats.near_entries = c->P.near_total;
   c->stats.hmat_bytes = (long long)H->bytes();
@@ -277,6 +327,7 @@ void ensure_work(ac3d_ctx* c) {
   c->r64.ensure(n * sizeof(cd), s);
   if (!c->h_state) AC3D_CUDA(cudaMallocHost(&c->h_state, 2 * sizeof(KState)));
   (void)device_sm_count();  // query outside any stream capture
+  prepare_matvec_kernels();
   if (!c->h_red) AC3D_CUDA(cudaMallocHost(&c->h_red, 8 * sizeof(double)));
 }
 
@@ -361,7 +412,21 @@ double reduce_norm2_residual(ac3d_ctx* c, const DevHMat& H, bool tr, const cd* b
 }
 
 // x = op(A)^{-1} b to relative residual solver_tol (FP64 b, x on device).
-void solve(ac3d_ctx* c, const DevHMat& H, const cd* b, cd* x, bool tr) {
+void check_pipeline(ac3d_ctx* c, const DevHMat& H) {
+  int e = 0;
+  AC3D_CUDA(cudaMemcpyAsync(&e, H.err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  AC3D_CUDA(cudaStreamSynchronize(c->stream));
+  if (e) throw Error(AC3D_ERR_CUDA, "matvec copy pipeline timed out (bounded mbarrier wait)");
+}
+
+void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr);
+
+void solve(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
+  solve_impl(c, H, b, x, tr);
+  check_pipeline(c, H);
+}
+
+void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   cudaStream_t s = c->stream;
   ensure_work(c);
   const int n = c->Ne;
@@ -803,6 +868,14 @@ int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int N
     std::vector<long long> no(c->P.near_off.begin(), c->P.near_off.end());
     upload(DP.near_off, no, s);
     upload(DP.aca_order, c->P.aca_order, s);
+    DP.naca = (int)c->P.aca_order.size();
+    upload(DP.near_seg, std::vector<long long>(c->P.near_seg.begin(), c->P.near_seg.end()), s);
+    upload(DP.didx_ptr, c->P.didx_ptr, s);
+    upload(DP.didx, c->P.didx, s);
+    upload(DP.blk_fw_ptr, c->P.blk_fw_ptr, s);
+    upload(DP.blk_fw, c->P.blk_fw, s);
+    upload(DP.blk_tr_ptr, c->P.blk_tr_ptr, s);
+    upload(DP.blk_tr, c->P.blk_tr, s);
     c->sum_mn = 0;
     c->worst_pool = 0;
     for (int b = 0; b < DP.na; b++) {

@@ -132,6 +132,35 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
   unsigned* used = (unsigned*)(toff + A.iter_cap);
 
   const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
+
+  // Exactly-zero blocks: every source element lies in one axis-aligned plane x_d = v (edge
+  // vectors have an exact zero d-component) that also holds every target point exactly. Then
+  // r_d = 0 and the normal has no other component, each quadrature term is exactly 0, and the
+  // iteration below would produce only zero terms, none of which is stored. Checked on the
+  // current geometry, so height updates are honoured.
+  if (A.zero_guard && iter_lim > 0) {
+    int zero_axes = 0;
+    for (int d = 0; d < 3; d++) {
+      const double v = d == 0 ? A.G.va[cs].x : (d == 1 ? A.G.va[cs].y : A.G.va[cs].z);
+      int ok = 1;
+      for (int j = tid; j < n && ok; j += T) {
+        const double4 a = A.G.va[cs + j];
+        const ElemGeo<R> g = A.G.eg[cs + j];
+        const double ad = d == 0 ? a.x : (d == 1 ? a.y : a.z);
+        ok = ad == v && g.ab[d] == R(0) && g.ac[d] == R(0);
+      }
+      for (int i = tid; i < m && ok; i += T) {
+        const double4 p = A.G.cen[rs + i];
+        ok = (d == 0 ? p.x : (d == 1 ? p.y : p.z)) == v;
+      }
+      if (__syncthreads_and(ok)) zero_axes++;
+    }
+    if (zero_axes) {
+      if (tid == 0) A.rank[b] = 0;
+      return;
+    }
+  }
+
   for (int w = tid; w < (m + 31) / 32; w += T) used[w] = 0;
   __syncthreads();
   if (tid == 0) used[0] = 1u;
@@ -320,13 +349,13 @@ void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double
                                G.cen.as<double4>(), H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cd>(),
                                H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
                                H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
-    aca_launch_t(a, DP.na, max_rows, s);
+    if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
   } else {
     AcaArgs<float, float4> a{geo_view<float>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
                              G.cen32.as<float4>(), (float)H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cf>(),
                              H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
                              H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
-    aca_launch_t(a, DP.na, max_rows, s);
+    if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
   }
 }
 

@@ -84,8 +84,16 @@ struct Partition {
   std::vector<int> fw_lr_ptr, fw_lr;       // admissible blocks whose rows contain the leaf
   std::vector<int> tr_near_ptr, tr_near;   // near blocks whose columns are the leaf
   std::vector<int> tr_lr_ptr, tr_lr;       // admissible blocks whose columns contain the leaf
-  std::vector<int64_t> near_off;       // element offset of each near block (column-major storage)
+  std::vector<int64_t> near_off;       // element offset of each near block (column-major storage);
+                                       // blocks of one row leaf are consecutive, so a leaf's near data is
+                                       // one R x NC column-major segment
   int64_t near_total = 0;
+  std::vector<int64_t> near_seg;       // per leaf: element offset of its near segment
+  std::vector<int> didx_ptr, didx;     // per leaf: global column index of every near-segment column
+  // per admissible block: its entries in the fw_lr / tr_lr lists (one per row / column leaf),
+  // in leaf order; the matvec sums a term's per-leaf partial dots over these
+  std::vector<int> blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
+  std::vector<int> iter_lim;           // per admissible block: min(maxk, m - 1, n - 1)
   std::vector<int> aca_order;          // admissible blocks by decreasing m + n
   int max_rows = 0;                    // largest admissible block row count
   int64_t aca_term_cap = 0;            // sum over blocks of min(maxk, m-1, n-1)
@@ -101,6 +109,9 @@ void build_leaf_lists(Partition& P, int maxk);
 // ------------------------------------------------------------------------------------------
 struct DevPartition {
   int nleaf = 0, nd = 0, na = 0;
+  int naca = 0;  // admissible blocks launched for ACA
+  DevBuf near_seg, didx_ptr, didx;
+  DevBuf blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
   DevBuf blocks_d, blocks_a;            // int4
   DevBuf leaf_start;                    // int (nleaf + 1)
   DevBuf fw_near_ptr, fw_near, fw_lr_ptr, fw_lr;
@@ -134,6 +145,15 @@ struct DevHMat {
   DevBuf t_off;           // int [na + 1] prefix of ranks
   DevBuf task_b;          // int [sum ranks] block of each stored term
   DevBuf task_off;        // int64 [sum ranks] pool offset of each stored term
+  // per-leaf segments packed from the pool after ACA (the pool is released afterwards)
+  DevBuf kseg_f, kseg_t;  // int [nleaf + 1]: prefix of (even-padded) segment columns per row / column leaf
+  DevBuf seg_f, seg_t;    // int64 [nleaf + 1]: element prefix of the U / V segments
+  DevBuf useg, vseg;      // R x K column-major slices of U (row leaves) / V (column leaves)
+  DevBuf uidx, vidx;      // int: phase-1 output index of every segment column (-1: padding)
+  DevBuf kpos_f, kpos_t;  // int: first segment column of every fw_lr / tr_lr list entry
+  DevBuf pbuf;            // per-column partial dots of the dot pass
+  DevBuf err;             // int: set by a kernel whose copy pipeline timed out
+  int64_t task_cap = 0;   // upper bound of the number of stored terms
   DevBuf tvec;            // intermediate V x per term (complex, vector precision)
   DevBuf tvec64;          // FP64 intermediate for refinement residuals
   DevBuf pool_used;       // unsigned long long
@@ -143,7 +163,8 @@ struct DevHMat {
   int64_t lr_entries = 0; // sum r (m + n)
   size_t bytes() const {
     return near.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
-           tvec.bytes + tvec64.bytes;
+           tvec.bytes + tvec64.bytes + useg.bytes + vseg.bytes + uidx.bytes + vidx.bytes + kpos_f.bytes +
+           kpos_t.bytes + pbuf.bytes + kseg_f.bytes + kseg_t.bytes + seg_f.bytes + seg_t.bytes;
   }
 };
 
@@ -157,6 +178,8 @@ void launch_rhs(const DevGeometry& G, int prec_vec64, double k, int kind, const 
 void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s);
 void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s);
 void launch_rank_scan(const DevPartition& DP, DevHMat& H, cudaStream_t s);
+// Packs the pool into the U segments (row leaves, cols = false) or V segments (column leaves).
+void launch_pack(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_t s);
 
 // Matvec y = op(A) x with op = identity or plain transpose. vec: 0 = complex FP32 vectors,
 // 1 = complex FP64 vectors. residual: y = b - op(A) x instead (b given).
@@ -170,5 +193,7 @@ void launch_matvec(const DevPartition& DP, const DevHMat& H, int ne, bool transp
                    const void* x, void* y, const void* b_minus, const MatvecEpilogue& ep, cudaStream_t s);
 int matvec_grid(const DevPartition& DP, bool transposed);
 int device_sm_count();
+// Sets the shared-memory limits of the matvec kernels (call outside stream capture).
+void prepare_matvec_kernels();
 
 }  // namespace ac3d

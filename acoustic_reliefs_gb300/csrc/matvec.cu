@@ -1,42 +1,30 @@
 // H-matrix matvec y = op(K - I/2) x (generic_product_impl::scaleAndAddTo, hmatrix.h:84-139),
 // op = identity or the plain (non-conjugate) transpose.
 //
-// Two kernels, no atomics, fixed summation order:
-//   phase 1: one warp per rank-1 term (b, q): t[b, q] = v_{b,q} . x[cols(b)]  (forward) or
-//            u_{b,q} . x[rows(b)] (transpose). Term vectors are contiguous in the pool.
-//   gather : one CTA per leaf cluster. Forward: rows of the leaf accumulate their near blocks
-//            (column-major, lane = row, coalesced) and the leaf's slice of every admissible block
-//            covering it (u_{b,q}[slice] t[b,q]); transpose: columns of the leaf accumulate the
-//            transposed near blocks and slices v_{b,q}[slice] t[b,q]. Then y = -x/2 + sum, or
-//            y = b - (that) for refinement residuals, with optional fused FP64 dot partials.
+// The matrix is held as per-leaf segments (R x K column-major, R = leaf size):
+//   near segment of a row leaf   : its dense blocks side by side, columns indexing x;
+//   U segment of a row leaf      : rows of the leaf of every admissible block above it, one column
+//                                  per rank-1 term;
+//   V segment of a column leaf   : columns of the leaf of every admissible block beside it.
+// Forward:    p = per-column dots of the V segments with x   (dot pass, one CTA per leaf)
+//             t[b, q] = sum over the column leaves of b of p (reduce, fixed leaf order)
+//             y = -x/2 + near x + U t                         (gather pass, one CTA per leaf)
+// Transpose:  the same with U and V swapped, plus the dense blocks read column-wise.
+// Both passes stream their segments through shared memory with bulk async copies, so the bytes
+// in flight are set by the copy ring, not by how many loads a warp can issue. No atomics; every
+// sum has a fixed order, so results are bit-reproducible.
 #include "common.cuh"
 #include "internal.h"
+#include "segstream.cuh"
 
 namespace ac3d {
 
 namespace {
-constexpr int kGatherThreads = 256;
-constexpr int kGatherWarps = kGatherThreads / 32;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxRpl = 8;  // rows per lane (leaf size <= 256)
 }  // namespace
 
-struct MvView {
-  const int4* blocks_a;
-  const int4* blocks_d;
-  const int* rank;
-  const int* t_off;
-  const long long* term_off;
-  const long long* near_off;
-  const int* task_b;
-  const long long* task_off;
-  const int* leaf_start;
-  const int* near_ptr;
-  const int* near_items;
-  const int* lr_ptr;
-  const int* lr_items;
-  int na, nleaf, maxk;
-};
-
-// acc (ar, ai) += a * x with the product formed in the accumulator precision
 template <typename AT, typename A, typename X>
 __device__ __forceinline__ void cmac(AT& ar, AT& ai, const A& a, const X& x) {
   ar = fma((AT)a.re, (AT)x.re, ar);
@@ -45,171 +33,280 @@ __device__ __forceinline__ void cmac(AT& ar, AT& ai, const A& a, const X& x) {
   ai = fma((AT)a.im, (AT)x.re, ai);
 }
 
-template <typename MT, typename VT, typename AT>
-__global__ void __launch_bounds__(256) mv_phase1(MvView V, const cplx<MT>* __restrict__ pool,
-                                                 const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ tvec,
-                                                 int transposed, const int* __restrict__ done) {
-  if (done && *done) return;
-  const int total = V.t_off[V.na];
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int task = gw; task < total; task += nw) {
-    const int b = V.task_b[task];
-    const cplx<MT>* vec = pool + V.task_off[task];
-    const int4 blk = V.blocks_a[b];
-    const int m = blk.y - blk.x, n = blk.w - blk.z;
-    const cplx<VT>* xs;
-    int len;
-    if (!transposed) {
-      vec += m;
-      xs = x + blk.z;
-      len = n;
+struct SegView {
+  const int* leaf_start;
+  // region A: near segments (forward gather only)
+  const long long* a_seg;
+  const int* a_kptr;
+  const int* a_idx;
+  // region B: low-rank segments
+  const long long* b_seg;
+  const int* b_kptr;
+  const int* b_idx;
+  // transposed dense blocks
+  const int4* blocks_d;
+  const long long* near_off;
+  const int* trn_ptr;
+  const int* trn;
+  int* err;
+};
+
+// Iterates the chunks of the (up to two) regions of one leaf through the copy ring and calls
+// fn(stage_ptr, region, first_column, columns) for each chunk, all threads together.
+template <typename MT, typename F>
+__device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes], uint64_t* full, int R,
+                                            const cplx<MT>* a_ptr, int a_cols, const cplx<MT>* b_ptr, int b_cols,
+                                            int* err, F&& fn) {
+  const int cpc = max(2, (int)(kStageBytes / sizeof(cplx<MT>)) / R & ~1);  // columns per chunk, even
+  const int na = (a_cols + cpc - 1) / cpc, nb = (b_cols + cpc - 1) / cpc;
+  const int nch = na + nb;
+  auto chunk = [&](int c, const cplx<MT>*& src, int& region, int& c0, int& ncols) {
+    if (c < na) {
+      region = 0;
+      c0 = c * cpc;
+      ncols = min(cpc, a_cols - c0);
+      src = a_ptr + (long long)c0 * R;
     } else {
-      xs = x + blk.x;
-      len = m;
+      region = 1;
+      c0 = (c - na) * cpc;
+      ncols = min(cpc, b_cols - c0);
+      src = b_ptr + (long long)c0 * R;
     }
-    AT ar = 0, ai = 0, br = 0, bi = 0;
-    int i = lane;
-    for (; i + 96 < len; i += 128) {
-      cplx<MT> a0 = vec[i], a1 = vec[i + 32], a2 = vec[i + 64], a3 = vec[i + 96];
-      cplx<VT> x0 = xs[i], x1 = xs[i + 32], x2 = xs[i + 64], x3 = xs[i + 96];
-      cmac<AT>(ar, ai, a0, x0);
-      cmac<AT>(br, bi, a1, x1);
-      cmac<AT>(ar, ai, a2, x2);
-      cmac<AT>(br, bi, a3, x3);
+  };
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < min(nch, kStages); c++) {
+      const cplx<MT>* src;
+      int region, c0, ncols;
+      chunk(c, src, region, c0, ncols);
+      const uint32_t bytes = (uint32_t)(ncols * R * sizeof(cplx<MT>));
+      mbar_expect_tx(&full[c], bytes);
+      bulk_copy_g2s(stage[c], src, bytes, &full[c]);
     }
-    for (; i < len; i += 32) cmac<AT>(ar, ai, vec[i], xs[i]);
-    ar = warp_sum(ar + br);
-    ai = warp_sum(ai + bi);
-    if (lane == 0) tvec[task] = cplx<AT>(ar, ai);
   }
+  bool ok = true;
+  int c = 0;
+  for (; c < nch; c++) {
+    const int s = c % kStages;
+    const uint32_t parity = (uint32_t)(c / kStages) & 1u;
+    const bool got = mbar_wait_bounded(&full[s], parity);
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    const cplx<MT>* src;
+    int region, c0, ncols;
+    chunk(c, src, region, c0, ncols);
+    fn((const cplx<MT>*)stage[s], region, c0, ncols);
+    __syncthreads();  // every warp is done with stage s
+    if (threadIdx.x == 0 && c + kStages < nch) {
+      fence_proxy_async();
+      const cplx<MT>* src2;
+      int region2, c02, ncols2;
+      chunk(c + kStages, src2, region2, c02, ncols2);
+      const uint32_t bytes = (uint32_t)(ncols2 * R * sizeof(cplx<MT>));
+      mbar_expect_tx(&full[s], bytes);
+      bulk_copy_g2s(stage[s], src2, bytes, &full[s]);
+    }
+  }
+  if (!ok) {
+    // record the failure and let the copies already issued land before the CTA exits
+    if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+      for (int cc = c; cc < min(nch, c + kStages); cc++)
+        mbar_wait_bounded(&full[cc % kStages], (uint32_t)(cc / kStages) & 1u);
+    }
+    __syncthreads();
+  }
+  return ok;
 }
 
-template <typename MT, typename VT, typename AT, bool TRANS>
-__global__ void __launch_bounds__(kGatherThreads) mv_gather(MvView V, const cplx<MT>* __restrict__ near,
-                                                            const cplx<MT>* __restrict__ pool,
-                                                            const cplx<AT>* __restrict__ tvec,
-                                                            const cplx<VT>* __restrict__ x, cplx<VT>* __restrict__ y,
-                                                            const cplx<VT>* __restrict__ bminus,
-                                                            const cplx<VT>* __restrict__ dot_a,
-                                                            const cplx<VT>* __restrict__ dot_b, double* partials,
-                                                            const int* __restrict__ done) {
-  __shared__ cplx<AT> part[kGatherWarps][32 * kGatherWarps];
-  __shared__ double sdot[kGatherWarps][5];
-  if (done && *done) return;
-  const int leaf = blockIdx.x;
-  const int ls = V.leaf_start[leaf], le = V.leaf_start[leaf + 1];
-  const int R = le - ls;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nrw = (R + 31) >> 5;           // warps needed to cover the leaf's rows
-  const int groups = kGatherWarps / nrw;   // independent groups splitting the work list
-  const int g = warp / nrw;
-  const int row = (warp - g * nrw) * 32 + lane;
-  const bool active = g < groups && row < R;
-
-  AT accr = 0, acci = 0;
-  if (g < groups) {
-    // dense near blocks
-    for (int it = V.near_ptr[leaf] + g; it < V.near_ptr[leaf + 1]; it += groups) {
-      const int b = V.near_items[it];
-      const int4 blk = V.blocks_d[b];
-      const cplx<MT>* D = near + V.near_off[b];
-      if (!TRANS) {
-        const int n = blk.w - blk.z;
-        const cplx<VT>* xs = x + blk.z;
-        if (active) {
-          int c = 0;
-          AT br = 0, bi = 0;
-          const cplx<MT>* Dr = D + row;
-          for (; c + 3 < n; c += 4) {
-            cplx<MT> d0 = Dr[(size_t)c * R], d1 = Dr[(size_t)(c + 1) * R], d2 = Dr[(size_t)(c + 2) * R],
-                     d3 = Dr[(size_t)(c + 3) * R];
-            cmac<AT>(accr, acci, d0, xs[c]);
-            cmac<AT>(br, bi, d1, xs[c + 1]);
-            cmac<AT>(accr, acci, d2, xs[c + 2]);
-            cmac<AT>(br, bi, d3, xs[c + 3]);
-          }
-          for (; c < n; c++) cmac<AT>(accr, acci, Dr[(size_t)c * R], xs[c]);
-          accr += br;
-          acci += bi;
-        }
-      } else {
-        const int m = blk.y - blk.x;
-        const cplx<VT>* xs = x + blk.x;
-        if (active) {
-          const cplx<MT>* Dc = D + (size_t)row * m;  // column `row` of the block
-          for (int r = 0; r < m; r++) {
-            cplx<MT> d0 = Dc[r];
-            cplx<VT> x0 = xs[r];
-            accr = fma((AT)d0.re, (AT)x0.re, accr);
-            accr = fma(-(AT)d0.im, (AT)x0.im, accr);
-            acci = fma((AT)d0.re, (AT)x0.im, acci);
-            acci = fma((AT)d0.im, (AT)x0.re, acci);
-          }
-        }
-      }
-    }
-    // low-rank slices
-    for (int it = V.lr_ptr[leaf] + g; it < V.lr_ptr[leaf + 1]; it += groups) {
-      const int b = V.lr_items[it];
-      const int4 blk = V.blocks_a[b];
-      const int rk = V.rank[b];
-      const cplx<AT>* tb = tvec + V.t_off[b];
-      const int off = TRANS ? (blk.y - blk.x) + (ls - blk.z) : (ls - blk.x);
-      if (active) {
-        const long long* tob = V.task_off + V.t_off[b];
-        const cplx<MT>* base = pool + off + row;
-        int q = 0;
-        AT br = 0, bi = 0;
-        for (; q + 3 < rk; q += 4) {
-          const long long o0 = tob[q], o1 = tob[q + 1], o2 = tob[q + 2], o3 = tob[q + 3];
-          cplx<MT> u0 = base[o0], u1 = base[o1], u2 = base[o2], u3 = base[o3];
-          cmac<AT>(accr, acci, u0, tb[q]);
-          cmac<AT>(br, bi, u1, tb[q + 1]);
-          cmac<AT>(accr, acci, u2, tb[q + 2]);
-          cmac<AT>(br, bi, u3, tb[q + 3]);
-        }
-        for (; q < rk; q++) cmac<AT>(accr, acci, base[tob[q]], tb[q]);
-        accr += br;
-        acci += bi;
-      }
-    }
-    part[g][row] = cplx<AT>(accr, acci);
+__device__ __forceinline__ void init_ring(uint64_t* full) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; s++) mbar_init(&full[s], 1);
+    fence_barrier_init();
   }
   __syncthreads();
+}
 
-  // combine groups in fixed order and apply the -x/2 jump term
-  double d[5] = {0, 0, 0, 0, 0};
-  if (threadIdx.x < R) {
-    const int r = threadIdx.x;
-    AT sr = 0, si = 0;
-    for (int gg = 0; gg < groups; gg++) {
-      sr += part[gg][r].re;
-      si += part[gg][r].im;
+// Dot pass: p[kptr[leaf] + k] = sum_rows S[k][row] x[leaf rows] for every column k of the leaf's
+// low-rank segment (region B).
+template <typename MT, typename VT, typename AT>
+__global__ void __launch_bounds__(kThreads) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
+                                                           const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ p,
+                                                           const int* __restrict__ done) {
+  extern __shared__ __align__(128) unsigned char dsmem[];
+  auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
+  __shared__ __align__(8) uint64_t full[kStages];
+  if (done && *done) return;
+  const int leaf = blockIdx.x;
+  const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
+  const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
+  if (K == 0) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rpl = (R + 31) >> 5;
+  AT xr[kMaxRpl], xi[kMaxRpl];
+#pragma unroll
+  for (int j = 0; j < kMaxRpl; j++) {
+    const int row = lane + 32 * j;
+    cplx<VT> v = (j < rpl && row < R) ? x[ls + row] : cplx<VT>();
+    xr[j] = (AT)v.re;
+    xi[j] = (AT)v.im;
+  }
+  init_ring(full);
+  cplx<AT>* out = p + k0;
+  stream_leaf<MT>(stage, full, R, nullptr, 0, lrseg + V.b_seg[leaf], K, V.err,
+                  [&](const cplx<MT>* S, int, int c0, int ncols) {
+                    for (int j = warp; j < ncols; j += kWarps) {
+                      AT ar = 0, ai = 0;
+#pragma unroll
+                      for (int jr = 0; jr < kMaxRpl; jr++) {
+                        const int row = lane + 32 * jr;
+                        if (jr < rpl && row < R) {
+                          const cplx<MT> s = S[j * R + row];
+                          ar = fma((AT)s.re, xr[jr], ar);
+                          ar = fma(-(AT)s.im, xi[jr], ar);
+                          ai = fma((AT)s.re, xi[jr], ai);
+                          ai = fma((AT)s.im, xr[jr], ai);
+                        }
+                      }
+                      ar = warp_sum(ar);
+                      ai = warp_sum(ai);
+                      if (lane == 0) out[c0 + j] = cplx<AT>(ar, ai);
+                    }
+                  });
+}
+
+// t[task] = sum over the leaf entries of the task's block of p[kpos[e] + q], in leaf order.
+template <typename AT>
+__global__ void seg_reduce_kernel(const int* __restrict__ task_b, const int* __restrict__ t_off, int ntask_cap,
+                                  const int* __restrict__ t_total, const int* __restrict__ ent_ptr,
+                                  const int* __restrict__ ent, const int* __restrict__ kpos,
+                                  const cplx<AT>* __restrict__ p, cplx<AT>* __restrict__ t,
+                                  const int* __restrict__ done) {
+  if (done && *done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *t_total || i >= ntask_cap) return;
+  const int b = task_b[i];
+  const int q = i - t_off[b];
+  AT sr = 0, si = 0;
+  for (int e = ent_ptr[b]; e < ent_ptr[b + 1]; e++) {
+    const cplx<AT> v = p[kpos[ent[e]] + q];
+    sr += v.re;
+    si += v.im;
+  }
+  t[i] = cplx<AT>(sr, si);
+}
+
+// Gather pass: y[leaf rows] = -x/2 + S_A x[a_idx] + S_B t[b_idx] (+ transposed dense blocks), or
+// b - that; optional fused FP64 dot partials (conj(a).y, conj(y).b, |y|^2) per leaf.
+template <typename MT, typename VT, typename AT, bool TRANS>
+__global__ void __launch_bounds__(kThreads) seg_gather_kernel(
+    SegView V, const cplx<MT>* __restrict__ near, const cplx<MT>* __restrict__ lrseg, const cplx<AT>* __restrict__ t,
+    const cplx<VT>* __restrict__ x, cplx<VT>* __restrict__ y, const cplx<VT>* __restrict__ bminus,
+    const cplx<VT>* __restrict__ dot_a, const cplx<VT>* __restrict__ dot_b, double* partials,
+    const int* __restrict__ done) {
+  extern __shared__ __align__(128) unsigned char dsmem[];
+  auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
+  __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ double sdot[kWarps][5];
+  if (done && *done) return;
+  const int leaf = blockIdx.x;
+  const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rpl = (R + 31) >> 5;
+  AT ar[kMaxRpl], ai[kMaxRpl];
+#pragma unroll
+  for (int j = 0; j < kMaxRpl; j++) ar[j] = ai[j] = 0;
+
+  const int a_cols = TRANS ? 0 : V.a_kptr[leaf + 1] - V.a_kptr[leaf];
+  const int* a_idx = TRANS ? nullptr : V.a_idx + V.a_kptr[leaf];
+  const int b_cols = V.b_kptr[leaf + 1] - V.b_kptr[leaf];
+  const int* b_idx = V.b_idx + V.b_kptr[leaf];
+  init_ring(full);
+  stream_leaf<MT>(stage, full, R, TRANS ? nullptr : near + V.a_seg[leaf], a_cols, lrseg + V.b_seg[leaf], b_cols,
+                  V.err, [&](const cplx<MT>* S, int region, int c0, int ncols) {
+                    const int* idx = region == 0 ? a_idx : b_idx;
+                    for (int j = warp; j < ncols; j += kWarps) {
+                      const int zi = idx[c0 + j];
+                      if (zi < 0) continue;  // padding column
+                      AT zr, zim;
+                      if (region == 0) {
+                        const cplx<VT> z = x[zi];
+                        zr = (AT)z.re;
+                        zim = (AT)z.im;
+                      } else {
+                        const cplx<AT> z = t[zi];
+                        zr = z.re;
+                        zim = z.im;
+                      }
+#pragma unroll
+                      for (int jr = 0; jr < kMaxRpl; jr++) {
+                        const int row = lane + 32 * jr;
+                        if (jr < rpl && row < R) {
+                          const cplx<MT> s = S[j * R + row];
+                          ar[jr] = fma((AT)s.re, zr, ar[jr]);
+                          ar[jr] = fma(-(AT)s.im, zim, ar[jr]);
+                          ai[jr] = fma((AT)s.re, zim, ai[jr]);
+                          ai[jr] = fma((AT)s.im, zr, ai[jr]);
+                        }
+                      }
+                    }
+                  });
+  if (TRANS) {
+    // dense blocks below this column leaf, read column-wise (lane = column of the leaf)
+    for (int it = V.trn_ptr[leaf] + warp; it < V.trn_ptr[leaf + 1]; it += kWarps) {
+      const int b = V.trn[it];
+      const int4 blk = V.blocks_d[b];
+      const int m = blk.y - blk.x;
+      const cplx<VT>* xs = x + blk.x;
+#pragma unroll
+      for (int jr = 0; jr < kMaxRpl; jr++) {
+        const int col = lane + 32 * jr;
+        if (jr < rpl && col < R) {
+          const cplx<MT>* Dc = near + V.near_off[b] + (long long)col * m;
+          for (int r = 0; r < m; r++) cmac<AT>(ar[jr], ai[jr], Dc[r], xs[r]);
+        }
+      }
     }
-    cplx<VT> xv = x[ls + r];
+  }
+  // combine the warps in fixed order (reusing the ring memory) and apply -x/2
+  cplx<AT>* part = (cplx<AT>*)stage;
+  __syncthreads();
+#pragma unroll
+  for (int jr = 0; jr < kMaxRpl; jr++) {
+    const int row = lane + 32 * jr;
+    if (jr < rpl && row < R) part[warp * R + row] = cplx<AT>(ar[jr], ai[jr]);
+  }
+  __syncthreads();
+  double d[5] = {0, 0, 0, 0, 0};
+  for (int r = threadIdx.x; r < R; r += kThreads) {
+    AT sr = 0, si = 0;
+    for (int w = 0; w < kWarps; w++) {
+      sr += part[w * R + r].re;
+      si += part[w * R + r].im;
+    }
+    const cplx<VT> xv = x[ls + r];
     AT yr = sr - AT(0.5) * (AT)xv.re;
     AT yi = si - AT(0.5) * (AT)xv.im;
     if (bminus) {
-      cplx<VT> bv = bminus[ls + r];
+      const cplx<VT> bv = bminus[ls + r];
       yr = (AT)bv.re - yr;
       yi = (AT)bv.im - yi;
     }
-    cplx<VT> out((VT)yr, (VT)yi);
-    y[ls + r] = out;
-    const double oyr = (double)out.re, oyi = (double)out.im;
+    const cplx<VT> o((VT)yr, (VT)yi);
+    y[ls + r] = o;
+    const double oyr = (double)o.re, oyi = (double)o.im;
     if (dot_a) {  // conj(a) . y
-      cplx<VT> a = dot_a[ls + r];
-      d[0] = (double)a.re * oyr + (double)a.im * oyi;
-      d[1] = (double)a.re * oyi - (double)a.im * oyr;
+      const cplx<VT> a = dot_a[ls + r];
+      d[0] += (double)a.re * oyr + (double)a.im * oyi;
+      d[1] += (double)a.re * oyi - (double)a.im * oyr;
     }
     if (dot_b) {  // conj(y) . b
-      cplx<VT> bb = dot_b[ls + r];
-      d[2] = oyr * (double)bb.re + oyi * (double)bb.im;
-      d[3] = oyr * (double)bb.im - oyi * (double)bb.re;
+      const cplx<VT> bb = dot_b[ls + r];
+      d[2] += oyr * (double)bb.re + oyi * (double)bb.im;
+      d[3] += oyr * (double)bb.im - oyi * (double)bb.re;
     }
-    d[4] = oyr * oyr + oyi * oyi;
+    d[4] += oyr * oyr + oyi * oyi;
   }
   if (partials) {
     for (int i = 0; i < 5; i++) d[i] = warp_sum(d[i]);
@@ -218,31 +315,10 @@ __global__ void __launch_bounds__(kGatherThreads) mv_gather(MvView V, const cplx
     __syncthreads();
     if (threadIdx.x < 5) {
       double s = 0;
-      for (int w = 0; w < kGatherWarps; w++) s += sdot[w][threadIdx.x];
+      for (int w = 0; w < kWarps; w++) s += sdot[w][threadIdx.x];
       partials[(size_t)leaf * 5 + threadIdx.x] = s;
     }
   }
-}
-
-static MvView mv_view(const DevPartition& DP, const DevHMat& H, bool tr) {
-  MvView v;
-  v.blocks_a = DP.blocks_a.as<int4>();
-  v.blocks_d = DP.blocks_d.as<int4>();
-  v.rank = H.rank.as<int>();
-  v.t_off = H.t_off.as<int>();
-  v.term_off = H.term_off.as<long long>();
-  v.near_off = DP.near_off.as<long long>();
-  v.task_b = H.task_b.as<int>();
-  v.task_off = H.task_off.as<long long>();
-  v.leaf_start = DP.leaf_start.as<int>();
-  v.near_ptr = tr ? DP.tr_near_ptr.as<int>() : DP.fw_near_ptr.as<int>();
-  v.near_items = tr ? DP.tr_near.as<int>() : DP.fw_near.as<int>();
-  v.lr_ptr = tr ? DP.tr_lr_ptr.as<int>() : DP.fw_lr_ptr.as<int>();
-  v.lr_items = tr ? DP.tr_lr.as<int>() : DP.fw_lr.as<int>();
-  v.na = DP.na;
-  v.nleaf = DP.nleaf;
-  v.maxk = H.maxk;
-  return v;
 }
 
 static int g_sms = 0;
@@ -255,25 +331,72 @@ int device_sm_count() {
   return g_sms;
 }
 
+constexpr size_t kRingBytes = (size_t)kStages * kStageBytes;
+
+template <typename MT, typename VT, typename AT>
+static void set_smem_attrs() {
+  static bool done = false;  // once per instantiation (per process; one device at a time)
+  if (done) return;
+  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, VT, AT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kRingBytes));
+  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kRingBytes));
+  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kRingBytes));
+  done = true;
+}
+
+void prepare_matvec_kernels() {
+  set_smem_attrs<float, float, float>();
+  set_smem_attrs<float, double, double>();
+  set_smem_attrs<double, double, double>();
+}
+
 template <typename MT, typename VT, typename AT>
 static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* x, void* y, const void* bminus,
                  const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s) {
-  MvView v = mv_view(DP, H, tr);
+  SegView v;
+  v.leaf_start = DP.leaf_start.as<int>();
+  v.a_seg = DP.near_seg.as<long long>();
+  v.a_kptr = DP.didx_ptr.as<int>();
+  v.a_idx = DP.didx.as<int>();
+  v.blocks_d = DP.blocks_d.as<int4>();
+  v.near_off = DP.near_off.as<long long>();
+  v.trn_ptr = DP.tr_near_ptr.as<int>();
+  v.trn = DP.tr_near.as<int>();
+  v.err = H.err.as<int>();
+  const cplx<MT>* useg = H.useg.as<cplx<MT>>();
+  const cplx<MT>* vseg = H.vseg.as<cplx<MT>>();
+  cplx<AT>* t = (cplx<AT>*)tvec;
+  cplx<AT>* p = H.pbuf.as<cplx<AT>>();
   if (DP.na > 0) {
+    // dot pass over the segments on the input side: V by column leaf (forward), U by row leaf
+    SegView d = v;
+    d.b_seg = tr ? H.seg_f.as<long long>() : H.seg_t.as<long long>();
+    d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
     note_launch();
-    mv_phase1<MT, VT, AT><<<device_sm_count() * 4, 256, 0, s>>>(v, H.pool.as<cplx<MT>>(), (const cplx<VT>*)x,
-                                                        (cplx<AT>*)tvec, tr ? 1 : 0, done);
+    seg_dot_kernel<MT, VT, AT><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, (const cplx<VT>*)x, p,
+                                                                       done);
+    AC3D_CUDA(cudaGetLastError());
+    note_launch();
+    seg_reduce_kernel<AT><<<(int)((H.task_cap + 255) / 256), 256, 0, s>>>(
+        H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na,
+        tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? DP.blk_fw.as<int>() : DP.blk_tr.as<int>(),
+        tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(), p, t, done);
     AC3D_CUDA(cudaGetLastError());
   }
+  v.b_seg = tr ? H.seg_t.as<long long>() : H.seg_f.as<long long>();
+  v.b_kptr = tr ? H.kseg_t.as<int>() : H.kseg_f.as<int>();
+  v.b_idx = tr ? H.vidx.as<int>() : H.uidx.as<int>();
   note_launch();
   if (tr)
-    mv_gather<MT, VT, AT, true><<<DP.nleaf, kGatherThreads, 0, s>>>(
-        v, H.near.as<cplx<MT>>(), H.pool.as<cplx<MT>>(), (const cplx<AT>*)tvec, (const cplx<VT>*)x, (cplx<VT>*)y,
-        (const cplx<VT>*)bminus, (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
+    seg_gather_kernel<MT, VT, AT, true><<<DP.nleaf, kThreads, kRingBytes, s>>>(
+        v, H.near.as<cplx<MT>>(), vseg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
+        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
   else
-    mv_gather<MT, VT, AT, false><<<DP.nleaf, kGatherThreads, 0, s>>>(
-        v, H.near.as<cplx<MT>>(), H.pool.as<cplx<MT>>(), (const cplx<AT>*)tvec, (const cplx<VT>*)x, (cplx<VT>*)y,
-        (const cplx<VT>*)bminus, (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
+    seg_gather_kernel<MT, VT, AT, false><<<DP.nleaf, kThreads, kRingBytes, s>>>(
+        v, H.near.as<cplx<MT>>(), useg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
+        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
   AC3D_CUDA(cudaGetLastError());
 }
 

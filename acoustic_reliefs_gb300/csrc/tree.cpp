@@ -137,15 +137,6 @@ void build_leaf_lists(Partition& P, int maxk) {
     for (int i = P.leaf_start[l]; i < P.leaf_start[l + 1]; i++) leaf_of[i] = l;
   int nd = (int)P.direct.size() / 4, na = (int)P.approx.size() / 4;
 
-  // near storage offsets (block order)
-  P.near_off.resize(nd);
-  int64_t off = 0;
-  for (int b = 0; b < nd; b++) {
-    P.near_off[b] = off;
-    off += (int64_t)(P.direct[4 * b + 1] - P.direct[4 * b]) * (P.direct[4 * b + 3] - P.direct[4 * b + 2]);
-  }
-  P.near_total = off;
-
   auto csr = [&](std::vector<std::vector<int>>& lists, std::vector<int>& ptr, std::vector<int>& items) {
     ptr.assign(nleaf + 1, 0);
     for (int l = 0; l < nleaf; l++) ptr[l + 1] = ptr[l] + (int)lists[l].size();
@@ -176,9 +167,50 @@ void build_leaf_lists(Partition& P, int maxk) {
     P.aca_term_cap += std::max(0, std::min(maxk, std::min(m - 1, n - 1)));
   }
   csr(fn, P.fw_near_ptr, P.fw_near);
+  // near storage in forward leaf order: each leaf's blocks form one R x NC column-major segment
+  P.near_off.assign(nd, 0);
+  P.near_seg.assign(nleaf + 1, 0);
+  P.didx_ptr.assign(nleaf + 1, 0);
+  P.didx.clear();
+  int64_t off = 0;
+  for (int l = 0; l < nleaf; l++) {
+    P.near_seg[l] = off;
+    for (int it = P.fw_near_ptr[l]; it < P.fw_near_ptr[l + 1]; it++) {
+      const int b = P.fw_near[it];
+      const int* q = &P.direct[4 * b];
+      P.near_off[b] = off;
+      off += (int64_t)(q[1] - q[0]) * (q[3] - q[2]);
+      for (int c = q[2]; c < q[3]; c++) P.didx.push_back(c);
+    }
+    // pad to an even column count: segments start and end on 16-byte boundaries (bulk copies)
+    if ((P.didx.size() - P.didx_ptr[l]) & 1) {
+      P.didx.push_back(-1);
+      off += P.leaf_start[l + 1] - P.leaf_start[l];
+    }
+    P.didx_ptr[l + 1] = (int)P.didx.size();
+  }
+  P.near_seg[nleaf] = off;
+  P.near_total = off;
   csr(fl, P.fw_lr_ptr, P.fw_lr);
   csr(tn, P.tr_near_ptr, P.tr_near);
   csr(tl, P.tr_lr_ptr, P.tr_lr);
+
+  P.iter_lim.assign(na, 0);
+  for (int b = 0; b < na; b++) {
+    const int* q = &P.approx[4 * b];
+    P.iter_lim[b] = std::max(0, std::min(maxk, std::min(q[1] - q[0] - 1, q[3] - q[2] - 1)));
+  }
+  // block -> its entries in the leaf lists, in leaf order
+  auto inv = [&](const std::vector<int>& items, std::vector<int>& bptr, std::vector<int>& bl) {
+    bptr.assign(na + 1, 0);
+    for (int b : items) bptr[b + 1]++;
+    for (int b = 0; b < na; b++) bptr[b + 1] += bptr[b];
+    bl.assign(items.size(), 0);
+    std::vector<int> fill(bptr.begin(), bptr.end() - 1);
+    for (size_t e = 0; e < items.size(); e++) bl[fill[items[e]]++] = (int)e;
+  };
+  inv(P.fw_lr, P.blk_fw_ptr, P.blk_fw);
+  inv(P.tr_lr, P.blk_tr_ptr, P.blk_tr);
 
   P.aca_order.resize(na);
   std::iota(P.aca_order.begin(), P.aca_order.end(), 0);
