@@ -319,7 +319,7 @@ void ensure_work(ac3d_ctx* c) {
   const size_t n = (size_t)c->Ne;
   c->kv.ensure(8 * n * sizeof(cd), s);
   const int G = krylov_vec_grid(c->Ne);
-  c->partials.ensure((size_t)std::max(c->DP.nleaf, G) * 5 * sizeof(double) + 64, s);
+  c->partials.ensure((size_t)(c->DP.nleaf + G) * 5 * sizeof(double) + 64, s);
   c->kstate.ensure(sizeof(KState), s);
   c->red.ensure(8 * sizeof(double), s);
   c->b64.ensure(n * sizeof(cd), s);
@@ -340,6 +340,7 @@ KrylovBufs bufs(ac3d_ctx* c, int vec64) {
   for (int i = 0; i < 8; i++) *slots[i] = base + (size_t)i * c->Ne * es;
   B.partials = c->partials.as<double>();
   B.nparts_r = krylov_vec_grid(c->Ne);
+  B.nleaf = c->DP.nleaf;
   B.state = c->kstate.as<KState>();
   return B;
 }
@@ -854,6 +855,7 @@ int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int N
     DP.nleaf = (int)c->P.leaf_start.size() - 1;
     DP.nd = (int)c->P.direct.size() / 4;
     DP.na = (int)c->P.approx.size() / 4;
+    DP.max_leaf = c->P.max_leaf;
     upload(DP.blocks_d, c->P.direct, s);
     upload(DP.blocks_a, c->P.approx, s);
     upload(DP.leaf_start, c->P.leaf_start, s);

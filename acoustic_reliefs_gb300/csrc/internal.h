@@ -110,6 +110,7 @@ void build_leaf_lists(Partition& P, int maxk);
 struct DevPartition {
   int nleaf = 0, nd = 0, na = 0;
   int naca = 0;  // admissible blocks launched for ACA
+  int max_leaf = 0;
   DevBuf near_seg, didx_ptr, didx;
   DevBuf blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
   DevBuf blocks_d, blocks_a;            // int4

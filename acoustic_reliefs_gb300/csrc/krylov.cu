@@ -99,132 +99,164 @@ __device__ __forceinline__ void cdivd(double ar, double ai, double br, double bi
   ci = (yi * xr - yr * xi) / d;
 }
 
-// Start of an iteration: convergence test, rho = (rhat, r), beta.
-__global__ void k_scalar_rho(KState* st, const double* partials, int n) {
-  if (st->done) return;
-  double s[5];
-  reduce_partials(partials, n, s);
-  if (threadIdx.x != 0) return;
-  double rr = s[4];
-  st->rnorm2 = rr;
-  st->restart = 0;
-  if (!(rr > st->tol2)) {
-    st->done = 1;
-    return;
+
+
+
+
+
+
+
+
+
+// ------------------------------------------------------------------------------------------
+// Fused iteration: every CTA of a vector kernel reduces the partials itself (same order, same
+// result in every CTA) instead of a separate single-CTA scalar kernel; CTA 0 commits the state,
+// only into fields that no other CTA of the same kernel reads.
+// ------------------------------------------------------------------------------------------
+struct RhoStep {
+  bool stop;      // converged or out of iterations: nothing more to do
+  bool restart;
+  double rho_re, rho_im, beta_re, beta_im, rr;
+  int done;
+};
+
+__device__ __forceinline__ RhoStep rho_step(const KState* st, const double* s) {
+  RhoStep o{};
+  o.rr = s[4];
+  o.done = 0;
+  if (!(o.rr > st->tol2)) {
+    o.stop = true;
+    o.done = 1;
+    return o;
   }
   if (st->iter >= st->maxit) {
-    st->done = 2;
-    return;
+    o.stop = true;
+    o.done = 2;
+    return o;
   }
-  double rho_re = s[0], rho_im = s[1];
-  double rho_old_re = st->rho_re, rho_old_im = st->rho_im;
-  // breakdown: the shadow residual has become orthogonal to r -> restart with rhat = r
-  if (rho_re * rho_re + rho_im * rho_im <= 1e-24 * st->rhat2 * rr) {
-    st->restart = 1;
-    st->restarts++;
-    st->rhat2 = rr;
-    st->rho_re = rr;
-    st->rho_im = 0.0;
-    st->rho_old_re = 1.0;
-    st->rho_old_im = 0.0;
-    st->alpha_re = st->omega_re = 1.0;
-    st->alpha_im = st->omega_im = 0.0;
-    st->beta_re = st->beta_im = 0.0;
-    return;
+  o.rho_re = s[0];
+  o.rho_im = s[1];
+  if (o.rho_re * o.rho_re + o.rho_im * o.rho_im <= 1e-24 * st->rhat2 * o.rr) {
+    o.restart = true;
+    o.rho_re = o.rr;
+    o.rho_im = 0.0;
+    return o;
   }
-  st->rho_old_re = rho_old_re;
-  st->rho_old_im = rho_old_im;
-  st->rho_re = rho_re;
-  st->rho_im = rho_im;
-  // beta = (rho / rho_old) (alpha / omega)
   double q1r, q1i, q2r, q2i;
-  cdivd(rho_re, rho_im, rho_old_re, rho_old_im, q1r, q1i);
+  cdivd(o.rho_re, o.rho_im, st->rho_re, st->rho_im, q1r, q1i);
   cdivd(st->alpha_re, st->alpha_im, st->omega_re, st->omega_im, q2r, q2i);
-  st->beta_re = q1r * q2r - q1i * q2i;
-  st->beta_im = q1r * q2i + q1i * q2r;
+  o.beta_re = q1r * q2r - q1i * q2i;
+  o.beta_im = q1r * q2i + q1i * q2r;
+  return o;
 }
 
+// start of an iteration: convergence test, rho, beta; p = r + beta (p - omega v)
 template <typename VT>
-__global__ void __launch_bounds__(kVecThreads) k_p(const KState* st, int n, const cplx<VT>* __restrict__ r,
-                                                   cplx<VT>* p, cplx<VT>* v, cplx<VT>* rhat) {
+__global__ void __launch_bounds__(kVecThreads) kf_p(KState* st, const double* partials, int nparts, int n,
+                                                    const cplx<VT>* __restrict__ r, cplx<VT>* p, cplx<VT>* v,
+                                                    cplx<VT>* rhat) {
   if (st->done) return;
-  const bool restart = st->restart != 0;
-  const VT br = (VT)st->beta_re, bi = (VT)st->beta_im, wr = (VT)st->omega_re, wi = (VT)st->omega_im;
+  double s[5];
+  reduce_partials(partials, nparts, s);
+  const RhoStep o = rho_step(st, s);
+  if (o.stop) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->rnorm2 = o.rr;
+      st->done = o.done;
+    }
+    return;
+  }
+  const VT br = (VT)o.beta_re, bi = (VT)o.beta_im;
+  const VT wr = (VT)(o.restart ? 1.0 : st->omega_re), wi = (VT)(o.restart ? 0.0 : st->omega_im);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    cplx<VT> ri = r[i];
-    if (restart) {
+    const cplx<VT> ri = r[i];
+    if (o.restart) {
       rhat[i] = ri;
       p[i] = ri;
       v[i] = cplx<VT>();
     } else {
-      cplx<VT> pi = p[i], vi = v[i];
-      // p = r + beta (p - omega v)
-      VT tr = pi.re - (wr * vi.re - wi * vi.im);
-      VT ti = pi.im - (wr * vi.im + wi * vi.re);
+      const cplx<VT> pi = p[i], vi = v[i];
+      const VT tr = pi.re - (wr * vi.re - wi * vi.im);
+      const VT ti = pi.im - (wr * vi.im + wi * vi.re);
       p[i] = cplx<VT>(ri.re + br * tr - bi * ti, ri.im + br * ti + bi * tr);
     }
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->rnorm2 = o.rr;
+    st->rho_new_re = o.rho_re;
+    st->rho_new_im = o.rho_im;
+    st->restart = o.restart ? 1 : 0;  // rhat2 is committed by kf_xr (other CTAs here read it)
+    if (o.restart) st->restarts++;
+  }
 }
 
-// alpha = rho / (rhat, v); partials from the matvec epilogue (slots 0, 1).
-__global__ void k_scalar_alpha(KState* st, const double* partials, int n) {
+// alpha = rho / (rhat, v); s = r - alpha v
+template <typename VT>
+__global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* partials, int nparts, int n,
+                                                    const cplx<VT>* __restrict__ r, const cplx<VT>* __restrict__ v,
+                                                    cplx<VT>* s) {
   if (st->done) return;
-  double s[5];
-  reduce_partials(partials, n, s);
-  if (threadIdx.x != 0) return;
-  if (s[0] == 0.0 && s[1] == 0.0) {
-    st->done = 3;
+  double d[5];
+  reduce_partials(partials, nparts, d);
+  double ar, ai;
+  if (d[0] == 0.0 && d[1] == 0.0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 3;
     return;
   }
-  cdivd(st->rho_re, st->rho_im, s[0], s[1], st->alpha_re, st->alpha_im);
-}
-
-template <typename VT>
-__global__ void __launch_bounds__(kVecThreads) k_s(const KState* st, int n, const cplx<VT>* __restrict__ r,
-                                                   const cplx<VT>* __restrict__ v, cplx<VT>* s) {
-  if (st->done) return;
-  const VT ar = (VT)st->alpha_re, ai = (VT)st->alpha_im;
+  cdivd(st->rho_new_re, st->rho_new_im, d[0], d[1], ar, ai);
+  const VT a_r = (VT)ar, a_i = (VT)ai;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    cplx<VT> ri = r[i], vi = v[i];
-    s[i] = cplx<VT>(ri.re - (ar * vi.re - ai * vi.im), ri.im - (ar * vi.im + ai * vi.re));
+    const cplx<VT> ri = r[i], vi = v[i];
+    s[i] = cplx<VT>(ri.re - (a_r * vi.re - a_i * vi.im), ri.im - (a_r * vi.im + a_i * vi.re));
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->alpha_new_re = ar;
+    st->alpha_new_im = ai;
   }
 }
 
-// omega = (t, s) / (t, t); partials from the matvec epilogue (slots 2, 3 and 4).
-__global__ void k_scalar_omega(KState* st, const double* partials, int n) {
-  if (st->done) return;
-  double s[5];
-  reduce_partials(partials, n, s);
-  if (threadIdx.x != 0) return;
-  if (s[4] > 0.0) {
-    st->omega_re = s[2] / s[4];
-    st->omega_im = s[3] / s[4];
-  } else {
-    st->omega_re = st->omega_im = 0.0;
-  }
-  st->iter++;
-}
-
+// omega = (t, s) / (t, t); x += alpha p + omega s; r = s - omega t; partials (rhat, r), |r|^2
 template <typename VT>
-__global__ void __launch_bounds__(kVecThreads) k_xr(const KState* st, int n, cplx<VT>* x, const cplx<VT>* __restrict__ p,
-                                                    const cplx<VT>* __restrict__ s, cplx<VT>* r,
-                                                    const cplx<VT>* __restrict__ t, const cplx<VT>* __restrict__ rhat,
-                                                    double* partials) {
+__global__ void __launch_bounds__(kVecThreads) kf_xr(KState* st, const double* partials, int nparts, int n, cplx<VT>* x,
+                                                     const cplx<VT>* __restrict__ p, const cplx<VT>* __restrict__ s,
+                                                     cplx<VT>* r, const cplx<VT>* __restrict__ t,
+                                                     const cplx<VT>* __restrict__ rhat, double* out_partials) {
   if (st->done) return;
-  const VT ar = (VT)st->alpha_re, ai = (VT)st->alpha_im, wr = (VT)st->omega_re, wi = (VT)st->omega_im;
+  double d5[5];
+  reduce_partials(partials, nparts, d5);
+  double wr_d = 0, wi_d = 0;
+  if (d5[4] > 0.0) {
+    wr_d = d5[2] / d5[4];
+    wi_d = d5[3] / d5[4];
+  }
+  const double ar_d = st->alpha_new_re, ai_d = st->alpha_new_im;
+  const VT ar = (VT)ar_d, ai = (VT)ai_d, wr = (VT)wr_d, wi = (VT)wi_d;
   double d[5] = {0, 0, 0, 0, 0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    cplx<VT> pi = p[i], si = s[i], ti = t[i], xi = x[i], hi = rhat[i];
+    const cplx<VT> pi = p[i], si = s[i], ti = t[i], hi = rhat[i];
+    cplx<VT> xi = x[i];
     xi.re += (ar * pi.re - ai * pi.im) + (wr * si.re - wi * si.im);
     xi.im += (ar * pi.im + ai * pi.re) + (wr * si.im + wi * si.re);
     x[i] = xi;
-    cplx<VT> ri(si.re - (wr * ti.re - wi * ti.im), si.im - (wr * ti.im + wi * ti.re));
+    const cplx<VT> ri(si.re - (wr * ti.re - wi * ti.im), si.im - (wr * ti.im + wi * ti.re));
     r[i] = ri;
     d[0] += (double)hi.re * ri.re + (double)hi.im * ri.im;
     d[1] += (double)hi.re * ri.im - (double)hi.im * ri.re;
     d[4] += (double)ri.re * ri.re + (double)ri.im * ri.im;
   }
-  write_partials(d, partials);
+  write_partials(d, out_partials);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->rho_old_re = st->rho_re;
+    st->rho_old_im = st->rho_im;
+    st->rho_re = st->rho_new_re;
+    st->rho_im = st->rho_new_im;
+    st->alpha_re = ar_d;
+    st->alpha_im = ai_d;
+    st->omega_re = wr_d;
+    st->omega_im = wi_d;
+    if (st->restart) st->rhat2 = st->rnorm2;
+    st->iter++;
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -277,41 +309,41 @@ static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const
   const int n = B.n, G = vec_grid(n);
   const int vec64 = sizeof(VT) == 8;
   KState* st = B.state;
+  // partials: xr / init write slots [0, G) of rpart; the matvec gathers write the per-leaf slots
+  double* rpart = B.partials + (size_t)DP.nleaf * 5;
   note_launch();
-  k_scalar_rho<<<1, kVecThreads, 0, s>>>(st, B.partials, B.nparts_r);
-  note_launch();
-  k_p<VT><<<G, kVecThreads, 0, s>>>(st, n, (const cplx<VT>*)B.r, (cplx<VT>*)B.p, (cplx<VT>*)B.v, (cplx<VT>*)B.rhat);
+  kf_p<VT><<<G, kVecThreads, 0, s>>>(st, rpart, G, n, (const cplx<VT>*)B.r, (cplx<VT>*)B.p, (cplx<VT>*)B.v,
+                                     (cplx<VT>*)B.rhat);
   MatvecEpilogue e1;
   e1.dot_a = B.rhat;
   e1.partials = B.partials;
   launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s);
   note_launch();
-  k_scalar_alpha<<<1, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf);
-  note_launch();
-  k_s<VT><<<G, kVecThreads, 0, s>>>(st, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v, (cplx<VT>*)B.s);
+  kf_s<VT><<<G, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v,
+                                     (cplx<VT>*)B.s);
   MatvecEpilogue e2;
   e2.dot_b = B.s;
   e2.partials = B.partials;
   launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s);
   note_launch();
-  k_scalar_omega<<<1, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf);
-  note_launch();
-  k_xr<VT><<<G, kVecThreads, 0, s>>>(st, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p, (const cplx<VT>*)B.s,
-                                     (cplx<VT>*)B.r, (const cplx<VT>*)B.t, (const cplx<VT>*)B.rhat, B.partials);
+  kf_xr<VT><<<G, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p,
+                                      (const cplx<VT>*)B.s, (cplx<VT>*)B.r, (const cplx<VT>*)B.t,
+                                      (const cplx<VT>*)B.rhat, rpart);
   AC3D_CUDA(cudaGetLastError());
 }
 
 void krylov_enqueue_init(const KrylovBufs& B, int vec64, double tol, int maxit, cudaStream_t s) {
   const int n = B.n, G = vec_grid(n);
+  double* rpart = B.partials + (size_t)B.nleaf * 5;
   note_launch();
   if (vec64)
     k_init<double><<<G, kVecThreads, 0, s>>>(n, (const cd*)B.b, (cd*)B.x, (cd*)B.r, (cd*)B.rhat, (cd*)B.p,
-                                             (cd*)B.v, B.partials);
+                                             (cd*)B.v, rpart);
   else
     k_init<float><<<G, kVecThreads, 0, s>>>(n, (const cf*)B.b, (cf*)B.x, (cf*)B.r, (cf*)B.rhat, (cf*)B.p,
-                                            (cf*)B.v, B.partials);
+                                            (cf*)B.v, rpart);
   note_launch();
-  k_scalar_init<<<1, kVecThreads, 0, s>>>(B.state, B.partials, G, tol, maxit);
+  k_scalar_init<<<1, kVecThreads, 0, s>>>(B.state, rpart, G, tol, maxit);
   AC3D_CUDA(cudaGetLastError());
 }
 

@@ -8,6 +8,8 @@ namespace ac3d {
 // Solver scalars, kept on the device for the whole solve.
 struct KState {
   double rho_re, rho_im, rho_old_re, rho_old_im;
+  double rho_new_re, rho_new_im;   // rho of the running iteration (committed at its end)
+  double alpha_new_re, alpha_new_im;
   double alpha_re, alpha_im, omega_re, omega_im;
   double beta_re, beta_im;
   double bnorm2, rnorm2, tol2, rhat2;
@@ -23,8 +25,9 @@ struct KrylovBufs {
   int n = 0;
   void *b = nullptr, *x = nullptr, *r = nullptr, *rhat = nullptr, *p = nullptr, *v = nullptr, *s = nullptr,
        *t = nullptr;
-  double* partials = nullptr;  // >= max(nleaf, vector grid) x 5
+  double* partials = nullptr;  // (nleaf + vector grid) x 5: per-leaf matvec partials, then vector partials
   int nparts_r = 0;            // number of partials feeding the rho step (vector grid)
+  int nleaf = 0;
   KState* state = nullptr;
 };
 

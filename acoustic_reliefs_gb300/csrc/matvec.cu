@@ -22,7 +22,6 @@ namespace ac3d {
 namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kMaxRpl = 8;  // rows per lane (leaf size <= 256)
 }  // namespace
 
 template <typename AT, typename A, typename X>
@@ -130,7 +129,7 @@ __device__ __forceinline__ void init_ring(uint64_t* full) {
 
 // Dot pass: p[kptr[leaf] + k] = sum_rows S[k][row] x[leaf rows] for every column k of the leaf's
 // low-rank segment (region B).
-template <typename MT, typename VT, typename AT>
+template <typename MT, typename VT, typename AT, int RPL>
 __global__ void __launch_bounds__(kThreads) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
                                                            const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ p,
                                                            const int* __restrict__ done) {
@@ -143,12 +142,11 @@ __global__ void __launch_bounds__(kThreads) seg_dot_kernel(SegView V, const cplx
   const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
   if (K == 0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int rpl = (R + 31) >> 5;
-  AT xr[kMaxRpl], xi[kMaxRpl];
+  AT xr[RPL], xi[RPL];
 #pragma unroll
-  for (int j = 0; j < kMaxRpl; j++) {
+  for (int j = 0; j < RPL; j++) {
     const int row = lane + 32 * j;
-    cplx<VT> v = (j < rpl && row < R) ? x[ls + row] : cplx<VT>();
+    cplx<VT> v = row < R ? x[ls + row] : cplx<VT>();
     xr[j] = (AT)v.re;
     xi[j] = (AT)v.im;
   }
@@ -159,9 +157,9 @@ __global__ void __launch_bounds__(kThreads) seg_dot_kernel(SegView V, const cplx
                     for (int j = warp; j < ncols; j += kWarps) {
                       AT ar = 0, ai = 0;
 #pragma unroll
-                      for (int jr = 0; jr < kMaxRpl; jr++) {
+                      for (int jr = 0; jr < RPL; jr++) {
                         const int row = lane + 32 * jr;
-                        if (jr < rpl && row < R) {
+                        if (row < R) {
                           const cplx<MT> s = S[j * R + row];
                           ar = fma((AT)s.re, xr[jr], ar);
                           ar = fma(-(AT)s.im, xi[jr], ar);
@@ -199,7 +197,7 @@ __global__ void seg_reduce_kernel(const int* __restrict__ task_b, const int* __r
 
 // Gather pass: y[leaf rows] = -x/2 + S_A x[a_idx] + S_B t[b_idx] (+ transposed dense blocks), or
 // b - that; optional fused FP64 dot partials (conj(a).y, conj(y).b, |y|^2) per leaf.
-template <typename MT, typename VT, typename AT, bool TRANS>
+template <typename MT, typename VT, typename AT, bool TRANS, int RPL>
 __global__ void __launch_bounds__(kThreads) seg_gather_kernel(
     SegView V, const cplx<MT>* __restrict__ near, const cplx<MT>* __restrict__ lrseg, const cplx<AT>* __restrict__ t,
     const cplx<VT>* __restrict__ x, cplx<VT>* __restrict__ y, const cplx<VT>* __restrict__ bminus,
@@ -213,10 +211,9 @@ __global__ void __launch_bounds__(kThreads) seg_gather_kernel(
   const int leaf = blockIdx.x;
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int rpl = (R + 31) >> 5;
-  AT ar[kMaxRpl], ai[kMaxRpl];
+  AT ar[RPL], ai[RPL];
 #pragma unroll
-  for (int j = 0; j < kMaxRpl; j++) ar[j] = ai[j] = 0;
+  for (int j = 0; j < RPL; j++) ar[j] = ai[j] = 0;
 
   const int a_cols = TRANS ? 0 : V.a_kptr[leaf + 1] - V.a_kptr[leaf];
   const int* a_idx = TRANS ? nullptr : V.a_idx + V.a_kptr[leaf];
@@ -225,29 +222,39 @@ __global__ void __launch_bounds__(kThreads) seg_gather_kernel(
   init_ring(full);
   stream_leaf<MT>(stage, full, R, TRANS ? nullptr : near + V.a_seg[leaf], a_cols, lrseg + V.b_seg[leaf], b_cols,
                   V.err, [&](const cplx<MT>* S, int region, int c0, int ncols) {
-                    const int* idx = region == 0 ? a_idx : b_idx;
-                    for (int j = warp; j < ncols; j += kWarps) {
-                      const int zi = idx[c0 + j];
-                      if (zi < 0) continue;  // padding column
-                      AT zr, zim;
-                      if (region == 0) {
-                        const cplx<VT> z = x[zi];
-                        zr = (AT)z.re;
-                        zim = (AT)z.im;
-                      } else {
-                        const cplx<AT> z = t[zi];
-                        zr = z.re;
-                        zim = z.im;
+                    const int* idx = (region == 0 ? a_idx : b_idx) + c0;
+                    // warp columns j = warp + 8 l; lane l fetches the multiplier of its column
+                    for (int jb = warp; jb < ncols; jb += 32 * kWarps) {
+                      const int jl = jb + kWarps * lane;
+                      AT zr = 0, zim = 0;
+                      if (jl < ncols) {
+                        const int zi = idx[jl];
+                        if (zi >= 0) {  // -1: padding column
+                          if (region == 0) {
+                            const cplx<VT> z = x[zi];
+                            zr = (AT)z.re;
+                            zim = (AT)z.im;
+                          } else {
+                            const cplx<AT> z = t[zi];
+                            zr = z.re;
+                            zim = z.im;
+                          }
+                        }
                       }
+                      const int nl = min(32, (ncols - jb + kWarps - 1) / kWarps);
+                      for (int l = 0; l < nl; l++) {
+                        const AT br = __shfl_sync(0xffffffffu, zr, l), bi = __shfl_sync(0xffffffffu, zim, l);
+                        const int j = jb + kWarps * l;
 #pragma unroll
-                      for (int jr = 0; jr < kMaxRpl; jr++) {
-                        const int row = lane + 32 * jr;
-                        if (jr < rpl && row < R) {
-                          const cplx<MT> s = S[j * R + row];
-                          ar[jr] = fma((AT)s.re, zr, ar[jr]);
-                          ar[jr] = fma(-(AT)s.im, zim, ar[jr]);
-                          ai[jr] = fma((AT)s.re, zim, ai[jr]);
-                          ai[jr] = fma((AT)s.im, zr, ai[jr]);
+                        for (int jr = 0; jr < RPL; jr++) {
+                          const int row = lane + 32 * jr;
+                          if (row < R) {
+                            const cplx<MT> sv = S[j * R + row];
+                            ar[jr] = fma((AT)sv.re, br, ar[jr]);
+                            ar[jr] = fma(-(AT)sv.im, bi, ar[jr]);
+                            ai[jr] = fma((AT)sv.re, bi, ai[jr]);
+                            ai[jr] = fma((AT)sv.im, br, ai[jr]);
+                          }
                         }
                       }
                     }
@@ -260,9 +267,9 @@ __global__ void __launch_bounds__(kThreads) seg_gather_kernel(
       const int m = blk.y - blk.x;
       const cplx<VT>* xs = x + blk.x;
 #pragma unroll
-      for (int jr = 0; jr < kMaxRpl; jr++) {
+      for (int jr = 0; jr < RPL; jr++) {
         const int col = lane + 32 * jr;
-        if (jr < rpl && col < R) {
+        if (col < R) {
           const cplx<MT>* Dc = near + V.near_off[b] + (long long)col * m;
           for (int r = 0; r < m; r++) cmac<AT>(ar[jr], ai[jr], Dc[r], xs[r]);
         }
@@ -273,9 +280,9 @@ __global__ void __launch_bounds__(kThreads) seg_gather_kernel(
   cplx<AT>* part = (cplx<AT>*)stage;
   __syncthreads();
 #pragma unroll
-  for (int jr = 0; jr < kMaxRpl; jr++) {
+  for (int jr = 0; jr < RPL; jr++) {
     const int row = lane + 32 * jr;
-    if (jr < rpl && row < R) part[warp * R + row] = cplx<AT>(ar[jr], ai[jr]);
+    if (row < R) part[warp * R + row] = cplx<AT>(ar[jr], ai[jr]);
   }
   __syncthreads();
   double d[5] = {0, 0, 0, 0, 0};
@@ -333,26 +340,34 @@ int device_sm_count() {
 
 constexpr size_t kRingBytes = (size_t)kStages * kStageBytes;
 
+template <typename MT, typename VT, typename AT, int RPL>
+static void set_smem_attrs_rpl() {
+  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, VT, AT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kRingBytes));
+  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, false, RPL>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
+  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, true, RPL>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
+}
+
 template <typename MT, typename VT, typename AT>
 static void set_smem_attrs() {
-  static bool done = false;  // once per instantiation (per process; one device at a time)
-  if (done) return;
-  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, VT, AT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kRingBytes));
-  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kRingBytes));
-  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kRingBytes));
-  done = true;
+  set_smem_attrs_rpl<MT, VT, AT, 1>();
+  set_smem_attrs_rpl<MT, VT, AT, 2>();
+  set_smem_attrs_rpl<MT, VT, AT, 4>();
+  set_smem_attrs_rpl<MT, VT, AT, 8>();
 }
 
 void prepare_matvec_kernels() {
+  static bool done = false;  // once per process (one device per process)
+  if (done) return;
   set_smem_attrs<float, float, float>();
   set_smem_attrs<float, double, double>();
   set_smem_attrs<double, double, double>();
+  done = true;
 }
 
-template <typename MT, typename VT, typename AT>
+template <typename MT, typename VT, typename AT, int RPL>
 static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* x, void* y, const void* bminus,
                  const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s) {
   SegView v;
@@ -375,8 +390,8 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
     d.b_seg = tr ? H.seg_f.as<long long>() : H.seg_t.as<long long>();
     d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
     note_launch();
-    seg_dot_kernel<MT, VT, AT><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, (const cplx<VT>*)x, p,
-                                                                       done);
+    seg_dot_kernel<MT, VT, AT, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, (const cplx<VT>*)x,
+                                                                            p, done);
     AC3D_CUDA(cudaGetLastError());
     note_launch();
     seg_reduce_kernel<AT><<<(int)((H.task_cap + 255) / 256), 256, 0, s>>>(
@@ -390,25 +405,39 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
   v.b_idx = tr ? H.vidx.as<int>() : H.uidx.as<int>();
   note_launch();
   if (tr)
-    seg_gather_kernel<MT, VT, AT, true><<<DP.nleaf, kThreads, kRingBytes, s>>>(
+    seg_gather_kernel<MT, VT, AT, true, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
         v, H.near.as<cplx<MT>>(), vseg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
         (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
   else
-    seg_gather_kernel<MT, VT, AT, false><<<DP.nleaf, kThreads, kRingBytes, s>>>(
+    seg_gather_kernel<MT, VT, AT, false, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
         v, H.near.as<cplx<MT>>(), useg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
         (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
   AC3D_CUDA(cudaGetLastError());
+}
+
+template <typename MT, typename VT, typename AT>
+static void mv_rpl(const DevPartition& DP, const DevHMat& H, bool tr, const void* x, void* y, const void* bminus,
+                   const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s) {
+  const int rpl = (DP.max_leaf + 31) / 32;
+  if (rpl <= 1)
+    mv_t<MT, VT, AT, 1>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
+  else if (rpl <= 2)
+    mv_t<MT, VT, AT, 2>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
+  else if (rpl <= 4)
+    mv_t<MT, VT, AT, 4>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
+  else
+    mv_t<MT, VT, AT, 8>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
 }
 
 void launch_matvec_ex(const DevPartition& DP, const DevHMat& H, bool transposed, int vec64, const void* x, void* y,
                       const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s) {
   if (H.prec == PREC_FP64) {
     if (!vec64) throw Error(3, "internal: FP64 H-matrix needs FP64 vectors");
-    mv_t<double, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
+    mv_rpl<double, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
   } else if (vec64) {
-    mv_t<float, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
+    mv_rpl<float, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
   } else {
-    mv_t<float, float, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s);
+    mv_rpl<float, float, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s);
   }
 }
 
