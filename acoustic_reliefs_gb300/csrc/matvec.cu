@@ -51,7 +51,9 @@ struct SegView {
 };
 
 // Iterates the chunks of the (up to two) regions of one leaf through the copy ring and calls
-// fn(stage_ptr, region, first_column, columns) for each chunk, all threads together.
+// fn(stage_ptr, region, first_column, columns, next_region, next_first_column, next_columns) for
+// each chunk, all threads together (next_columns = 0 after the last chunk), so that the callback
+// can prefetch what the next chunk needs while it computes this one.
 template <typename MT, typename F>
 __device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes], uint64_t* full, int R,
                                             const cplx<MT>* a_ptr, int a_cols, const cplx<MT>* b_ptr, int b_cols,
@@ -95,7 +97,12 @@ __device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes],
     const cplx<MT>* src;
     int region, c0, ncols;
     chunk(c, src, region, c0, ncols);
-    fn((const cplx<MT>*)stage[s], region, c0, ncols);
+    int nregion = 0, nc0 = 0, nncols = 0;
+    if (c + 1 < nch) {
+      const cplx<MT>* nsrc;
+      chunk(c + 1, nsrc, nregion, nc0, nncols);
+    }
+    fn((const cplx<MT>*)stage[s], region, c0, ncols, nregion, nc0, nncols);
     __syncthreads();  // every warp is done with stage s
     if (threadIdx.x == 0 && c + kStages < nch) {
       fence_proxy_async();
@@ -130,7 +137,7 @@ __device__ __forceinline__ void init_ring(uint64_t* full) {
 // Dot pass: p[kptr[leaf] + k] = sum_rows S[k][row] x[leaf rows] for every column k of the leaf's
 // low-rank segment (region B).
 template <typename MT, typename VT, typename AT, int RPL>
-__global__ void __launch_bounds__(kThreads) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
+__global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
                                                            const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ p,
                                                            const int* __restrict__ done) {
   extern __shared__ __align__(128) unsigned char dsmem[];
@@ -153,23 +160,45 @@ __global__ void __launch_bounds__(kThreads) seg_dot_kernel(SegView V, const cplx
   init_ring(full);
   cplx<AT>* out = p + k0;
   stream_leaf<MT>(stage, full, R, nullptr, 0, lrseg + V.b_seg[leaf], K, V.err,
-                  [&](const cplx<MT>* S, int, int c0, int ncols) {
-                    for (int j = warp; j < ncols; j += kWarps) {
-                      AT ar = 0, ai = 0;
+                  [&](const cplx<MT>* S, int, int c0, int ncols, int, int, int) {
+                    // four columns per warp at a time: four independent shuffle reductions
+                    for (int j0 = warp; j0 < ncols; j0 += 4 * kWarps) {
+                      AT a[8];
 #pragma unroll
-                      for (int jr = 0; jr < RPL; jr++) {
-                        const int row = lane + 32 * jr;
-                        if (row < R) {
-                          const cplx<MT> s = S[j * R + row];
-                          ar = fma((AT)s.re, xr[jr], ar);
-                          ar = fma(-(AT)s.im, xi[jr], ar);
-                          ai = fma((AT)s.re, xi[jr], ai);
-                          ai = fma((AT)s.im, xr[jr], ai);
+                      for (int u = 0; u < 4; u++) {
+                        const int j = j0 + u * kWarps;
+                        AT ar = 0, ai = 0;
+                        if (j < ncols) {
+#pragma unroll
+                          for (int jr = 0; jr < RPL; jr++) {
+                            const int row = lane + 32 * jr;
+                            if (row < R) {
+                              const cplx<MT> sv = S[j * R + row];
+                              ar = fma((AT)sv.re, xr[jr], ar);
+                              ar = fma(-(AT)sv.im, xi[jr], ar);
+                              ai = fma((AT)sv.re, xi[jr], ai);
+                              ai = fma((AT)sv.im, xr[jr], ai);
+                            }
+                          }
                         }
+                        a[2 * u] = ar;
+                        a[2 * u + 1] = ai;
                       }
-                      ar = warp_sum(ar);
-                      ai = warp_sum(ai);
-                      if (lane == 0) out[c0 + j] = cplx<AT>(ar, ai);
+#pragma unroll
+                      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                        for (int u = 0; u < 8; u++) a[u] += __shfl_xor_sync(0xffffffffu, a[u], o);
+                      if (lane < 4) {
+                        const int j = j0 + lane * kWarps;
+                        AT vr = a[0], vi = a[1];
+#pragma unroll
+                        for (int u = 1; u < 4; u++)
+                          if (lane == u) {
+                            vr = a[2 * u];
+                            vi = a[2 * u + 1];
+                          }
+                        if (j < ncols) out[c0 + j] = cplx<AT>(vr, vi);
+                      }
                     }
                   });
 }
@@ -198,7 +227,7 @@ __global__ void seg_reduce_kernel(const int* __restrict__ task_b, const int* __r
 // Gather pass: y[leaf rows] = -x/2 + S_A x[a_idx] + S_B t[b_idx] (+ transposed dense blocks), or
 // b - that; optional fused FP64 dot partials (conj(a).y, conj(y).b, |y|^2) per leaf.
 template <typename MT, typename VT, typename AT, bool TRANS, int RPL>
-__global__ void __launch_bounds__(kThreads) seg_gather_kernel(
+__global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
     SegView V, const cplx<MT>* __restrict__ near, const cplx<MT>* __restrict__ lrseg, const cplx<AT>* __restrict__ t,
     const cplx<VT>* __restrict__ x, cplx<VT>* __restrict__ y, const cplx<VT>* __restrict__ bminus,
     const cplx<VT>* __restrict__ dot_a, const cplx<VT>* __restrict__ dot_b, double* partials,
@@ -219,27 +248,42 @@ __global__ void __launch_bounds__(kThreads) seg_gather_kernel(
   const int* a_idx = TRANS ? nullptr : V.a_idx + V.a_kptr[leaf];
   const int b_cols = V.b_kptr[leaf + 1] - V.b_kptr[leaf];
   const int* b_idx = V.b_idx + V.b_kptr[leaf];
+  // multiplier of column jb + 8 lane of a chunk: x[idx] (near region) or t[idx] (low-rank region)
+  auto fetch = [&](int region, int c0, int ncols, int jb, AT& zr, AT& zim) {
+    zr = 0;
+    zim = 0;
+    const int jl = jb + kWarps * lane;
+    if (jl < ncols) {
+      const int zi = (region == 0 ? a_idx : b_idx)[c0 + jl];
+      if (zi >= 0) {  // -1: padding column
+        if (region == 0) {
+          const cplx<VT> z = x[zi];
+          zr = (AT)z.re;
+          zim = (AT)z.im;
+        } else {
+          const cplx<AT> z = t[zi];
+          zr = z.re;
+          zim = z.im;
+        }
+      }
+    }
+  };
   init_ring(full);
+  AT nzr = 0, nzi = 0;  // prefetched multipliers of the first batch of the next chunk
+  bool have_next = false;
   stream_leaf<MT>(stage, full, R, TRANS ? nullptr : near + V.a_seg[leaf], a_cols, lrseg + V.b_seg[leaf], b_cols,
-                  V.err, [&](const cplx<MT>* S, int region, int c0, int ncols) {
-                    const int* idx = (region == 0 ? a_idx : b_idx) + c0;
-                    // warp columns j = warp + 8 l; lane l fetches the multiplier of its column
+                  V.err, [&](const cplx<MT>* S, int region, int c0, int ncols, int nreg, int nc0, int nnc) {
                     for (int jb = warp; jb < ncols; jb += 32 * kWarps) {
-                      const int jl = jb + kWarps * lane;
-                      AT zr = 0, zim = 0;
-                      if (jl < ncols) {
-                        const int zi = idx[jl];
-                        if (zi >= 0) {  // -1: padding column
-                          if (region == 0) {
-                            const cplx<VT> z = x[zi];
-                            zr = (AT)z.re;
-                            zim = (AT)z.im;
-                          } else {
-                            const cplx<AT> z = t[zi];
-                            zr = z.re;
-                            zim = z.im;
-                          }
-                        }
+                      AT zr, zim;
+                      if (jb == warp && have_next) {
+                        zr = nzr;
+                        zim = nzi;
+                      } else {
+                        fetch(region, c0, ncols, jb, zr, zim);
+                      }
+                      if (jb + 32 * kWarps >= ncols) {  // last batch: prefetch the next chunk's first
+                        have_next = nnc > 0;
+                        if (have_next) fetch(nreg, nc0, nnc, warp, nzr, nzi);
                       }
                       const int nl = min(32, (ncols - jb + kWarps - 1) / kWarps);
                       for (int l = 0; l < nl; l++) {
@@ -257,6 +301,10 @@ __global__ void __launch_bounds__(kThreads) seg_gather_kernel(
                           }
                         }
                       }
+                    }
+                    if (warp >= ncols) {  // a warp with no column here still prefetches for the next
+                      have_next = nnc > 0;
+                      if (have_next) fetch(nreg, nc0, nnc, warp, nzr, nzi);
                     }
                   });
   if (TRANS) {

@@ -8,7 +8,7 @@
 
 namespace ac3d {
 
-constexpr int kStages = 4;
+constexpr int kStages = 3;
 constexpr int kStageBytes = 16384;        // 16 KB per stage (multiple of 16)
 constexpr uint32_t kSpinLimit = 1u << 26; // polls before a wait is declared failed
 
