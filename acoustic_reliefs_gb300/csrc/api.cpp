@@ -278,6 +278,33 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     H->kpos_f.alloc((size_t)std::max<size_t>(c->P.fw_lr.size(), 1) * sizeof(int), s);
     H->kpos_t.alloc((size_t)std::max<size_t>(c->P.tr_lr.size(), 1) * sizeof(int), s);
     H->pbuf.alloc((size_t)std::max<int64_t>(std::max(kf, kt), 1) * sizeof(cd), s);
+    // leaves by decreasing streamed bytes: row leaves (near + U columns) for the forward gather and
+    // the transposed dot, column leaves (V columns; + transposed near) for the forward dot and the
+    // transposed gather. The hardware dispatches CTAs in index order, so this is
+    // longest-first list scheduling.
+    {
+      std::vector<int64_t> wr(nleaf), wc(nleaf);
+      std::vector<int> ord(nleaf);
+      for (int l = 0; l < nleaf; l++) {
+        const int Rl = c->P.leaf_start[l + 1] - c->P.leaf_start[l];
+        int64_t kr = c->P.didx_ptr[l + 1] - c->P.didx_ptr[l], kc = 0;
+        for (int it = c->P.fw_lr_ptr[l]; it < c->P.fw_lr_ptr[l + 1]; it++) kr += H->ranks_host[c->P.fw_lr[it]];
+        for (int it = c->P.tr_lr_ptr[l]; it < c->P.tr_lr_ptr[l + 1]; it++) kc += H->ranks_host[c->P.tr_lr[it]];
+        for (int it = c->P.tr_near_ptr[l]; it < c->P.tr_near_ptr[l + 1]; it++) {
+          const int* q = &c->P.direct[4 * c->P.tr_near[it]];
+          kc += q[1] - q[0];
+        }
+        wr[l] = kr * Rl;
+        wc[l] = kc * Rl;
+      }
+      auto sorted = [&](const std::vector<int64_t>& w) {
+        for (int l = 0; l < nleaf; l++) ord[l] = l;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return w[a] > w[b]; });
+        return ord;
+      };
+      upload(H->order_rows, sorted(wr), s);
+      upload(H->order_cols, sorted(wc), s);
+    }
     launch_pack(c->DP, *H, false, s);
     launch_pack(c->DP, *H, true, s);
     H->pool.release();
@@ -301,6 +328,10 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     H->vseg.alloc(32, s);
     H->uidx.alloc(16, s);
     H->vidx.alloc(16, s);
+    std::vector<int> ord(c->DP.nleaf);
+    for (int l = 0; l < c->DP.nleaf; l++) ord[l] = l;
+    upload(H->order_rows, ord, s);
+    upload(H->order_cols, ord, s);
   }
   c->stats.near_entries = c->P.near_total;
   c->stats.hmat_bytes = (long long)H->bytes();
@@ -869,8 +900,17 @@ int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int N
     upload(DP.tr_lr, c->P.tr_lr, s);
     std::vector<long long> no(c->P.near_off.begin(), c->P.near_off.end());
     upload(DP.near_off, no, s);
-    upload(DP.aca_order, c->P.aca_order, s);
-    DP.naca = (int)c->P.aca_order.size();
+    {
+      // large blocks first (CTA kernel, by decreasing m + n), then small ones (warp kernel)
+      std::vector<int> big, small;
+      for (int b : c->P.aca_order) {
+        const int* q = &c->P.approx[4 * b];
+        ((q[1] - q[0]) <= 64 && (q[3] - q[2]) <= 64 ? small : big).push_back(b);
+      }
+      DP.naca = (int)big.size();
+      big.insert(big.end(), small.begin(), small.end());
+      upload(DP.aca_order, big, s);
+    }
     upload(DP.near_seg, std::vector<long long>(c->P.near_seg.begin(), c->P.near_seg.end()), s);
     upload(DP.didx_ptr, c->P.didx_ptr, s);
     upload(DP.didx, c->P.didx, s);
@@ -878,6 +918,8 @@ int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int N
     upload(DP.blk_fw, c->P.blk_fw, s);
     upload(DP.blk_tr_ptr, c->P.blk_tr_ptr, s);
     upload(DP.blk_tr, c->P.blk_tr, s);
+    upload(DP.fw_pos, c->P.fw_pos, s);
+    upload(DP.tr_pos, c->P.tr_pos, s);
     c->sum_mn = 0;
     c->worst_pool = 0;
     for (int b = 0; b < DP.na; b++) {

@@ -281,6 +281,172 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
   if (tid == 0) A.rank[b] = nst;
 }
 
+// ------------------------------------------------------------------------------------------
+// Warp-per-block ACA for small blocks (m, n <= 64): the same sequence as aca_kernel (pivot rules,
+// stop rule, dropped converging term, zero terms not stored, exactly-zero blocks skipped) with
+// warp shuffles in place of block barriers. Each lane owns rows / columns l and l + 32.
+// ------------------------------------------------------------------------------------------
+constexpr int kWarpAcaMax = 64;
+
+template <typename R>
+__device__ __forceinline__ void warp_argmax(R& val, int& idx) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    R ov = __shfl_xor_sync(0xffffffffu, val, o);
+    int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ov > val || (ov == val && oi < idx)) {
+      val = ov;
+      idx = oi;
+    }
+  }
+}
+
+template <typename R, typename P4>
+__global__ void __launch_bounds__(256) aca_warp_kernel(AcaArgs<R, P4> A, int nblocks) {
+  __shared__ cplx<R> s_uq[8][kWarpAcaMax];
+  __shared__ cplx<R> s_vq[8][kWarpAcaMax];
+  __shared__ long long s_toff[8][kWarpAcaMax];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int bi = blockIdx.x * 8 + warp;
+  if (bi >= nblocks) return;
+  const int b = A.order[bi];
+  const int4 q = A.blocks[b];
+  const int rs = q.x, cs = q.z, m = q.y - q.x, n = q.w - q.z;
+  int iter_lim = min(A.maxk, min(m - 1, n - 1));
+  if (iter_lim < 0) iter_lim = 0;
+  cplx<R>* uq = s_uq[warp];
+  cplx<R>* vq = s_vq[warp];
+  long long* toff = s_toff[warp];
+
+  if (A.zero_guard && iter_lim > 0) {  // exactly-zero block (see aca_kernel)
+    bool zero = false;
+    for (int d = 0; d < 3 && !zero; d++) {
+      const double4 a0 = A.G.va[cs];
+      const double v = d == 0 ? a0.x : (d == 1 ? a0.y : a0.z);
+      bool ok = true;
+      for (int j = lane; j < n; j += 32) {
+        const double4 a = A.G.va[cs + j];
+        const ElemGeo<R> g = A.G.eg[cs + j];
+        ok = ok && (d == 0 ? a.x : (d == 1 ? a.y : a.z)) == v && g.ab[d] == R(0) && g.ac[d] == R(0);
+      }
+      for (int i = lane; i < m; i += 32) {
+        const double4 p = A.G.cen[rs + i];
+        ok = ok && (d == 0 ? p.x : (d == 1 ? p.y : p.z)) == v;
+      }
+      zero = __all_sync(0xffffffffu, ok);
+    }
+    if (zero) {
+      if (lane == 0) A.rank[b] = 0;
+      return;
+    }
+  }
+
+  unsigned long long used = 1ull;  // row 0
+  double err = 0;
+  int i = 0, iter = 0, nst = 0;
+  bool need_alloc = true;
+  long long base = 0;
+  while (iter < iter_lim) {
+    if (need_alloc) {
+      unsigned long long bb = 0;
+      int ovf = 0;
+      if (lane == 0) {
+        const unsigned long long need = (unsigned long long)(m + n);
+        bb = atomicAdd(A.pool_used, need);
+        ovf = bb + need > (unsigned long long)A.pool_cap;
+        if (ovf) atomicOr(A.status, 1);
+      }
+      ovf = __shfl_sync(0xffffffffu, ovf, 0);
+      if (ovf) break;
+      base = (long long)__shfl_sync(0xffffffffu, bb, 0);
+      need_alloc = false;
+    }
+    cplx<R>* unew = A.pool + base;
+    cplx<R>* vnew = unew + m;
+    for (int p = lane; p < nst; p += 32) uq[p] = A.pool[toff[p] + i];
+    __syncwarp();
+    // row residual and column pivot
+    const P4 pi = A.rowpts[rs + i];
+    R best = R(-1);
+    int bidx = 0;
+    for (int c = lane; c < n; c += 32) {
+      cplx<R> v = entry_far<R>(A.k, A.G, pi, cs + c);
+      for (int p = 0; p < nst; p++) cfms(v, uq[p], A.pool[toff[p] + m + c]);
+      vnew[c] = v;
+      const R a = abs2(v);
+      if (a > best) {
+        best = a;
+        bidx = c;
+      }
+    }
+    warp_argmax<R>(best, bidx);
+    const int j = bidx;
+    __syncwarp();
+    const cplx<R> vj = vnew[j];
+    for (int p = lane; p < nst; p += 32) vq[p] = A.pool[toff[p] + m + j];
+    __syncwarp();
+    const bool keep = A.zero_guard && vj.re == R(0) && vj.im == R(0);
+    double vn = 0;
+    for (int c = lane; c < n; c += 32) {
+      cplx<R> v = vnew[c];
+      if (!keep) v = cdiv(v, vj);
+      vnew[c] = v;
+      vn += (double)v.re * (double)v.re + (double)v.im * (double)v.im;
+    }
+    // column residual
+    double un = 0;
+    for (int r = lane; r < m; r += 32) {
+      cplx<R> u = entry_far<R>(A.k, A.G, A.rowpts[rs + r], cs + j);
+      for (int p = 0; p < nst; p++) cfms(u, A.pool[toff[p] + r], vq[p]);
+      unew[r] = u;
+      un += (double)u.re * (double)u.re + (double)u.im * (double)u.im;
+    }
+    __syncwarp();
+    // cross terms
+    double dots = 0;
+    for (int p = 0; p < nst; p++) {
+      const cplx<R>* Up = A.pool + toff[p];
+      const cplx<R>* Vp = Up + m;
+      cplx<R> ud(0, 0), vd(0, 0);
+      for (int r = lane; r < m; r += 32) cfma(ud, unew[r], Up[r]);
+      for (int c = lane; c < n; c += 32) cfma(vd, vnew[c], Vp[c]);
+      const double udr = warp_sum((double)ud.re), udi = warp_sum((double)ud.im);
+      const double vdr = warp_sum((double)vd.re), vdi = warp_sum((double)vd.im);
+      dots += sqrt(udr * udr + udi * udi) * sqrt(vdr * vdr + vdi * vdi);
+    }
+    un = warp_sum(un);
+    vn = warp_sum(vn);
+    err += un * vn + 2 * dots;
+    if (sqrt(un * vn / err) <= A.eps) break;
+    const bool zero_term = (un == 0.0) || (vn == 0.0);
+    // next row pivot over unused rows
+    best = R(-1);
+    bidx = 0;
+    for (int r = lane; r < m; r += 32) {
+      if ((used >> r) & 1ull) continue;
+      const R a = abs2(unew[r]);
+      if (a > best) {
+        best = a;
+        bidx = r;
+      }
+    }
+    warp_argmax<R>(best, bidx);
+    i = bidx;
+    used |= 1ull << i;
+    if (!zero_term) {
+      if (lane == 0) {
+        toff[nst] = base;
+        A.term_off[(long long)b * A.maxk + nst] = base;
+      }
+      nst++;
+      need_alloc = true;
+    }
+    iter++;
+    __syncwarp();
+  }
+  if (lane == 0) A.rank[b] = nst;
+}
+
 __global__ void rank_scan_kernel(const int* __restrict__ rank, int na, int* t_off) {
   __shared__ int sums[1024];
   const int tid = threadIdx.x;
@@ -330,6 +496,14 @@ void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat&
 }
 
 template <typename R, typename P4>
+static void aca_launch_warp(const AcaArgs<R, P4>& a, int nblocks, cudaStream_t s) {
+  if (nblocks <= 0) return;
+  note_launch();
+  aca_warp_kernel<R, P4><<<(nblocks + 7) / 8, 256, 0, s>>>(a, nblocks);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+template <typename R, typename P4>
 static void aca_launch_t(const AcaArgs<R, P4>& a, int nblocks, int max_rows, cudaStream_t s) {
   size_t smem = (size_t)a.iter_cap * (2 * sizeof(cplx<R>) + sizeof(long long)) + (size_t)((max_rows + 31) / 32) * 4;
   if (smem > 48 * 1024) {
@@ -350,12 +524,16 @@ void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double
                                H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
                                H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
     if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
+    a.order = DP.aca_order.as<int>() + DP.naca;
+    aca_launch_warp(a, DP.na - DP.naca, s);
   } else {
     AcaArgs<float, float4> a{geo_view<float>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
                              G.cen32.as<float4>(), (float)H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cf>(),
                              H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
                              H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
     if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
+    a.order = DP.aca_order.as<int>() + DP.naca;
+    aca_launch_warp(a, DP.na - DP.naca, s);
   }
 }
 

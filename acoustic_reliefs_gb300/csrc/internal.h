@@ -93,6 +93,7 @@ struct Partition {
   // per admissible block: its entries in the fw_lr / tr_lr lists (one per row / column leaf),
   // in leaf order; the matvec sums a term's per-leaf partial dots over these
   std::vector<int> blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
+  std::vector<int> fw_pos, tr_pos;     // list entry -> its position in the block-major lists
   std::vector<int> iter_lim;           // per admissible block: min(maxk, m - 1, n - 1)
   std::vector<int> aca_order;          // admissible blocks by decreasing m + n
   int max_rows = 0;                    // largest admissible block row count
@@ -109,10 +110,12 @@ void build_leaf_lists(Partition& P, int maxk);
 // ------------------------------------------------------------------------------------------
 struct DevPartition {
   int nleaf = 0, nd = 0, na = 0;
-  int naca = 0;  // admissible blocks launched for ACA
+  int naca = 0;  // admissible blocks for the CTA ACA kernel (aca_order[0, naca)); the rest are
+                 // small (m, n <= 64) and run one per warp
   int max_leaf = 0;
   DevBuf near_seg, didx_ptr, didx;
   DevBuf blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
+  DevBuf fw_pos, tr_pos;
   DevBuf blocks_d, blocks_a;            // int4
   DevBuf leaf_start;                    // int (nleaf + 1)
   DevBuf fw_near_ptr, fw_near, fw_lr_ptr, fw_lr;
@@ -151,7 +154,8 @@ struct DevHMat {
   DevBuf seg_f, seg_t;    // int64 [nleaf + 1]: element prefix of the U / V segments
   DevBuf useg, vseg;      // R x K column-major slices of U (row leaves) / V (column leaves)
   DevBuf uidx, vidx;      // int: phase-1 output index of every segment column (-1: padding)
-  DevBuf kpos_f, kpos_t;  // int: first segment column of every fw_lr / tr_lr list entry
+  DevBuf kpos_f, kpos_t;  // int: first segment column of every list entry, block-major order
+  DevBuf order_rows, order_cols;  // int [nleaf]: leaves by decreasing streamed bytes (gather / dot)
   DevBuf pbuf;            // per-column partial dots of the dot pass
   DevBuf err;             // int: set by a kernel whose copy pipeline timed out
   int64_t task_cap = 0;   // upper bound of the number of stored terms

@@ -34,6 +34,7 @@ __device__ __forceinline__ void cmac(AT& ar, AT& ai, const A& a, const X& x) {
 
 struct SegView {
   const int* leaf_start;
+  const int* order;  // CTA -> leaf, leaves by decreasing work
   // region A: near segments (forward gather only)
   const long long* a_seg;
   const int* a_kptr;
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
   if (done && *done) return;
-  const int leaf = blockIdx.x;
+  const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
   if (K == 0) return;
@@ -203,13 +204,13 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
                   });
 }
 
-// t[task] = sum over the leaf entries of the task's block of p[kpos[e] + q], in leaf order.
+// t[task] = sum over the leaf entries of the task's block of p[kpos[e] + q], in leaf order
+// (kpos is stored block-major, so a block's entries are consecutive).
 template <typename AT>
 __global__ void seg_reduce_kernel(const int* __restrict__ task_b, const int* __restrict__ t_off, int ntask_cap,
                                   const int* __restrict__ t_total, const int* __restrict__ ent_ptr,
-                                  const int* __restrict__ ent, const int* __restrict__ kpos,
-                                  const cplx<AT>* __restrict__ p, cplx<AT>* __restrict__ t,
-                                  const int* __restrict__ done) {
+                                  const int* __restrict__ kpos, const cplx<AT>* __restrict__ p,
+                                  cplx<AT>* __restrict__ t, const int* __restrict__ done) {
   if (done && *done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *t_total || i >= ntask_cap) return;
@@ -217,7 +218,7 @@ __global__ void seg_reduce_kernel(const int* __restrict__ task_b, const int* __r
   const int q = i - t_off[b];
   AT sr = 0, si = 0;
   for (int e = ent_ptr[b]; e < ent_ptr[b + 1]; e++) {
-    const cplx<AT> v = p[kpos[ent[e]] + q];
+    const cplx<AT> v = p[kpos[e] + q];
     sr += v.re;
     si += v.im;
   }
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ double sdot[kWarps][5];
   if (done && *done) return;
-  const int leaf = blockIdx.x;
+  const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   AT ar[RPL], ai[RPL];
@@ -437,6 +438,7 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
     SegView d = v;
     d.b_seg = tr ? H.seg_f.as<long long>() : H.seg_t.as<long long>();
     d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
+    d.order = tr ? H.order_rows.as<int>() : H.order_cols.as<int>();
     note_launch();
     seg_dot_kernel<MT, VT, AT, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, (const cplx<VT>*)x,
                                                                             p, done);
@@ -444,13 +446,14 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
     note_launch();
     seg_reduce_kernel<AT><<<(int)((H.task_cap + 255) / 256), 256, 0, s>>>(
         H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na,
-        tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? DP.blk_fw.as<int>() : DP.blk_tr.as<int>(),
-        tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(), p, t, done);
+        tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(), p, t,
+        done);
     AC3D_CUDA(cudaGetLastError());
   }
   v.b_seg = tr ? H.seg_t.as<long long>() : H.seg_f.as<long long>();
   v.b_kptr = tr ? H.kseg_t.as<int>() : H.kseg_f.as<int>();
   v.b_idx = tr ? H.vidx.as<int>() : H.uidx.as<int>();
+  v.order = tr ? H.order_cols.as<int>() : H.order_rows.as<int>();
   note_launch();
   if (tr)
     seg_gather_kernel<MT, VT, AT, true, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(

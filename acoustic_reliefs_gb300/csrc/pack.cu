@@ -66,7 +66,7 @@ __global__ void pack_segments_kernel(const cplx<R>* __restrict__ pool, const lon
                                      const int4* __restrict__ blocks, const int* __restrict__ leaf_start,
                                      const int* __restrict__ ptr, const int* __restrict__ items, int cols,
                                      const int* __restrict__ kseg, const long long* __restrict__ seg, cplx<R>* S,
-                                     int* sidx, int* kpos) {
+                                     int* sidx, const int* __restrict__ pos, int* kpos) {
   const int l = blockIdx.x;
   const int ls = leaf_start[l], Rn = leaf_start[l + 1] - ls;
   cplx<R>* dst = S + seg[l];
@@ -83,7 +83,7 @@ __global__ void pack_segments_kernel(const cplx<R>* __restrict__ pool, const lon
       dst[(long long)(kbase + q) * Rn + row] = pool[to[q] + off + row];
     }
     for (int q = threadIdx.x; q < r; q += blockDim.x) idx[kbase + q] = t_off[b] + q;
-    if (threadIdx.x == 0) kpos[it] = kseg[l] + kbase;
+    if (threadIdx.x == 0) kpos[pos[it]] = kseg[l] + kbase;  // block-major order
     kbase += r;
   }
   if (kbase & 1) {  // padding column
@@ -110,7 +110,7 @@ static void pack_side(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_
                                                    H.t_off.as<int>(), H.rank.as<int>(), DP.blocks_a.as<int4>(),
                                                    DP.leaf_start.as<int>(), ptr, items, cols ? 1 : 0, kseg.as<int>(),
                                                    seg.as<long long>(), S.as<cplx<R>>(), idx.as<int>(),
-                                                   kpos.as<int>());
+                                                   cols ? DP.tr_pos.as<int>() : DP.fw_pos.as<int>(), kpos.as<int>());
   AC3D_CUDA(cudaGetLastError());
 }
 

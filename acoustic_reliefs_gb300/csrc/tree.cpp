@@ -201,16 +201,20 @@ void build_leaf_lists(Partition& P, int maxk) {
     P.iter_lim[b] = std::max(0, std::min(maxk, std::min(q[1] - q[0] - 1, q[3] - q[2] - 1)));
   }
   // block -> its entries in the leaf lists, in leaf order
-  auto inv = [&](const std::vector<int>& items, std::vector<int>& bptr, std::vector<int>& bl) {
+  auto inv = [&](const std::vector<int>& items, std::vector<int>& bptr, std::vector<int>& bl, std::vector<int>& pos) {
     bptr.assign(na + 1, 0);
     for (int b : items) bptr[b + 1]++;
     for (int b = 0; b < na; b++) bptr[b + 1] += bptr[b];
     bl.assign(items.size(), 0);
+    pos.assign(items.size(), 0);
     std::vector<int> fill(bptr.begin(), bptr.end() - 1);
-    for (size_t e = 0; e < items.size(); e++) bl[fill[items[e]]++] = (int)e;
+    for (size_t e = 0; e < items.size(); e++) {
+      pos[e] = fill[items[e]];
+      bl[fill[items[e]]++] = (int)e;
+    }
   };
-  inv(P.fw_lr, P.blk_fw_ptr, P.blk_fw);
-  inv(P.tr_lr, P.blk_tr_ptr, P.blk_tr);
+  inv(P.fw_lr, P.blk_fw_ptr, P.blk_fw, P.fw_pos);
+  inv(P.tr_lr, P.blk_tr_ptr, P.blk_tr, P.tr_pos);
 
   P.aca_order.resize(na);
   std::iota(P.aca_order.begin(), P.aca_order.end(), 0);
