@@ -145,6 +145,8 @@ struct ac3d_ctx {
   int maxk = 100;          // APPROX_ACA_MAX_K (constants.h:16)
 
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;                 // concurrent assembly work
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   ac3d_stats stats{};
 
@@ -200,6 +202,10 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
   launch_near_assembly(c->G, c->DP, *H, s);
   H->err.alloc(16, s);
   AC3D_CUDA(cudaMemsetAsync(H->err.p, 0, 16, s));
+  H->ticket.alloc(16, s);
+  AC3D_CUDA(cudaMemsetAsync(H->ticket.p, 0, 16, s));
+  H->arrivals.alloc((size_t)std::max(c->DP.na, 1) * sizeof(int), s);
+  AC3D_CUDA(cudaMemsetAsync(H->arrivals.p, 0, (size_t)std::max(c->DP.na, 1) * sizeof(int), s));
   const int na = c->DP.na;
   H->rank.alloc((size_t)std::max(na, 1) * sizeof(int), s);
   H->t_off.alloc((size_t)(na + 1) * sizeof(int), s);
@@ -214,7 +220,12 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
       H->pool.alloc((size_t)cap * cs, s);
       H->pool_cap = cap;
       AC3D_CUDA(cudaMemsetAsync(H->pool_used.p, 0, 16, s));
-      launch_aca(c->G, c->DP, *H, c->aca_tol, c->P.max_rows, s);
+      // small blocks (one warp each) run on the side stream, concurrently with the large ones
+      AC3D_CUDA(cudaEventRecord(c->ev_fork, s));
+      AC3D_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+      launch_aca(c->G, c->DP, *H, c->aca_tol, c->P.max_rows, s, c->side);
+      AC3D_CUDA(cudaEventRecord(c->ev_join, c->side));
+      AC3D_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
       unsigned long long hu[2];
       AC3D_CUDA(cudaMemcpyAsync(hu, H->pool_used.p, 16, cudaMemcpyDeviceToHost, s));
       AC3D_CUDA(cudaStreamSynchronize(s));
@@ -352,7 +363,7 @@ void ensure_work(ac3d_ctx* c) {
   const int G = krylov_vec_grid(c->Ne);
   c->partials.ensure((size_t)(c->DP.nleaf + G) * 5 * sizeof(double) + 64, s);
   c->kstate.ensure(sizeof(KState), s);
-  c->red.ensure(8 * sizeof(double), s);
+  c->red.ensure(16 * sizeof(double), s);
   c->b64.ensure(n * sizeof(cd), s);
   c->x64.ensure(n * sizeof(cd), s);
   c->r64.ensure(n * sizeof(cd), s);
@@ -372,6 +383,7 @@ KrylovBufs bufs(ac3d_ctx* c, int vec64) {
   B.partials = c->partials.as<double>();
   B.nparts_r = krylov_vec_grid(c->Ne);
   B.nleaf = c->DP.nleaf;
+  B.red5 = c->red.as<double>() + 8;
   B.state = c->kstate.as<KState>();
   return B;
 }
@@ -755,6 +767,9 @@ int ac3d_create(ac3d_ctx** out, int cluster_size, double radius_factor, const do
   c->Ls = hemisphere(listener_radius, listener_ds);
   int rc = guard(c, [&] {
     AC3D_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    AC3D_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     int dev = 0;
     AC3D_CUDA(cudaGetDevice(&dev));
     cudaMemPool_t pool;
@@ -784,6 +799,12 @@ void ac3d_destroy(ac3d_ctx* c) {
   for (DevBuf* b : bufs) b->release();
   c->DP = DevPartition();
   c->G = DevGeometry();
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (s) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);

@@ -515,7 +515,8 @@ static void aca_launch_t(const AcaArgs<R, P4>& a, int nblocks, int max_rows, cud
   AC3D_CUDA(cudaGetLastError());
 }
 
-void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s) {
+void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s,
+                cudaStream_t s_small) {
   if (DP.na == 0) return;
   int iter_cap = H.maxk;
   if (H.prec == PREC_FP64) {
@@ -525,7 +526,7 @@ void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double
                                H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
     if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
     a.order = DP.aca_order.as<int>() + DP.naca;
-    aca_launch_warp(a, DP.na - DP.naca, s);
+    aca_launch_warp(a, DP.na - DP.naca, s_small);
   } else {
     AcaArgs<float, float4> a{geo_view<float>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
                              G.cen32.as<float4>(), (float)H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cf>(),
@@ -533,7 +534,7 @@ void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double
                              H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
     if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
     a.order = DP.aca_order.as<int>() + DP.naca;
-    aca_launch_warp(a, DP.na - DP.naca, s);
+    aca_launch_warp(a, DP.na - DP.naca, s_small);
   }
 }
 

@@ -158,6 +158,8 @@ struct DevHMat {
   DevBuf order_rows, order_cols;  // int [nleaf]: leaves by decreasing streamed bytes (gather / dot)
   DevBuf pbuf;            // per-column partial dots of the dot pass
   DevBuf err;             // int: set by a kernel whose copy pipeline timed out
+  DevBuf arrivals;        // int [na]: dot-pass arrival counters (all zero between launches)
+  DevBuf ticket;          // unsigned: gather-pass completion ticket (zero between launches)
   int64_t task_cap = 0;   // upper bound of the number of stored terms
   DevBuf tvec;            // intermediate V x per term (complex, vector precision)
   DevBuf tvec64;          // FP64 intermediate for refinement residuals
@@ -181,7 +183,9 @@ void launch_pack_points(const double* p, int n, void* out, cudaStream_t s);
 void launch_rhs(const DevGeometry& G, int prec_vec64, double k, int kind, const double* v3, void* out, cudaStream_t s);
 
 void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s);
-void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s);
+// Large blocks run on s, small blocks (one warp each) on s_small, which may be another stream.
+void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s,
+                cudaStream_t s_small);
 void launch_rank_scan(const DevPartition& DP, DevHMat& H, cudaStream_t s);
 // Packs the pool into the U segments (row leaves, cols = false) or V segments (column leaves).
 void launch_pack(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_t s);
@@ -192,7 +196,8 @@ struct MatvecEpilogue {
   // optional fused dot products over the produced vector y (FP64 partials per CTA)
   const void* dot_a = nullptr;  // if set: partial sum conj(dot_a) . y
   const void* dot_b = nullptr;  // if set: partial sum conj(y) . dot_b  (and |y|^2)
-  double* partials = nullptr;   // per-CTA partials [grid x 6]
+  double* partials = nullptr;   // per-CTA partials [grid x 5]
+  double* red5 = nullptr;       // if set: the fixed-order total of the partials (last CTA writes it)
 };
 void launch_matvec(const DevPartition& DP, const DevHMat& H, int ne, bool transposed, int vec64,
                    const void* x, void* y, const void* b_minus, const MatvecEpilogue& ep, cudaStream_t s);

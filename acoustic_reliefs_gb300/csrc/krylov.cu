@@ -192,12 +192,12 @@ __global__ void __launch_bounds__(kVecThreads) kf_p(KState* st, const double* pa
 
 // alpha = rho / (rhat, v); s = r - alpha v
 template <typename VT>
-__global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* partials, int nparts, int n,
+__global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* red5, int n,
                                                     const cplx<VT>* __restrict__ r, const cplx<VT>* __restrict__ v,
                                                     cplx<VT>* s) {
   if (st->done) return;
   double d[5];
-  reduce_partials(partials, nparts, d);
+  for (int i = 0; i < 5; i++) d[i] = red5[i];
   double ar, ai;
   if (d[0] == 0.0 && d[1] == 0.0) {
     if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 3;
@@ -217,13 +217,13 @@ __global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* pa
 
 // omega = (t, s) / (t, t); x += alpha p + omega s; r = s - omega t; partials (rhat, r), |r|^2
 template <typename VT>
-__global__ void __launch_bounds__(kVecThreads) kf_xr(KState* st, const double* partials, int nparts, int n, cplx<VT>* x,
+__global__ void __launch_bounds__(kVecThreads) kf_xr(KState* st, const double* red5, int n, cplx<VT>* x,
                                                      const cplx<VT>* __restrict__ p, const cplx<VT>* __restrict__ s,
                                                      cplx<VT>* r, const cplx<VT>* __restrict__ t,
                                                      const cplx<VT>* __restrict__ rhat, double* out_partials) {
   if (st->done) return;
   double d5[5];
-  reduce_partials(partials, nparts, d5);
+  for (int i = 0; i < 5; i++) d5[i] = red5[i];
   double wr_d = 0, wi_d = 0;
   if (d5[4] > 0.0) {
     wr_d = d5[2] / d5[4];
@@ -317,16 +317,17 @@ static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const
   MatvecEpilogue e1;
   e1.dot_a = B.rhat;
   e1.partials = B.partials;
+  e1.red5 = B.red5;
   launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s);
   note_launch();
-  kf_s<VT><<<G, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v,
-                                     (cplx<VT>*)B.s);
+  kf_s<VT><<<G, kVecThreads, 0, s>>>(st, B.red5, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v, (cplx<VT>*)B.s);
   MatvecEpilogue e2;
   e2.dot_b = B.s;
   e2.partials = B.partials;
+  e2.red5 = B.red5;
   launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s);
   note_launch();
-  kf_xr<VT><<<G, kVecThreads, 0, s>>>(st, B.partials, DP.nleaf, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p,
+  kf_xr<VT><<<G, kVecThreads, 0, s>>>(st, B.red5, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p,
                                       (const cplx<VT>*)B.s, (cplx<VT>*)B.r, (const cplx<VT>*)B.t,
                                       (const cplx<VT>*)B.rhat, rpart);
   AC3D_CUDA(cudaGetLastError());

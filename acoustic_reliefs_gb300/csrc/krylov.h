@@ -28,6 +28,7 @@ struct KrylovBufs {
   double* partials = nullptr;  // (nleaf + vector grid) x 5: per-leaf matvec partials, then vector partials
   int nparts_r = 0;            // number of partials feeding the rho step (vector grid)
   int nleaf = 0;
+  double* red5 = nullptr;      // fixed-order totals of the latest matvec's dot partials
   KState* state = nullptr;
 };
 

@@ -49,6 +49,14 @@ struct SegView {
   const int* trn_ptr;
   const int* trn;
   int* err;
+  // dot pass: the leaf's list of admissible blocks and the per-block reduction of its partials
+  const int* lr_ptr;
+  const int* lr_items;
+  const int* rank;
+  const int* t_off;
+  const int* ent_ptr;     // block -> its entries (block-major)
+  const int* kpos;        // entry -> first column of the block's terms in p
+  int* arrivals;          // per block: leaf CTAs done so far (reset by the last one)
 };
 
 // Iterates the chunks of the (up to two) regions of one leaf through the copy ring and calls
@@ -140,7 +148,7 @@ __device__ __forceinline__ void init_ring(uint64_t* full) {
 template <typename MT, typename VT, typename AT, int RPL>
 __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
                                                            const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ p,
-                                                           const int* __restrict__ done) {
+                                                           cplx<AT>* __restrict__ t, const int* __restrict__ done) {
   extern __shared__ __align__(128) unsigned char dsmem[];
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
@@ -148,7 +156,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
   const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
-  if (K == 0) return;
+  if (V.lr_ptr[leaf + 1] == V.lr_ptr[leaf]) return;  // no admissible block beside this leaf
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   AT xr[RPL], xi[RPL];
 #pragma unroll
@@ -202,27 +210,30 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
                       }
                     }
                   });
-}
-
-// t[task] = sum over the leaf entries of the task's block of p[kpos[e] + q], in leaf order
-// (kpos is stored block-major, so a block's entries are consecutive).
-template <typename AT>
-__global__ void seg_reduce_kernel(const int* __restrict__ task_b, const int* __restrict__ t_off, int ntask_cap,
-                                  const int* __restrict__ t_total, const int* __restrict__ ent_ptr,
-                                  const int* __restrict__ kpos, const cplx<AT>* __restrict__ p,
-                                  cplx<AT>* __restrict__ t, const int* __restrict__ done) {
-  if (done && *done) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *t_total || i >= ntask_cap) return;
-  const int b = task_b[i];
-  const int q = i - t_off[b];
-  AT sr = 0, si = 0;
-  for (int e = ent_ptr[b]; e < ent_ptr[b + 1]; e++) {
-    const cplx<AT> v = p[kpos[e] + q];
-    sr += v.re;
-    si += v.im;
+  // Per block of this leaf: count the leaf as arrived; the last leaf CTA of a block sums the
+  // block's partials over its leaves in fixed (leaf) order, so t is deterministic.
+  __syncthreads();
+  __threadfence();
+  __syncthreads();
+  for (int it = V.lr_ptr[leaf] + threadIdx.x; it < V.lr_ptr[leaf + 1]; it += kThreads) {
+    const int b = V.lr_items[it];
+    const int e0 = V.ent_ptr[b], ne = V.ent_ptr[b + 1] - e0;
+    if (atomicAdd(&V.arrivals[b], 1) == ne - 1) {
+      __threadfence();
+      const int r = V.rank[b];
+      cplx<AT>* tb = t + V.t_off[b];
+      for (int q = 0; q < r; q++) {
+        AT sr = 0, si = 0;
+        for (int e = e0; e < e0 + ne; e++) {
+          const cplx<AT>* pe = p + V.kpos[e] + q;
+          sr += __ldcg(&pe->re);
+          si += __ldcg(&pe->im);
+        }
+        tb[q] = cplx<AT>(sr, si);
+      }
+      V.arrivals[b] = 0;
+    }
   }
-  t[i] = cplx<AT>(sr, si);
 }
 
 // Gather pass: y[leaf rows] = -x/2 + S_A x[a_idx] + S_B t[b_idx] (+ transposed dense blocks), or
@@ -232,8 +243,9 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
     SegView V, const cplx<MT>* __restrict__ near, const cplx<MT>* __restrict__ lrseg, const cplx<AT>* __restrict__ t,
     const cplx<VT>* __restrict__ x, cplx<VT>* __restrict__ y, const cplx<VT>* __restrict__ bminus,
     const cplx<VT>* __restrict__ dot_a, const cplx<VT>* __restrict__ dot_b, double* partials,
-    const int* __restrict__ done) {
+    double* red5, unsigned* ticket, const int* __restrict__ done) {
   extern __shared__ __align__(128) unsigned char dsmem[];
+  __shared__ bool s_last;
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ double sdot[kWarps][5];
@@ -374,6 +386,30 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
       for (int w = 0; w < kWarps; w++) s += sdot[w][threadIdx.x];
       partials[(size_t)leaf * 5 + threadIdx.x] = s;
     }
+    if (red5) {
+      // the last CTA to finish reduces all leaves' partials in fixed order into red5
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        double acc[5] = {0, 0, 0, 0, 0};
+        for (int l = threadIdx.x; l < (int)gridDim.x; l += kThreads)
+          for (int i = 0; i < 5; i++) acc[i] += __ldcg(&partials[(size_t)l * 5 + i]);
+        for (int i = 0; i < 5; i++) acc[i] = warp_sum(acc[i]);
+        __syncthreads();
+        if (lane == 0)
+          for (int i = 0; i < 5; i++) sdot[warp][i] = acc[i];
+        __syncthreads();
+        if (threadIdx.x < 5) {
+          double sum = 0;
+          for (int w = 0; w < kWarps; w++) sum += sdot[w][threadIdx.x];
+          red5[threadIdx.x] = sum;
+        }
+        if (threadIdx.x == 0) *ticket = 0u;
+      }
+    }
   }
 }
 
@@ -439,15 +475,16 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
     d.b_seg = tr ? H.seg_f.as<long long>() : H.seg_t.as<long long>();
     d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
     d.order = tr ? H.order_rows.as<int>() : H.order_cols.as<int>();
+    d.lr_ptr = tr ? DP.fw_lr_ptr.as<int>() : DP.tr_lr_ptr.as<int>();
+    d.lr_items = tr ? DP.fw_lr.as<int>() : DP.tr_lr.as<int>();
+    d.rank = H.rank.as<int>();
+    d.t_off = H.t_off.as<int>();
+    d.ent_ptr = tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>();
+    d.kpos = tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>();
+    d.arrivals = H.arrivals.as<int>();
     note_launch();
     seg_dot_kernel<MT, VT, AT, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, (const cplx<VT>*)x,
-                                                                            p, done);
-    AC3D_CUDA(cudaGetLastError());
-    note_launch();
-    seg_reduce_kernel<AT><<<(int)((H.task_cap + 255) / 256), 256, 0, s>>>(
-        H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na,
-        tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(), p, t,
-        done);
+                                                                            p, t, done);
     AC3D_CUDA(cudaGetLastError());
   }
   v.b_seg = tr ? H.seg_t.as<long long>() : H.seg_f.as<long long>();
@@ -458,11 +495,11 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
   if (tr)
     seg_gather_kernel<MT, VT, AT, true, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
         v, H.near.as<cplx<MT>>(), vseg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
-        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
+        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
   else
     seg_gather_kernel<MT, VT, AT, false, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
         v, H.near.as<cplx<MT>>(), useg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
-        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, done);
+        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
   AC3D_CUDA(cudaGetLastError());
 }
 
