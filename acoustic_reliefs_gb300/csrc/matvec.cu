@@ -211,28 +211,39 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
                     }
                   });
   // Per block of this leaf: count the leaf as arrived; the last leaf CTA of a block sums the
-  // block's partials over its leaves in fixed (leaf) order, so t is deterministic.
+  // block's partials over its leaves in fixed (leaf) order, so t is deterministic. Blocks this
+  // CTA completes are collected first, then reduced one warp per block, lanes over terms.
+  __shared__ int s_last[kThreads];
+  __shared__ int s_nlast;
   __syncthreads();
   __threadfence();
-  __syncthreads();
-  for (int it = V.lr_ptr[leaf] + threadIdx.x; it < V.lr_ptr[leaf + 1]; it += kThreads) {
-    const int b = V.lr_items[it];
-    const int e0 = V.ent_ptr[b], ne = V.ent_ptr[b + 1] - e0;
-    if (atomicAdd(&V.arrivals[b], 1) == ne - 1) {
-      __threadfence();
+  for (int base = V.lr_ptr[leaf]; base < V.lr_ptr[leaf + 1]; base += kThreads) {
+    if (threadIdx.x == 0) s_nlast = 0;
+    __syncthreads();
+    const int it = base + threadIdx.x;
+    if (it < V.lr_ptr[leaf + 1]) {
+      const int b = V.lr_items[it];
+      if (atomicAdd(&V.arrivals[b], 1) == V.ent_ptr[b + 1] - V.ent_ptr[b] - 1) s_last[atomicAdd(&s_nlast, 1)] = b;
+    }
+    __syncthreads();
+    __threadfence();
+    for (int w = warp; w < s_nlast; w += kWarps) {
+      const int b = s_last[w];
+      const int e0 = V.ent_ptr[b], e1 = V.ent_ptr[b + 1];
       const int r = V.rank[b];
       cplx<AT>* tb = t + V.t_off[b];
-      for (int q = 0; q < r; q++) {
+      for (int q = lane; q < r; q += 32) {
         AT sr = 0, si = 0;
-        for (int e = e0; e < e0 + ne; e++) {
+        for (int e = e0; e < e1; e++) {
           const cplx<AT>* pe = p + V.kpos[e] + q;
           sr += __ldcg(&pe->re);
           si += __ldcg(&pe->im);
         }
         tb[q] = cplx<AT>(sr, si);
       }
-      V.arrivals[b] = 0;
+      if (lane == 0) V.arrivals[b] = 0;
     }
+    __syncthreads();
   }
 }
 
