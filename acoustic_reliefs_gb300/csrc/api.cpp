@@ -204,8 +204,7 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
   AC3D_CUDA(cudaMemsetAsync(H->err.p, 0, 16, s));
   H->ticket.alloc(16, s);
   AC3D_CUDA(cudaMemsetAsync(H->ticket.p, 0, 16, s));
-  H->arrivals.alloc((size_t)std::max(c->DP.na, 1) * sizeof(int), s);
-  AC3D_CUDA(cudaMemsetAsync(H->arrivals.p, 0, (size_t)std::max(c->DP.na, 1) * sizeof(int), s));
+
   const int na = c->DP.na;
   H->rank.alloc((size_t)std::max(na, 1) * sizeof(int), s);
   H->t_off.alloc((size_t)(na + 1) * sizeof(int), s);

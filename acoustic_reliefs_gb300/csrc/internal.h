@@ -158,7 +158,6 @@ struct DevHMat {
   DevBuf order_rows, order_cols;  // int [nleaf]: leaves by decreasing streamed bytes (gather / dot)
   DevBuf pbuf;            // per-column partial dots of the dot pass
   DevBuf err;             // int: set by a kernel whose copy pipeline timed out
-  DevBuf arrivals;        // int [na]: dot-pass arrival counters (all zero between launches)
   DevBuf ticket;          // unsigned: gather-pass completion ticket (zero between launches)
   int64_t task_cap = 0;   // upper bound of the number of stored terms
   DevBuf tvec;            // intermediate V x per term (complex, vector precision)

@@ -49,14 +49,6 @@ struct SegView {
   const int* trn_ptr;
   const int* trn;
   int* err;
-  // dot pass: the leaf's list of admissible blocks and the per-block reduction of its partials
-  const int* lr_ptr;
-  const int* lr_items;
-  const int* rank;
-  const int* t_off;
-  const int* ent_ptr;     // block -> its entries (block-major)
-  const int* kpos;        // entry -> first column of the block's terms in p
-  int* arrivals;          // per block: leaf CTAs done so far (reset by the last one)
 };
 
 // Iterates the chunks of the (up to two) regions of one leaf through the copy ring and calls
@@ -148,7 +140,7 @@ __device__ __forceinline__ void init_ring(uint64_t* full) {
 template <typename MT, typename VT, typename AT, int RPL>
 __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
                                                            const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ p,
-                                                           cplx<AT>* __restrict__ t, const int* __restrict__ done) {
+                                                           const int* __restrict__ done) {
   extern __shared__ __align__(128) unsigned char dsmem[];
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
@@ -156,7 +148,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
   const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
-  if (V.lr_ptr[leaf + 1] == V.lr_ptr[leaf]) return;  // no admissible block beside this leaf
+  if (K == 0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   AT xr[RPL], xi[RPL];
 #pragma unroll
@@ -210,41 +202,44 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
                       }
                     }
                   });
-  // Per block of this leaf: count the leaf as arrived; the last leaf CTA of a block sums the
-  // block's partials over its leaves in fixed (leaf) order, so t is deterministic. Blocks this
-  // CTA completes are collected first, then reduced one warp per block, lanes over terms.
-  __shared__ int s_last[kThreads];
-  __shared__ int s_nlast;
-  __syncthreads();
-  __threadfence();
-  for (int base = V.lr_ptr[leaf]; base < V.lr_ptr[leaf + 1]; base += kThreads) {
-    if (threadIdx.x == 0) s_nlast = 0;
-    __syncthreads();
-    const int it = base + threadIdx.x;
-    if (it < V.lr_ptr[leaf + 1]) {
-      const int b = V.lr_items[it];
-      if (atomicAdd(&V.arrivals[b], 1) == V.ent_ptr[b + 1] - V.ent_ptr[b] - 1) s_last[atomicAdd(&s_nlast, 1)] = b;
-    }
-    __syncthreads();
-    __threadfence();
-    for (int w = warp; w < s_nlast; w += kWarps) {
-      const int b = s_last[w];
-      const int e0 = V.ent_ptr[b], e1 = V.ent_ptr[b + 1];
-      const int r = V.rank[b];
-      cplx<AT>* tb = t + V.t_off[b];
-      for (int q = lane; q < r; q += 32) {
-        AT sr = 0, si = 0;
-        for (int e = e0; e < e1; e++) {
-          const cplx<AT>* pe = p + V.kpos[e] + q;
-          sr += __ldcg(&pe->re);
-          si += __ldcg(&pe->im);
-        }
-        tb[q] = cplx<AT>(sr, si);
-      }
-      if (lane == 0) V.arrivals[b] = 0;
-    }
-    __syncthreads();
+}
+
+// t[task] = sum over the leaf entries of the task's block of p[kpos[e] + q], in leaf order
+// (kpos is stored block-major, so a block's entries are consecutive).
+template <typename AT>
+__global__ void __launch_bounds__(256) seg_reduce_kernel(const int* __restrict__ task_b,
+                                                         const int* __restrict__ t_off, int ntask_cap,
+                                                         const int* __restrict__ t_total,
+                                                         const int* __restrict__ ent_ptr,
+                                                         const int* __restrict__ kpos,
+                                                         const cplx<AT>* __restrict__ p, cplx<AT>* __restrict__ t,
+                                                         const int* __restrict__ done) {
+  if (done && *done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntask_cap || i >= *t_total) return;
+  const int b = task_b[i];
+  const int q = i - t_off[b];
+  const int e0 = ent_ptr[b], e1 = ent_ptr[b + 1];
+  AT sr = 0, si = 0;
+  int e = e0;
+  for (; e + 3 < e1; e += 4) {
+    const int k0 = kpos[e], k1 = kpos[e + 1], k2 = kpos[e + 2], k3 = kpos[e + 3];
+    const cplx<AT> v0 = p[k0 + q], v1 = p[k1 + q], v2 = p[k2 + q], v3 = p[k3 + q];
+    sr += v0.re;
+    si += v0.im;
+    sr += v1.re;
+    si += v1.im;
+    sr += v2.re;
+    si += v2.im;
+    sr += v3.re;
+    si += v3.im;
   }
+  for (; e < e1; e++) {
+    const cplx<AT> v = p[kpos[e] + q];
+    sr += v.re;
+    si += v.im;
+  }
+  t[i] = cplx<AT>(sr, si);
 }
 
 // Gather pass: y[leaf rows] = -x/2 + S_A x[a_idx] + S_B t[b_idx] (+ transposed dense blocks), or
@@ -486,16 +481,15 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
     d.b_seg = tr ? H.seg_f.as<long long>() : H.seg_t.as<long long>();
     d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
     d.order = tr ? H.order_rows.as<int>() : H.order_cols.as<int>();
-    d.lr_ptr = tr ? DP.fw_lr_ptr.as<int>() : DP.tr_lr_ptr.as<int>();
-    d.lr_items = tr ? DP.fw_lr.as<int>() : DP.tr_lr.as<int>();
-    d.rank = H.rank.as<int>();
-    d.t_off = H.t_off.as<int>();
-    d.ent_ptr = tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>();
-    d.kpos = tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>();
-    d.arrivals = H.arrivals.as<int>();
     note_launch();
     seg_dot_kernel<MT, VT, AT, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, (const cplx<VT>*)x,
-                                                                            p, t, done);
+                                                                            p, done);
+    AC3D_CUDA(cudaGetLastError());
+    note_launch();
+    seg_reduce_kernel<AT><<<(int)((H.task_cap + 255) / 256), 256, 0, s>>>(
+        H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na,
+        tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(), p, t,
+        done);
     AC3D_CUDA(cudaGetLastError());
   }
   v.b_seg = tr ? H.seg_t.as<long long>() : H.seg_f.as<long long>();
