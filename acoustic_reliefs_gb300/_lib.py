@@ -50,6 +50,7 @@ SIGNATURES = {
     "ac3d_sphere": (_I, [_P, _I, _P, _I, _D, _I, _D, _I, _P]),
     "ac3d_get_stats": (_I, [_P, _P]),
     "ac3d_matvec_timing": (_I, [_P, _I, _I, _P, _P]),
+    "ac3d_far_field_noalloc": (_I, [_P, _I, _P, _I, _P, _D, _P, _I, _P, _P]),
     "ac3d_partition_build": (_I, [_P, _I, _P, _I, _I, _D, ctypes.POINTER(_P)]),
     "ac3d_partition_counts": (_I, [_P, _P, _P, _P, _P]),
     "ac3d_partition_get": (_I, [_P, _P, _P, _P, _P]),

@@ -129,6 +129,21 @@ int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
  * stored matrix entries x entry size + 16 Ne (read x, write y). No reference counterpart. */
 int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_matvec, long long* bytes);
 
+/* Receiver far field y_l = sum_j M(receiver l, element j) x_j (FP64), with every argument in
+ * device memory: Ps_dev (V x 3 float64), Es_dev (Ne x 3 int32, the connectivity x is ordered by,
+ * e.g. the Es returned by ac3d_set_mesh), x_dev (Ne complex), Ls_dev (L x 3 float64), y_dev (L
+ * complex); k = 2 pi f / 344. It allocates no device memory: for callers that cannot allocate
+ * at that point (a real-time audio callback, a frame loop, a host whose allocator owns the device
+ * memory). Its scratch is a fixed 65536-entry (1 MiB) array reserved on every GPU that loads the
+ * library; L above 65536 is rejected with AC3D_ERR_RESOURCE. The first call on a device looks up
+ * that array's address, so make the first call on each device before any stream capture. All
+ * calls share the array: calls that overlap on the GPU (different streams) race. Work is ordered
+ * on `stream` (a cudaStream_t); the call does not wait for it. Elements whose indices fall
+ * outside [0, V) are skipped. No counterpart in the reference (its far field is a host ACA
+ * product, aca.cpp:84-134 with adjoint.cpp:101-102). */
+int ac3d_far_field_noalloc(const double* Ps_dev, int V, const int32_t* Es_dev, int Ne, const double* x_dev, double k,
+                           const double* Ls_dev, int L, double* y_dev, void* stream);
+
 /* Host-only cluster tree and block partition (ClusterTree, clustertree.cpp:49-137, as used by
  * set_mesh, acoustics3d.cpp:43-58). No GPU work: for inspection and tests. */
 typedef struct ac3d_partition ac3d_partition;
