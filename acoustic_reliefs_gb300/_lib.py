@@ -55,6 +55,14 @@ SIGNATURES = {
     "ac3d_partition_counts": (_I, [_P, _P, _P, _P, _P]),
     "ac3d_partition_get": (_I, [_P, _P, _P, _P, _P]),
     "ac3d_partition_free": (None, [_P]),
+    "ac3d_server_create": (_I, [ctypes.POINTER(_P), _I, _I, ctypes.c_longlong]),
+    "ac3d_server_destroy": (None, [_P]),
+    "ac3d_server_last_error": (ctypes.c_char_p, [_P]),
+    "ac3d_server_add_mesh": (_I, [_P, _P, _I, _P, _I, _I, _D, _D, _D, _P, ctypes.POINTER(_I)]),
+    "ac3d_server_submit": (_I, [_P, _I, _D, _I, _P, _P, _I, ctypes.POINTER(ctypes.c_longlong)]),
+    "ac3d_server_poll": (_I, [_P, ctypes.c_longlong, ctypes.POINTER(_I)]),
+    "ac3d_server_wait": (_I, [_P, ctypes.c_longlong, _P, _P]),
+    "ac3d_admit_next": (_I, [_P, _P, _I, ctypes.c_longlong, ctypes.c_longlong, _I]),
 }
 
 
@@ -70,6 +78,22 @@ class Stats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class RequestInfo(ctypes.Structure):
+    """Mirror of ``ac3d_request_info``."""
+    _fields_ = [("status", _I), ("slot", _I), ("queue_ms", _D), ("run_ms", _D), ("latency_ms", _D),
+                ("footprint_bytes", ctypes.c_longlong), ("hmat_bytes", ctypes.c_longlong),
+                ("lr_entries", ctypes.c_longlong), ("near_entries", ctypes.c_longlong),
+                ("iterations", _I), ("outer_steps", _I), ("rel_residual", _D),
+                ("ms_assemble", _D), ("ms_solve", _D), ("ms_listener", _D)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
+SERVE_MAX_BYPASS = 8
 
 
 class AC3DError(RuntimeError):

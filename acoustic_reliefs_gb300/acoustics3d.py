@@ -182,6 +182,23 @@ class DiffBEM:
         self._check(_L.lib().ac3d_gradient(self._h, _L.ptr(xx), ctypes.byref(c), _L.ptr(g)))
         return c.value, g
 
+    def value_dev(self, x_ptr: int | None, c_ptr: int, stream: int = 0) -> None:
+        """value(x) with x (HH float64, or None for the stored heights) and c (one float64) in device
+        memory, ordered on the CUDA stream handle `stream`; c is the band mean."""
+        self._actual_unsupported()
+        self._check(_L.lib().ac3d_value_dev(self._h, ctypes.c_void_p(x_ptr or 0), ctypes.c_void_p(c_ptr),
+                                            ctypes.c_void_p(stream)))
+
+    def gradient_dev(self, x_ptr: int, c_ptr: int, grad_ptr: int, stream: int = 0) -> None:
+        """gradient(x) with x, c and grad (HH float64) in device memory; c and grad band-summed."""
+        self._actual_unsupported()
+        self._check(_L.lib().ac3d_gradient_dev(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(c_ptr),
+                                               ctypes.c_void_p(grad_ptr), ctypes.c_void_p(stream)))
+
+    @property
+    def n_bands(self) -> int:
+        return len(self._bands)
+
     def pvals_dev(self, frequency, out_ptr: int, listeners_ptr: int | None = None, n_listeners: int = 0,
                   stream: int = 0) -> None:
         """Pressures into device memory (out_ptr: L complex128), receivers optionally in device

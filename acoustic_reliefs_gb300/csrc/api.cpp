@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/ac3d.h"
+#include "context.h"
 #include "internal.h"
 #include "krylov.h"
 #include "listener.h"
@@ -57,7 +58,7 @@ static void upload(DevBuf& d, const std::vector<T>& h, cudaStream_t s) {
   if (!h.empty()) AC3D_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
 }
 
-static double wavenumber(double f) { return 2 * kPiHost * f / 344.0; }  // helpers.h:8, constants.h:13
+double wavenumber(double f) { return 2 * kPiHost * f / 344.0; }  // helpers.h:8, constants.h:13
 
 // get_frequencies (helpers.cpp:67-83)
 static std::vector<double> frequencies(double band, int n) {
@@ -124,64 +125,8 @@ struct GraphCache {
 
 using namespace ac3d;
 
-struct ac3d_ctx {
-  // constructor parameters (DiffBEM, acoustics3d.cpp:22-34)
-  int cluster_size = 64;
-  double radius_factor = 1.5;
-  std::vector<double> bands{1000};
-  int n_freqs = 1;
-  double aca_tol = 1e-3, q_tol = 1e-3, solver_tol = 1e-3;
-  double src[3] = {0, 100, 0};
-  int src_kind = AC3D_INCIDENT_POINT;
-  double listener_radius = 50, listener_ds = 5;
-  bool recompute = false;
-  // extensions
-  int prec = AC3D_PREC_MIXED;
-  int listener_mode = AC3D_LISTENER_DENSE;
-  int maxit = 0;           // 0: twice the number of unknowns
-  double inner_tol = 1e-6; // floor of the relative tolerance of each FP32 inner solve
-  int max_outer = 10;
-  int chunk = 8;           // BiCGSTAB iterations per captured graph launch
-  int maxk = 100;          // APPROX_ACA_MAX_K (constants.h:16)
 
-  cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;                 // concurrent assembly work
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  std::string err;
-  ac3d_stats stats{};
-
-  // mesh
-  bool mesh_set = false, diff_set = false;
-  int V = 0, Ne = 0;
-  std::vector<double> Ps0;  // base positions
-  std::vector<int> Es;      // tree order
-  Partition P;
-  DevPartition DP;
-  DevGeometry G;
-  int64_t sum_mn = 0, worst_pool = 0;
-  int64_t pool_hint[2] = {0, 0};
-  std::vector<double> Ls;   // receivers for value/gradient
-  DevBuf Ls_dev;
-  // differentiable points
-  std::vector<int> diff_pts;
-  std::unordered_map<int, int> Hs;
-  std::vector<int> h_off, pair_elem, pair_corner, pair_touch, touch;
-  DevBuf d_h_off, d_pair_elem, d_pair_corner, d_pair_touch, d_touch;
-
-  // work buffers
-  DevBuf kv, partials, kstate, red, b64, x64, r64, ff_scratch, adj_scratch, tmp_recv;
-  std::unique_ptr<DevHMat> last_H;  // H-matrix of the latest forward solve (matvec timing)
-  bool geom_base = false;           // the device geometry holds Ps0 (no heights applied)
-  KState* h_state = nullptr;  // pinned
-  double* h_red = nullptr;    // pinned
-
-  ~ac3d_ctx() {
-    if (h_state) cudaFreeHost(h_state);
-    if (h_red) cudaFreeHost(h_red);
-  }
-};
-
-namespace {
+namespace ac3d {
 
 void require_mesh(ac3d_ctx* c) {
   if (!c->mesh_set) throw Error(AC3D_ERR_STATE, "No mesh set. Set one using set_mesh or precompute.");
@@ -197,23 +142,23 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
   H->k = k;
   H->maxk = c->maxk;
   const size_t cs = prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
-  H->near.alloc((size_t)std::max<int64_t>(c->P.near_total, 2) * cs, s);
-  AC3D_CUDA(cudaMemsetAsync(H->near.p, 0, (size_t)std::max<int64_t>(c->P.near_total, 2) * cs, s));
-  launch_near_assembly(c->G, c->DP, *H, s);
+  H->near.alloc((size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s);
+  AC3D_CUDA(cudaMemsetAsync(H->near.p, 0, (size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s));
+  launch_near_assembly(c->m->G, c->m->DP, *H, s);
   H->err.alloc(16, s);
   AC3D_CUDA(cudaMemsetAsync(H->err.p, 0, 16, s));
   H->ticket.alloc(16, s);
   AC3D_CUDA(cudaMemsetAsync(H->ticket.p, 0, 16, s));
 
-  const int na = c->DP.na;
+  const int na = c->m->DP.na;
   H->rank.alloc((size_t)std::max(na, 1) * sizeof(int), s);
   H->t_off.alloc((size_t)(na + 1) * sizeof(int), s);
   AC3D_CUDA(cudaMemsetAsync(H->rank.p, 0, (size_t)std::max(na, 1) * sizeof(int), s));
   if (na > 0) {
     H->term_off.alloc((size_t)na * c->maxk * sizeof(long long), s);
     H->pool_used.alloc(16, s);
-    int64_t cap = c->pool_hint[prec];
-    if (cap <= 0) cap = std::min<int64_t>(c->worst_pool, 16 * c->sum_mn);
+    int64_t cap = c->m->pool_hint[prec];
+    if (cap <= 0) cap = std::min<int64_t>(c->m->worst_pool, 16 * c->m->sum_mn);
     cap = std::max<int64_t>(cap, 1024);
     for (int attempt = 0;; attempt++) {
       H->pool.alloc((size_t)cap * cs, s);
@@ -222,7 +167,7 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
       // small blocks (one warp each) run on the side stream, concurrently with the large ones
       AC3D_CUDA(cudaEventRecord(c->ev_fork, s));
       AC3D_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-      launch_aca(c->G, c->DP, *H, c->aca_tol, c->P.max_rows, s, c->side);
+      launch_aca(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, s, c->side);
       AC3D_CUDA(cudaEventRecord(c->ev_join, c->side));
       AC3D_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
       unsigned long long hu[2];
@@ -233,15 +178,15 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
         H->pool_used_host = (int64_t)hu[0];
         break;
       }
-      if (cap >= c->worst_pool || attempt > 8) throw Error(AC3D_ERR_INTERNAL, "ACA pool overflow at worst-case size");
-      cap = std::min<int64_t>(c->worst_pool, std::max<int64_t>(cap * 2, (int64_t)hu[0]));
+      if (cap >= c->m->worst_pool || attempt > 8) throw Error(AC3D_ERR_INTERNAL, "ACA pool overflow at worst-case size");
+      cap = std::min<int64_t>(c->m->worst_pool, std::max<int64_t>(cap * 2, (int64_t)hu[0]));
     }
-    c->pool_hint[prec] = std::min<int64_t>(c->worst_pool, H->pool_used_host + H->pool_used_host / 8 + 4096);
-    const size_t tcap = (size_t)std::max<int64_t>(c->P.aca_term_cap, 1);
+    c->m->pool_hint[prec] = std::min<int64_t>(c->m->worst_pool, H->pool_used_host + H->pool_used_host / 8 + 4096);
+    const size_t tcap = (size_t)std::max<int64_t>(c->m->P.aca_term_cap, 1);
     H->task_cap = (int64_t)tcap;
     H->task_b.alloc(tcap * sizeof(int), s);
     H->task_off.alloc(tcap * sizeof(long long), s);
-    launch_rank_scan(c->DP, *H, s);
+    launch_rank_scan(c->m->DP, *H, s);
     H->tvec.alloc(tcap * (prec == PREC_FP64 ? sizeof(cd) : sizeof(cf)), s);
     H->tvec64.alloc(tcap * sizeof(cd), s);
     H->ranks_host.resize(na);
@@ -252,7 +197,7 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     double sr = 0;
     for (int b = 0; b < na; b++) {
       int r = H->ranks_host[b];
-      const int* q = &c->P.approx[4 * b];
+      const int* q = &c->m->P.approx[4 * b];
       lr += (int64_t)r * ((q[1] - q[0]) + (q[3] - q[2]));
       mx = std::max(mx, r);
       sr += r;
@@ -261,18 +206,18 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     c->stats.lr_entries = lr;
     // per-leaf segments (U by row leaf, V by column leaf), then the pool is released
     int64_t sum_rn = 0, kf = 0, kt = 0;
-    for (int b = 0; b < na; b++) sum_rn += (int64_t)H->ranks_host[b] * (c->P.approx[4 * b + 3] - c->P.approx[4 * b + 2]);
-    const int nleaf = c->DP.nleaf;
+    for (int b = 0; b < na; b++) sum_rn += (int64_t)H->ranks_host[b] * (c->m->P.approx[4 * b + 3] - c->m->P.approx[4 * b + 2]);
+    const int nleaf = c->m->DP.nleaf;
     int64_t segf = 0, segt = 0;
     for (int l = 0; l < nleaf; l++) {
-      const int Rl = c->P.leaf_start[l + 1] - c->P.leaf_start[l];
+      const int Rl = c->m->P.leaf_start[l + 1] - c->m->P.leaf_start[l];
       int K = 0;
-      for (int it = c->P.fw_lr_ptr[l]; it < c->P.fw_lr_ptr[l + 1]; it++) K += H->ranks_host[c->P.fw_lr[it]];
+      for (int it = c->m->P.fw_lr_ptr[l]; it < c->m->P.fw_lr_ptr[l + 1]; it++) K += H->ranks_host[c->m->P.fw_lr[it]];
       K += K & 1;
       kf += K;
       segf += (int64_t)K * Rl;
       K = 0;
-      for (int it = c->P.tr_lr_ptr[l]; it < c->P.tr_lr_ptr[l + 1]; it++) K += H->ranks_host[c->P.tr_lr[it]];
+      for (int it = c->m->P.tr_lr_ptr[l]; it < c->m->P.tr_lr_ptr[l + 1]; it++) K += H->ranks_host[c->m->P.tr_lr[it]];
       K += K & 1;
       kt += K;
       segt += (int64_t)K * Rl;
@@ -285,8 +230,8 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     H->vseg.alloc((size_t)std::max<int64_t>(segt, 2) * cs, s);
     H->uidx.alloc((size_t)std::max<int64_t>(kf, 1) * sizeof(int), s);
     H->vidx.alloc((size_t)std::max<int64_t>(kt, 1) * sizeof(int), s);
-    H->kpos_f.alloc((size_t)std::max<size_t>(c->P.fw_lr.size(), 1) * sizeof(int), s);
-    H->kpos_t.alloc((size_t)std::max<size_t>(c->P.tr_lr.size(), 1) * sizeof(int), s);
+    H->kpos_f.alloc((size_t)std::max<size_t>(c->m->P.fw_lr.size(), 1) * sizeof(int), s);
+    H->kpos_t.alloc((size_t)std::max<size_t>(c->m->P.tr_lr.size(), 1) * sizeof(int), s);
     H->pbuf.alloc((size_t)std::max<int64_t>(std::max(kf, kt), 1) * sizeof(cd), s);
     // leaves by decreasing streamed bytes: row leaves (near + U columns) for the forward gather and
     // the transposed dot, column leaves (V columns; + transposed near) for the forward dot and the
@@ -296,12 +241,12 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
       std::vector<int64_t> wr(nleaf), wc(nleaf);
       std::vector<int> ord(nleaf);
       for (int l = 0; l < nleaf; l++) {
-        const int Rl = c->P.leaf_start[l + 1] - c->P.leaf_start[l];
-        int64_t kr = c->P.didx_ptr[l + 1] - c->P.didx_ptr[l], kc = 0;
-        for (int it = c->P.fw_lr_ptr[l]; it < c->P.fw_lr_ptr[l + 1]; it++) kr += H->ranks_host[c->P.fw_lr[it]];
-        for (int it = c->P.tr_lr_ptr[l]; it < c->P.tr_lr_ptr[l + 1]; it++) kc += H->ranks_host[c->P.tr_lr[it]];
-        for (int it = c->P.tr_near_ptr[l]; it < c->P.tr_near_ptr[l + 1]; it++) {
-          const int* q = &c->P.direct[4 * c->P.tr_near[it]];
+        const int Rl = c->m->P.leaf_start[l + 1] - c->m->P.leaf_start[l];
+        int64_t kr = c->m->P.didx_ptr[l + 1] - c->m->P.didx_ptr[l], kc = 0;
+        for (int it = c->m->P.fw_lr_ptr[l]; it < c->m->P.fw_lr_ptr[l + 1]; it++) kr += H->ranks_host[c->m->P.fw_lr[it]];
+        for (int it = c->m->P.tr_lr_ptr[l]; it < c->m->P.tr_lr_ptr[l + 1]; it++) kc += H->ranks_host[c->m->P.tr_lr[it]];
+        for (int it = c->m->P.tr_near_ptr[l]; it < c->m->P.tr_near_ptr[l + 1]; it++) {
+          const int* q = &c->m->P.direct[4 * c->m->P.tr_near[it]];
           kc += q[1] - q[0];
         }
         wr[l] = kr * Rl;
@@ -315,8 +260,8 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
       upload(H->order_rows, sorted(wr), s);
       upload(H->order_cols, sorted(wc), s);
     }
-    launch_pack(c->DP, *H, false, s);
-    launch_pack(c->DP, *H, true, s);
+    launch_pack(c->m->DP, *H, false, s);
+    launch_pack(c->m->DP, *H, true, s);
     H->pool.release();
     H->term_off.release();
     (void)sum_rn;
@@ -327,23 +272,23 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     H->tvec.alloc(16, s);
     H->tvec64.alloc(16, s);
     for (DevBuf* kb : {&H->kseg_f, &H->kseg_t}) {
-      kb->alloc((size_t)(c->DP.nleaf + 1) * sizeof(int), s);
-      AC3D_CUDA(cudaMemsetAsync(kb->p, 0, (size_t)(c->DP.nleaf + 1) * sizeof(int), s));
+      kb->alloc((size_t)(c->m->DP.nleaf + 1) * sizeof(int), s);
+      AC3D_CUDA(cudaMemsetAsync(kb->p, 0, (size_t)(c->m->DP.nleaf + 1) * sizeof(int), s));
     }
     for (DevBuf* sb : {&H->seg_f, &H->seg_t}) {
-      sb->alloc((size_t)(c->DP.nleaf + 1) * sizeof(long long), s);
-      AC3D_CUDA(cudaMemsetAsync(sb->p, 0, (size_t)(c->DP.nleaf + 1) * sizeof(long long), s));
+      sb->alloc((size_t)(c->m->DP.nleaf + 1) * sizeof(long long), s);
+      AC3D_CUDA(cudaMemsetAsync(sb->p, 0, (size_t)(c->m->DP.nleaf + 1) * sizeof(long long), s));
     }
     H->useg.alloc(32, s);
     H->vseg.alloc(32, s);
     H->uidx.alloc(16, s);
     H->vidx.alloc(16, s);
-    std::vector<int> ord(c->DP.nleaf);
-    for (int l = 0; l < c->DP.nleaf; l++) ord[l] = l;
+    std::vector<int> ord(c->m->DP.nleaf);
+    for (int l = 0; l < c->m->DP.nleaf; l++) ord[l] = l;
     upload(H->order_rows, ord, s);
     upload(H->order_cols, ord, s);
   }
-  c->stats.near_entries = c->P.near_total;
+  c->stats.near_entries = c->m->P.near_total;
   c->stats.hmat_bytes = (long long)H->bytes();
   return H;
 }
@@ -357,10 +302,10 @@ struct SolveCache {
 
 void ensure_work(ac3d_ctx* c) {
   cudaStream_t s = c->stream;
-  const size_t n = (size_t)c->Ne;
+  const size_t n = (size_t)c->m->Ne;
   c->kv.ensure(8 * n * sizeof(cd), s);
-  const int G = krylov_vec_grid(c->Ne);
-  c->partials.ensure((size_t)(c->DP.nleaf + G) * 5 * sizeof(double) + 64, s);
+  const int G = krylov_vec_grid(c->m->Ne);
+  c->partials.ensure((size_t)(c->m->DP.nleaf + G) * 5 * sizeof(double) + 64, s);
   c->kstate.ensure(sizeof(KState), s);
   c->red.ensure(16 * sizeof(double), s);
   c->b64.ensure(n * sizeof(cd), s);
@@ -374,14 +319,14 @@ void ensure_work(ac3d_ctx* c) {
 
 KrylovBufs bufs(ac3d_ctx* c, int vec64) {
   KrylovBufs B;
-  B.n = c->Ne;
+  B.n = c->m->Ne;
   const size_t es = vec64 ? sizeof(cd) : sizeof(cf);
   char* base = (char*)c->kv.p;
   void** slots[8] = {&B.b, &B.x, &B.r, &B.rhat, &B.p, &B.v, &B.s, &B.t};
-  for (int i = 0; i < 8; i++) *slots[i] = base + (size_t)i * c->Ne * es;
+  for (int i = 0; i < 8; i++) *slots[i] = base + (size_t)i * c->m->Ne * es;
   B.partials = c->partials.as<double>();
-  B.nparts_r = krylov_vec_grid(c->Ne);
-  B.nleaf = c->DP.nleaf;
+  B.nparts_r = krylov_vec_grid(c->m->Ne);
+  B.nleaf = c->m->DP.nleaf;
   B.red5 = c->red.as<double>() + 8;
   B.state = c->kstate.as<KState>();
   return B;
@@ -390,13 +335,13 @@ KrylovBufs bufs(ac3d_ctx* c, int vec64) {
 // Runs BiCGSTAB on the prepared buffers (B.b filled). Returns iterations; done flag in *done.
 int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int vec64, double tol, int* done) {
   cudaStream_t s = c->stream;
-  const int maxit = c->maxit > 0 ? c->maxit : 2 * c->Ne;
+  const int maxit = c->maxit > 0 ? c->maxit : 2 * c->m->Ne;
   krylov_enqueue_init(B, vec64, tol, maxit, s);
   // capture one chunk of iterations as a graph and replay it until the state reports completion
   cudaGraph_t graph;
   const long long before = g_kernel_launches.load();
   AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  krylov_enqueue_iterations(B, c->DP, H, tr, vec64, c->chunk, s);
+  krylov_enqueue_iterations(B, c->m->DP, H, tr, vec64, c->chunk, s);
   AC3D_CUDA(cudaStreamEndCapture(s, &graph));
   const long long nodes = g_kernel_launches.load() - before;
   g_kernel_launches.fetch_sub(nodes);  // captured, not launched
@@ -446,8 +391,8 @@ double reduce_norm2_residual(ac3d_ctx* c, const DevHMat& H, bool tr, const cd* b
   cudaStream_t s = c->stream;
   MatvecEpilogue ep;
   ep.partials = c->partials.as<double>();
-  launch_matvec(c->DP, H, c->Ne, tr, 1, x, r, b, ep, s);
-  launch_reduce5(c->partials.as<double>(), c->DP.nleaf, c->red.as<double>(), s);
+  launch_matvec(c->m->DP, H, c->m->Ne, tr, 1, x, r, b, ep, s);
+  launch_reduce5(c->partials.as<double>(), c->m->DP.nleaf, c->red.as<double>(), s);
   AC3D_CUDA(cudaMemcpyAsync(c->h_red, c->red.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
   AC3D_CUDA(cudaStreamSynchronize(s));
   c->stats.matvecs++;
@@ -472,7 +417,7 @@ void solve(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
 void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   cudaStream_t s = c->stream;
   ensure_work(c);
-  const int n = c->Ne;
+  const int n = c->m->Ne;
   const double tol = c->solver_tol;
   int done = 0;
   if (H.prec == PREC_FP64) {
@@ -496,7 +441,13 @@ void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   // mixed precision: FP32 inner BiCGSTAB inside FP64 iterative refinement
   KrylovBufs B = bufs(c, 0);
   launch_zero64(n, x, s);
-  double bn2 = reduce_norm2_residual(c, H, tr, b, x, c->r64.as<cd>());  // r = b - A 0 = b
+  // x = 0: the first residual is b itself
+  launch_copy64(n, b, c->r64.p, s);
+  const int nb = launch_norm2_64(n, b, c->partials.as<double>(), s);
+  launch_reduce5(c->partials.as<double>(), nb, c->red.as<double>(), s);
+  AC3D_CUDA(cudaMemcpyAsync(c->h_red, c->red.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  double bn2 = c->h_red[4];
   double rn2 = bn2;
   int outer = 0;
   while (outer < c->max_outer && rn2 > tol * tol * bn2) {
@@ -518,24 +469,23 @@ void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
 // ------------------------------------------------------------------------------------------
 // Geometry / mesh
 // ------------------------------------------------------------------------------------------
-void upload_points(ac3d_ctx* c, const std::vector<double>& Ps) {
-  cudaStream_t s = c->stream;
-  c->G.P.ensure(Ps.size() * sizeof(double), s);
-  AC3D_CUDA(cudaMemcpyAsync(c->G.P.p, Ps.data(), Ps.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-  launch_geometry(c->G, s);
+void upload_points(MeshState& m, const std::vector<double>& Ps, cudaStream_t s) {
+  m.G.P.ensure(Ps.size() * sizeof(double), s);
+  AC3D_CUDA(cudaMemcpyAsync(m.G.P.p, Ps.data(), Ps.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_geometry(m.G, s);
 }
 
 void ensure_base_geometry(ac3d_ctx* c) {
-  if (!c->geom_base) {
-    upload_points(c, c->Ps0);
-    c->geom_base = true;
+  if (!c->m->geom_base) {
+    upload_points(*c->m, c->m->Ps0, c->stream);
+    c->m->geom_base = true;
   }
 }
 
 std::vector<double> heights_to_points(ac3d_ctx* c, const double* x) {
-  std::vector<double> Ps = c->Ps0;
+  std::vector<double> Ps = c->m->Ps0;
   if (x)
-    for (const auto& kv : c->Hs) Ps[3 * (size_t)kv.first + 1] = x[kv.second] + c->Ps0[3 * (size_t)kv.first + 1];
+    for (const auto& kv : c->Hs) Ps[3 * (size_t)kv.first + 1] = x[kv.second] + c->m->Ps0[3 * (size_t)kv.first + 1];
   return Ps;
 }
 
@@ -561,16 +511,16 @@ std::unique_ptr<ListenerLR> listener_lr(ac3d_ctx* c, double k, const double* Lh,
   auto Q = std::make_unique<ListenerLR>();
   Q->L = L;
   const int maxk = 5000;  // Q_ACA_MAX_K (constants.h:17)
-  Q->iter_lim = std::max(1, std::min(maxk, std::min(L - 1, c->Ne - 1)));
+  Q->iter_lim = std::max(1, std::min(maxk, std::min(L - 1, c->m->Ne - 1)));
   const size_t cs = c->prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
-  const long long cap = (long long)Q->iter_lim * (L + c->Ne);
+  const long long cap = (long long)Q->iter_lim * (L + c->m->Ne);
   Q->pool.alloc((size_t)cap * cs, s);
   Q->toff.alloc((size_t)Q->iter_lim * sizeof(long long), s);
   Q->rank.alloc(sizeof(int), s);
   Q->used.alloc(16, s);
   Q->t.alloc((size_t)Q->iter_lim * sizeof(cd), s);
   AC3D_CUDA(cudaMemsetAsync(Q->used.p, 0, 16, s));
-  upload(Q->blk, std::vector<int>{0, L, 0, c->Ne}, s);
+  upload(Q->blk, std::vector<int>{0, L, 0, c->m->Ne}, s);
   upload(Q->ord, std::vector<int>{0}, s);
   if (c->prec == PREC_FP64) {
     std::vector<double> v(4 * (size_t)L);
@@ -583,20 +533,20 @@ std::unique_ptr<ListenerLR> listener_lr(ac3d_ctx* c, double k, const double* Lh,
       for (int d = 0; d < 3; d++) v[4 * i + d] = (float)Lh[3 * i + d];
     upload(Q->pts, v, s);
   }
-  launch_listener_aca(c->G, c->prec, Q->pts.p, L, k, c->q_tol, maxk, Q->pool.p, cap,
+  launch_listener_aca(c->m->G, c->prec, Q->pts.p, L, k, c->q_tol, maxk, Q->pool.p, cap,
                       Q->used.as<unsigned long long>(), Q->toff.as<long long>(), Q->rank.as<int>(),
                       (int*)(Q->used.as<unsigned long long>() + 1), Q->blk.as<int4>(), Q->ord.as<int>(), s);
   return Q;
 }
 
 void listener_apply(ac3d_ctx* c, const ListenerLR& Q, const cd* in, cd* out, bool trans) {
-  launch_lr_apply(c->prec, Q.pool.p, Q.toff.as<long long>(), Q.rank.as<int>(), Q.iter_lim, Q.L, c->Ne, in,
+  launch_lr_apply(c->prec, Q.pool.p, Q.toff.as<long long>(), Q.rank.as<int>(), Q.iter_lim, Q.L, c->m->Ne, in,
                   trans ? 1 : 0, Q.t.as<cd>(), out, c->stream);
 }
 
 // One frequency: assemble, solve -b, receivers. Keeps H if `keep`.
 std::unique_ptr<DevHMat> forward_one(ac3d_ctx* c, double f, const double4* recv, const double* Lh, int L, cd* x_out,
-                                     cd* y_out, bool keep, std::unique_ptr<ListenerLR>* q_keep = nullptr) {
+                                     cd* y_out, bool keep, std::unique_ptr<ListenerLR>* q_keep) {
   cudaStream_t s = c->stream;
   const double k = wavenumber(f);
   GpuTimer ta(s);
@@ -605,8 +555,8 @@ std::unique_ptr<DevHMat> forward_one(ac3d_ctx* c, double f, const double4* recv,
   ensure_work(c);
   // b = -incident field (the system is (K - I/2) x = -b, adjoint.cpp:95)
   GpuTimer ts(s);
-  launch_rhs(c->G, 1, k, c->src_kind, c->src, c->b64.p, s);
-  launch_negate64(c->Ne, c->b64.p, s);
+  launch_rhs(c->m->G, 1, k, c->src_kind, c->src, c->b64.p, s);
+  launch_negate64(c->m->Ne, c->b64.p, s);
   solve(c, *H, c->b64.as<cd>(), x_out, false);
   c->stats.solves++;
   c->stats.ms_solve += ts.stop();
@@ -617,7 +567,7 @@ std::unique_ptr<DevHMat> forward_one(ac3d_ctx* c, double f, const double4* recv,
       listener_apply(c, *Q, x_out, y_out, false);
       if (q_keep) *q_keep = std::move(Q);
     } else {
-      launch_far_field(c->G, c->prec, recv, L, k, x_out, y_out, c->ff_scratch, s);
+      launch_far_field(c->m->G, c->prec, recv, L, k, x_out, y_out, c->ff_scratch, s);
     }
     c->stats.ms_listener += tl.stop();
   }
@@ -629,7 +579,7 @@ std::unique_ptr<DevHMat> forward_one(ac3d_ctx* c, double f, const double4* recv,
 double band_eval(ac3d_ctx* c, double band, bool forward_only, double* grad_dev) {
   cudaStream_t s = c->stream;
   const int L = (int)c->Ls.size() / 3;
-  const int n = c->Ne;
+  const int n = c->m->Ne;
   auto freqs = frequencies(band, c->n_freqs);
   const int F = (int)freqs.size();
   DevBuf xs, ys, yt, u, coef, vf, adjb, lmb;
@@ -669,7 +619,7 @@ double band_eval(ac3d_ctx* c, double band, bool forward_only, double* grad_dev) 
       if (!Q) Q = listener_lr(c, k, c->Ls.data(), L);  // recompute (adjoint.cpp:177-178)
       listener_apply(c, *Q, vf.as<cd>(), adjb.as<cd>(), true);
     } else {
-      launch_far_field_t(c->G, c->prec, c->Ls_dev.as<double4>(), L, k, vf.as<cd>(), adjb.as<cd>(), s);
+      launch_far_field_t(c->m->G, c->prec, c->Ls_dev.as<double4>(), L, k, vf.as<cd>(), adjb.as<cd>(), s);
     }
     std::unique_ptr<DevHMat> H = std::move(saved[fi]);
     if (!H) H = assemble(c, k, c->prec);  // recompute_matrices (adjoint.cpp:173-195)
@@ -695,7 +645,7 @@ double band_eval(ac3d_ctx* c, double band, bool forward_only, double* grad_dev) 
     a.h_off = c->d_h_off.as<int>();
     a.HH = (int)c->h_off.size() - 1;
     a.grad = grad_dev;
-    launch_adjoint_terms(c->G, a, c->adj_scratch, s);
+    launch_adjoint_terms(c->m->G, a, c->adj_scratch, s);
   }
   AC3D_CUDA(cudaStreamSynchronize(s));
   c->stats.ms_adjoint += tadj.stop();
@@ -704,10 +654,10 @@ double band_eval(ac3d_ctx* c, double band, bool forward_only, double* grad_dev) 
 
 void reset_stats(ac3d_ctx* c) {
   ac3d_stats z{};
-  z.n_elements = c->Ne;
-  z.n_direct = c->DP.nd;
-  z.n_approx = c->DP.na;
-  z.n_leaves = c->DP.nleaf;
+  z.n_elements = c->m->Ne;
+  z.n_direct = c->m->DP.nd;
+  z.n_approx = c->m->DP.na;
+  z.n_leaves = c->m->DP.nleaf;
   z.converged = 1;
   c->stats = z;
 }
@@ -733,7 +683,107 @@ int guard(ac3d_ctx* c, F&& f) {
   }
 }
 
-}  // namespace
+
+// Tree, partition and geometry of a mesh (DiffBEM::set_mesh, acoustics3d.cpp:36-67), built with
+// its device arrays on stream s (synchronised before returning).
+std::shared_ptr<MeshState> build_mesh_state(const double* Ps, int V, const int32_t* Es, int Ne, int cluster_size,
+                                            double radius_factor, int maxk, cudaStream_t s) {
+  for (int i = 0; i < 3 * Ne; i++)
+    if (Es[i] < 0 || Es[i] >= V) {
+      throw Error(AC3D_ERR_ARG, "element index out of range");
+    }
+  for (int i = 0; i < 3 * V; i++)
+    if (!std::isfinite(Ps[i])) {
+      throw Error(AC3D_ERR_ARG, "non-finite vertex coordinate");
+    }
+  auto ms = std::make_shared<MeshState>();
+  MeshState* mp = ms.get();
+  {
+    mp->V = V;
+    mp->Ne = Ne;
+    mp->Ps0.assign(Ps, Ps + 3 * (size_t)V);
+    // centroids in the input order (compute_centers, helpers.cpp:7-14)
+    std::vector<double> C(3 * (size_t)Ne);
+    for (int e = 0; e < Ne; e++)
+      for (int d = 0; d < 3; d++)
+        C[3 * e + d] = (Ps[3 * Es[3 * e] + d] + Ps[3 * Es[3 * e + 1] + d] + Ps[3 * Es[3 * e + 2] + d]) / 3;
+    build_partition(C.data(), Ne, cluster_size, radius_factor, mp->P);
+    if (mp->P.max_leaf > 256) throw Error(AC3D_ERR_ARG, "leaf clusters above 256 elements are not supported");
+    mp->Es.resize(3 * (size_t)Ne);
+    for (int i = 0; i < Ne; i++)
+      for (int d = 0; d < 3; d++) mp->Es[3 * i + d] = Es[3 * mp->P.order[i] + d];
+    build_leaf_lists(mp->P, maxk);
+    // ClusterTree::check (clustertree.cpp:33-47) on the reordered centroids
+    for (int e = 0; e < Ne; e++)
+      for (int d = 0; d < 3; d++)
+        C[3 * e + d] =
+            (Ps[3 * mp->Es[3 * e] + d] + Ps[3 * mp->Es[3 * e + 1] + d] + Ps[3 * mp->Es[3 * e + 2] + d]) / 3;
+    mp->P.tree_ok = true;
+    for (const TreeNode& nd : mp->P.nodes)
+      for (int i = nd.s; i < nd.e; i++) {
+        double dx = C[3 * i] - nd.c[0], dy = C[3 * i + 1] - nd.c[1], dz = C[3 * i + 2] - nd.c[2];
+        if (!(std::sqrt(dx * dx + dy * dy + dz * dz) <= nd.r + 1e-6)) mp->P.tree_ok = false;
+      }
+    // device partition
+    DevPartition& DP = mp->DP;
+    DP.nleaf = (int)mp->P.leaf_start.size() - 1;
+    DP.nd = (int)mp->P.direct.size() / 4;
+    DP.na = (int)mp->P.approx.size() / 4;
+    DP.max_leaf = mp->P.max_leaf;
+    upload(DP.blocks_d, mp->P.direct, s);
+    upload(DP.blocks_a, mp->P.approx, s);
+    upload(DP.leaf_start, mp->P.leaf_start, s);
+    upload(DP.fw_near_ptr, mp->P.fw_near_ptr, s);
+    upload(DP.fw_near, mp->P.fw_near, s);
+    upload(DP.fw_lr_ptr, mp->P.fw_lr_ptr, s);
+    upload(DP.fw_lr, mp->P.fw_lr, s);
+    upload(DP.tr_near_ptr, mp->P.tr_near_ptr, s);
+    upload(DP.tr_near, mp->P.tr_near, s);
+    upload(DP.tr_lr_ptr, mp->P.tr_lr_ptr, s);
+    upload(DP.tr_lr, mp->P.tr_lr, s);
+    std::vector<long long> no(mp->P.near_off.begin(), mp->P.near_off.end());
+    upload(DP.near_off, no, s);
+    {
+      // large blocks first (CTA kernel, by decreasing m + n), then small ones (warp kernel)
+      std::vector<int> big, small;
+      for (int b : mp->P.aca_order) {
+        const int* q = &mp->P.approx[4 * b];
+        ((q[1] - q[0]) <= 64 && (q[3] - q[2]) <= 64 ? small : big).push_back(b);
+      }
+      DP.naca = (int)big.size();
+      big.insert(big.end(), small.begin(), small.end());
+      upload(DP.aca_order, big, s);
+    }
+    upload(DP.near_seg, std::vector<long long>(mp->P.near_seg.begin(), mp->P.near_seg.end()), s);
+    upload(DP.didx_ptr, mp->P.didx_ptr, s);
+    upload(DP.didx, mp->P.didx, s);
+    upload(DP.blk_fw_ptr, mp->P.blk_fw_ptr, s);
+    upload(DP.blk_fw, mp->P.blk_fw, s);
+    upload(DP.blk_tr_ptr, mp->P.blk_tr_ptr, s);
+    upload(DP.blk_tr, mp->P.blk_tr, s);
+    upload(DP.fw_pos, mp->P.fw_pos, s);
+    upload(DP.tr_pos, mp->P.tr_pos, s);
+    mp->sum_mn = 0;
+    mp->worst_pool = 0;
+    for (int b = 0; b < DP.na; b++) {
+      const int* q = &mp->P.approx[4 * b];
+      int m = q[1] - q[0], n = q[3] - q[2];
+      mp->sum_mn += m + n;
+      mp->worst_pool += (int64_t)std::max(0, std::min(maxk, std::min(m - 1, n - 1))) * (m + n);
+    }
+    mp->pool_hint[0] = mp->pool_hint[1] = 0;
+    // geometry
+    mp->G.ne = Ne;
+    mp->G.nv = V;
+    upload(mp->G.E, mp->Es, s);
+    upload_points(*mp, mp->Ps0, s);
+    mp->geom_base = true;
+    AC3D_CUDA(cudaStreamSynchronize(s));
+  }
+  return ms;
+}
+
+}  // namespace ac3d
 
 // ============================================================================================
 // C-ABI
@@ -796,8 +846,7 @@ void ac3d_destroy(ac3d_ctx* c) {
                     &c->adj_scratch, &c->tmp_recv, &c->Ls_dev, &c->d_h_off, &c->d_pair_elem, &c->d_pair_corner,
                     &c->d_pair_touch, &c->d_touch};
   for (DevBuf* b : bufs) b->release();
-  c->DP = DevPartition();
-  c->G = DevGeometry();
+  c->m.reset();  // a mesh shared with other contexts stays alive until its last user goes
   if (c->side) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
@@ -862,103 +911,15 @@ int ac3d_set_listeners(ac3d_ctx* c, const double* Ls, int L) {
 
 int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int Ne, int32_t* Es_out) {
   if (!c || !Ps || !Es || V < 3 || Ne < 1) return AC3D_ERR_ARG;
-  for (int i = 0; i < 3 * Ne; i++)
-    if (Es[i] < 0 || Es[i] >= V) {
-      c->err = "element index out of range";
-      return AC3D_ERR_ARG;
-    }
-  for (int i = 0; i < 3 * V; i++)
-    if (!std::isfinite(Ps[i])) {
-      c->err = "non-finite vertex coordinate";
-      return AC3D_ERR_ARG;
-    }
   return guard(c, [&] {
-    cudaStream_t s = c->stream;
     c->mesh_set = false;
     c->diff_set = false;
-    c->V = V;
-    c->Ne = Ne;
-    c->Ps0.assign(Ps, Ps + 3 * (size_t)V);
-    // centroids in the input order (compute_centers, helpers.cpp:7-14)
-    std::vector<double> C(3 * (size_t)Ne);
-    for (int e = 0; e < Ne; e++)
-      for (int d = 0; d < 3; d++)
-        C[3 * e + d] = (Ps[3 * Es[3 * e] + d] + Ps[3 * Es[3 * e + 1] + d] + Ps[3 * Es[3 * e + 2] + d]) / 3;
-    build_partition(C.data(), Ne, c->cluster_size, c->radius_factor, c->P);
-    if (c->P.max_leaf > 256) throw Error(AC3D_ERR_ARG, "leaf clusters above 256 elements are not supported");
-    c->Es.resize(3 * (size_t)Ne);
-    for (int i = 0; i < Ne; i++)
-      for (int d = 0; d < 3; d++) c->Es[3 * i + d] = Es[3 * c->P.order[i] + d];
-    build_leaf_lists(c->P, c->maxk);
-    // ClusterTree::check (clustertree.cpp:33-47) on the reordered centroids
-    for (int e = 0; e < Ne; e++)
-      for (int d = 0; d < 3; d++)
-        C[3 * e + d] =
-            (Ps[3 * c->Es[3 * e] + d] + Ps[3 * c->Es[3 * e + 1] + d] + Ps[3 * c->Es[3 * e + 2] + d]) / 3;
-    c->P.tree_ok = true;
-    for (const TreeNode& nd : c->P.nodes)
-      for (int i = nd.s; i < nd.e; i++) {
-        double dx = C[3 * i] - nd.c[0], dy = C[3 * i + 1] - nd.c[1], dz = C[3 * i + 2] - nd.c[2];
-        if (!(std::sqrt(dx * dx + dy * dy + dz * dz) <= nd.r + 1e-6)) c->P.tree_ok = false;
-      }
-    // device partition
-    DevPartition& DP = c->DP;
-    DP.nleaf = (int)c->P.leaf_start.size() - 1;
-    DP.nd = (int)c->P.direct.size() / 4;
-    DP.na = (int)c->P.approx.size() / 4;
-    DP.max_leaf = c->P.max_leaf;
-    upload(DP.blocks_d, c->P.direct, s);
-    upload(DP.blocks_a, c->P.approx, s);
-    upload(DP.leaf_start, c->P.leaf_start, s);
-    upload(DP.fw_near_ptr, c->P.fw_near_ptr, s);
-    upload(DP.fw_near, c->P.fw_near, s);
-    upload(DP.fw_lr_ptr, c->P.fw_lr_ptr, s);
-    upload(DP.fw_lr, c->P.fw_lr, s);
-    upload(DP.tr_near_ptr, c->P.tr_near_ptr, s);
-    upload(DP.tr_near, c->P.tr_near, s);
-    upload(DP.tr_lr_ptr, c->P.tr_lr_ptr, s);
-    upload(DP.tr_lr, c->P.tr_lr, s);
-    std::vector<long long> no(c->P.near_off.begin(), c->P.near_off.end());
-    upload(DP.near_off, no, s);
-    {
-      // large blocks first (CTA kernel, by decreasing m + n), then small ones (warp kernel)
-      std::vector<int> big, small;
-      for (int b : c->P.aca_order) {
-        const int* q = &c->P.approx[4 * b];
-        ((q[1] - q[0]) <= 64 && (q[3] - q[2]) <= 64 ? small : big).push_back(b);
-      }
-      DP.naca = (int)big.size();
-      big.insert(big.end(), small.begin(), small.end());
-      upload(DP.aca_order, big, s);
-    }
-    upload(DP.near_seg, std::vector<long long>(c->P.near_seg.begin(), c->P.near_seg.end()), s);
-    upload(DP.didx_ptr, c->P.didx_ptr, s);
-    upload(DP.didx, c->P.didx, s);
-    upload(DP.blk_fw_ptr, c->P.blk_fw_ptr, s);
-    upload(DP.blk_fw, c->P.blk_fw, s);
-    upload(DP.blk_tr_ptr, c->P.blk_tr_ptr, s);
-    upload(DP.blk_tr, c->P.blk_tr, s);
-    upload(DP.fw_pos, c->P.fw_pos, s);
-    upload(DP.tr_pos, c->P.tr_pos, s);
-    c->sum_mn = 0;
-    c->worst_pool = 0;
-    for (int b = 0; b < DP.na; b++) {
-      const int* q = &c->P.approx[4 * b];
-      int m = q[1] - q[0], n = q[3] - q[2];
-      c->sum_mn += m + n;
-      c->worst_pool += (int64_t)std::max(0, std::min(c->maxk, std::min(m - 1, n - 1))) * (m + n);
-    }
-    c->pool_hint[0] = c->pool_hint[1] = 0;
-    // geometry
-    c->G.ne = Ne;
-    c->G.nv = V;
-    upload(c->G.E, c->Es, s);
-    upload_points(c, c->Ps0);
-    c->geom_base = true;
-    AC3D_CUDA(cudaStreamSynchronize(s));
+    std::shared_ptr<MeshState> m = build_mesh_state(Ps, V, Es, Ne, c->cluster_size, c->radius_factor, c->maxk,
+                                                    c->stream);
+    c->m = std::move(m);
     c->mesh_set = true;
     reset_stats(c);
-    if (Es_out) std::memcpy(Es_out, c->Es.data(), c->Es.size() * sizeof(int32_t));
+    if (Es_out) std::memcpy(Es_out, c->m->Es.data(), c->m->Es.size() * sizeof(int32_t));
   });
 }
 
@@ -971,14 +932,14 @@ int ac3d_set_diff_points(ac3d_ctx* c, const int32_t* pts, int HH) {
     c->diff_pts.assign(pts, pts + HH);
     int h = 0;
     for (int i = 0; i < HH; i++) {
-      if (pts[i] < 0 || pts[i] >= c->V) throw Error(AC3D_ERR_ARG, "differentiable point index out of range");
+      if (pts[i] < 0 || pts[i] >= c->m->V) throw Error(AC3D_ERR_ARG, "differentiable point index out of range");
       c->Hs[pts[i]] = h++;  // later duplicates overwrite, as std::unordered_map::operator[] does
     }
     // incidence lists (acoustics3d.cpp:79-98): for each element j, corners 0..2
     std::vector<std::vector<std::pair<int, int>>> lists(HH);
-    for (int j = 0; j < c->Ne; j++)
+    for (int j = 0; j < c->m->Ne; j++)
       for (int o = 0; o < 3; o++) {
-        auto it = c->Hs.find(c->Es[3 * j + o]);
+        auto it = c->Hs.find(c->m->Es[3 * j + o]);
         if (it != c->Hs.end()) lists[it->second].push_back({j, o});
       }
     c->h_off.assign(HH + 1, 0);
@@ -991,7 +952,7 @@ int ac3d_set_diff_points(ac3d_ctx* c, const int32_t* pts, int HH) {
       }
       c->h_off[i + 1] = (int)c->pair_elem.size();
     }
-    std::vector<int> tid(c->Ne, -1);
+    std::vector<int> tid(c->m->Ne, -1);
     c->touch.clear();
     c->pair_touch.resize(c->pair_elem.size());
     for (size_t t = 0; t < c->pair_elem.size(); t++) {
@@ -1040,9 +1001,9 @@ int ac3d_set_points(ac3d_ctx* c, const double* Ps) {
   if (!c || !Ps) return AC3D_ERR_ARG;
   return guard(c, [&] {
     require_mesh(c);
-    c->Ps0.assign(Ps, Ps + 3 * (size_t)c->V);
-    upload_points(c, c->Ps0);
-    c->geom_base = true;
+    c->m->Ps0.assign(Ps, Ps + 3 * (size_t)c->m->V);
+    upload_points(*c->m, c->m->Ps0, c->stream);
+    c->m->geom_base = true;
   });
 }
 
@@ -1115,7 +1076,7 @@ int ac3d_surface_values(ac3d_ctx* c, double f, double* out) {
     ensure_work(c);
     c->last_H.reset();
     c->last_H = forward_one(c, f, nullptr, nullptr, 0, c->x64.as<cd>(), nullptr, true);
-    AC3D_CUDA(cudaMemcpyAsync(out, c->x64.p, (size_t)c->Ne * sizeof(cd), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaMemcpyAsync(out, c->x64.p, (size_t)c->m->Ne * sizeof(cd), cudaMemcpyDeviceToHost, s));
     AC3D_CUDA(cudaStreamSynchronize(s));
     if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
   });
@@ -1146,8 +1107,8 @@ int ac3d_value(ac3d_ctx* c, const double* x, double* cv) {
   return guard(c, [&] {
     require_mesh(c);
     reset_stats(c);
-    upload_points(c, heights_to_points(c, x));
-    c->geom_base = x == nullptr;
+    upload_points(*c->m, heights_to_points(c, x), c->stream);
+    c->m->geom_base = x == nullptr;
     double acc = 0;
     for (double fb : c->bands) acc += band_eval(c, fb, true, nullptr);
     *cv = acc / (double)c->bands.size();
@@ -1162,8 +1123,8 @@ int ac3d_gradient(ac3d_ctx* c, const double* x, double* cv, double* grad) {
       throw Error(AC3D_ERR_STATE, "No differentiable points set. Set them using set_diff_pts or precompute.");
     reset_stats(c);
     cudaStream_t s = c->stream;
-    upload_points(c, heights_to_points(c, x));
-    c->geom_base = false;
+    upload_points(*c->m, heights_to_points(c, x), c->stream);
+    c->m->geom_base = false;
     const int HH = (int)c->h_off.size() - 1;
     DevBuf g;
     g.alloc((size_t)std::max(HH, 1) * sizeof(double), s);
@@ -1194,8 +1155,8 @@ int ac3d_value_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, void* stream
       AC3D_CUDA(cudaStreamSynchronize(s));
     }
     reset_stats(c);
-    upload_points(c, heights_to_points(c, x_dev ? x.data() : nullptr));
-    c->geom_base = x_dev == nullptr;
+    upload_points(*c->m, heights_to_points(c, x_dev ? x.data() : nullptr), c->stream);
+    c->m->geom_base = x_dev == nullptr;
     double acc = 0;
     for (double fb : c->bands) acc += band_eval(c, fb, true, nullptr);
     acc /= (double)c->bands.size();
@@ -1224,8 +1185,8 @@ int ac3d_gradient_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, double* g
     AC3D_CUDA(cudaMemcpyAsync(x.data(), x_dev, HH * sizeof(double), cudaMemcpyDeviceToHost, s));
     AC3D_CUDA(cudaStreamSynchronize(s));
     reset_stats(c);
-    upload_points(c, heights_to_points(c, x.data()));
-    c->geom_base = false;
+    upload_points(*c->m, heights_to_points(c, x.data()), c->stream);
+    c->m->geom_base = false;
     AC3D_CUDA(cudaMemsetAsync(g_dev, 0, (size_t)HH * sizeof(double), s));
     double acc = 0;
     for (double fb : c->bands) acc += band_eval(c, fb, false, g_dev);
@@ -1323,17 +1284,17 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     KrylovBufs B = bufs(c, vec64);
     // x = the last solution rounded to the vector precision, y = scratch
     if (vec64)
-      launch_copy64(c->Ne, c->x64.p, B.p, s);
+      launch_copy64(c->m->Ne, c->x64.p, B.p, s);
     else
-      launch_to32(c->Ne, c->x64.p, B.p, s);
+      launch_to32(c->m->Ne, c->x64.p, B.p, s);
     MatvecEpilogue ep;
-    launch_matvec(c->DP, H, c->Ne, transposed != 0, vec64, B.p, B.v, nullptr, ep, s);  // warm-up
+    launch_matvec(c->m->DP, H, c->m->Ne, transposed != 0, vec64, B.p, B.v, nullptr, ep, s);  // warm-up
     cudaEvent_t e0, e1;
     AC3D_CUDA(cudaEventCreate(&e0));
     AC3D_CUDA(cudaEventCreate(&e1));
     AC3D_CUDA(cudaEventRecord(e0, s));
     for (int i = 0; i < iters; i++)
-      launch_matvec(c->DP, H, c->Ne, transposed != 0, vec64, (i & 1) ? B.v : B.p, (i & 1) ? B.t : B.v, nullptr, ep,
+      launch_matvec(c->m->DP, H, c->m->Ne, transposed != 0, vec64, (i & 1) ? B.v : B.p, (i & 1) ? B.t : B.v, nullptr, ep,
                     s);
     AC3D_CUDA(cudaEventRecord(e1, s));
     AC3D_CUDA(cudaEventSynchronize(e1));
@@ -1343,7 +1304,7 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     cudaEventDestroy(e1);
     *ms = t / iters;
     const long long es = vec64 ? 16 : 8;
-    *bytes = (c->P.near_total + H.lr_entries) * es + 2LL * c->Ne * es;
+    *bytes = (c->m->P.near_total + H.lr_entries) * es + 2LL * c->m->Ne * es;
   });
 }
 

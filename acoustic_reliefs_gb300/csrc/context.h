@@ -1,0 +1,82 @@
+// Host state of one solver context (the C-ABI's ac3d_ctx) and the orchestration steps that the
+// request server (serve.cpp) shares with the single-context entry points (api.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ac3d.h"
+#include "common.cuh"
+#include "internal.h"
+#include "krylov.h"
+
+struct ac3d_ctx {
+  // constructor parameters (DiffBEM, acoustics3d.cpp:22-34)
+  int cluster_size = 64;
+  double radius_factor = 1.5;
+  std::vector<double> bands{1000};
+  int n_freqs = 1;
+  double aca_tol = 1e-3, q_tol = 1e-3, solver_tol = 1e-3;
+  double src[3] = {0, 100, 0};
+  int src_kind = AC3D_INCIDENT_POINT;
+  double listener_radius = 50, listener_ds = 5;
+  bool recompute = false;
+  // extensions
+  int prec = AC3D_PREC_MIXED;
+  int listener_mode = AC3D_LISTENER_DENSE;
+  int maxit = 0;           // 0: twice the number of unknowns
+  double inner_tol = 1e-6; // floor of the relative tolerance of each FP32 inner solve
+  int max_outer = 10;
+  int chunk = 8;           // BiCGSTAB iterations per captured graph launch
+  int maxk = 100;          // APPROX_ACA_MAX_K (constants.h:16)
+
+  cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;                 // concurrent assembly work
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  std::string err;
+  ac3d_stats stats{};
+
+  // mesh (shared with a server's other slots when the context serves requests)
+  bool mesh_set = false, diff_set = false;
+  std::shared_ptr<ac3d::MeshState> m = std::make_shared<ac3d::MeshState>();
+  std::vector<double> Ls;   // receivers for value/gradient
+  ac3d::DevBuf Ls_dev;
+  // differentiable points
+  std::vector<int> diff_pts;
+  std::unordered_map<int, int> Hs;
+  std::vector<int> h_off, pair_elem, pair_corner, pair_touch, touch;
+  ac3d::DevBuf d_h_off, d_pair_elem, d_pair_corner, d_pair_touch, d_touch;
+
+  // work buffers
+  ac3d::DevBuf kv, partials, kstate, red, b64, x64, r64, ff_scratch, adj_scratch, tmp_recv;
+  std::unique_ptr<ac3d::DevHMat> last_H;  // H-matrix of the latest forward solve (matvec timing)
+  ac3d::KState* h_state = nullptr;  // pinned
+  double* h_red = nullptr;    // pinned
+
+  ~ac3d_ctx() {
+    if (h_state) cudaFreeHost(h_state);
+    if (h_red) cudaFreeHost(h_red);
+  }
+};
+
+namespace ac3d {
+
+struct ListenerLR;
+
+double wavenumber(double f);  // k = 2 pi f / c, c = 344 m/s (helpers.h:8, constants.h:13)
+// Tree, partition and geometry of a mesh, device arrays on stream s (synchronised on return).
+std::shared_ptr<MeshState> build_mesh_state(const double* Ps, int V, const int32_t* Es, int Ne, int cluster_size,
+                                            double radius_factor, int maxk, cudaStream_t s);
+void ensure_work(ac3d_ctx* c);
+void reset_stats(ac3d_ctx* c);
+void upload_receivers(ac3d_ctx* c, const double* L, int n, DevBuf& dst);
+// One frequency on the context's mesh: assemble, solve, receivers (x_out: Ne, y_out: L complex
+// FP64 device vectors). Returns the H-matrix if `keep`.
+std::unique_ptr<DevHMat> forward_one(ac3d_ctx* c, double f, const double4* recv, const double* Lh, int L, cd* x_out,
+                                     cd* y_out, bool keep, std::unique_ptr<ListenerLR>* q_keep = nullptr);
+
+}  // namespace ac3d

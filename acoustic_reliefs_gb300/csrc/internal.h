@@ -135,6 +135,25 @@ struct DevGeometry {
   DevBuf eg64;       // ElemGeo<double>
 };
 
+// One mesh: positions, elements in tree order, block partition (host and device) and element
+// geometry. Read-only while solves run on it, so several contexts (a server's slots) share one.
+struct MeshState {
+  int V = 0, Ne = 0;
+  std::vector<double> Ps0;  // base positions (V x 3)
+  std::vector<int> Es;      // elements in tree order (Ne x 3)
+  Partition P;
+  DevPartition DP;
+  DevGeometry G;
+  int64_t sum_mn = 0;      // sum over admissible blocks of m + n
+  int64_t worst_pool = 0;  // ACA pool entries if every block reached its iteration limit
+  std::atomic<int64_t> pool_hint[2];  // per storage precision: pool size the last assembly needed
+  bool geom_base = false;  // G holds Ps0 (no heights applied)
+  MeshState() {
+    pool_hint[0] = 0;
+    pool_hint[1] = 0;
+  }
+};
+
 enum Precision { PREC_MIXED = 0, PREC_FP64 = 1 };
 
 // An assembled H-matrix of (K - I/2) at one wavenumber.

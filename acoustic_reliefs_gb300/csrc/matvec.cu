@@ -13,6 +13,9 @@
 // Both passes stream their segments through shared memory with bulk async copies, so the bytes
 // in flight are set by the copy ring, not by how many loads a warp can issue. No atomics; every
 // sum has a fixed order, so results are bit-reproducible.
+#include <atomic>
+#include <mutex>
+
 #include "common.cuh"
 #include "internal.h"
 #include "segstream.cuh"
@@ -419,14 +422,16 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   }
 }
 
-static int g_sms = 0;
+static std::atomic<int> g_sms{0};
 int device_sm_count() {
-  if (!g_sms) {
+  int n = g_sms.load();
+  if (!n) {
     int dev = 0;
     AC3D_CUDA(cudaGetDevice(&dev));
-    AC3D_CUDA(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev));
+    AC3D_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    g_sms.store(n);
   }
-  return g_sms;
+  return n;
 }
 
 constexpr size_t kRingBytes = (size_t)kStages * kStageBytes;
@@ -450,12 +455,13 @@ static void set_smem_attrs() {
 }
 
 void prepare_matvec_kernels() {
-  static bool done = false;  // once per process (one device per process)
-  if (done) return;
-  set_smem_attrs<float, float, float>();
-  set_smem_attrs<float, double, double>();
-  set_smem_attrs<double, double, double>();
-  done = true;
+  // once per process (one device per process); contexts on other threads wait for the first call
+  static std::once_flag once;
+  std::call_once(once, [] {
+    set_smem_attrs<float, float, float>();
+    set_smem_attrs<float, double, double>();
+    set_smem_attrs<double, double, double>();
+  });
 }
 
 template <typename MT, typename VT, typename AT, int RPL>

@@ -39,6 +39,90 @@ WORKLOAD = ("0.6 m relief, 64x64 smoothed seeded heightmap, 20480 triangles, 2 k
             "181 receivers on a 5 m semicircle, leaf 32, eta 2, ACA 1e-4, BiCGSTAB 1e-6")
 
 
+SWEEP_BANDS = (125, 160, 200, 250, 315, 400, 500, 630, 800, 1000, 1250, 1600, 2000, 2500, 3150, 4000)
+SWEEP_WORKLOAD = ("served sweep: 0.6 m reliefs (30x7x30 box, subdiv_top {subdivs}: {sizes} triangles), seeded "
+                  "smoothed 64x64 heightmap, 3 frequencies per third-octave band 125 Hz - 4 kHz (48 per relief), "
+                  "normal plane wave, 181 receivers on a 5 m semicircle, leaf 32, eta 2, ACA 1e-4, BiCGSTAB 1e-6")
+
+
+def band_frequencies(band: float, n: int = 3):
+    """n log-spaced frequencies over +-1/6 octave around a band centre (get_frequencies,
+    helpers.cpp:67-83)."""
+    bw = 2.0 ** (1.0 / 6.0)
+    return list(np.exp(np.linspace(np.log(band / bw), np.log(band * bw), n)))
+
+
+def sweep_workload(seed: int, subdivs):
+    from acoustic_reliefs_gb300 import meshes
+    hm = meshes.smooth_heightmap(64, seed)
+    reliefs = [meshes.relief(0.6, 0.6, 0.05, 30, 7, 30, s, hm) for s in subdivs]
+    freqs = [f for b in SWEEP_BANDS for f in band_frequencies(b)]
+    reqs = [(m, f) for m in range(len(reliefs)) for f in freqs]
+    order = np.random.default_rng(seed).permutation(len(reqs))
+    return reliefs, [reqs[i] for i in order]
+
+
+def run_served(precision, reliefs, reqs, Ls, slots, rate, seed):
+    """Submits the requests with Poisson arrivals at `rate` per second (all at once if rate is None)
+    to a server with `slots` slots; returns (solves/s over the makespan, latencies ms, results)."""
+    import threading
+    from acoustic_reliefs_gb300.serve import Server
+    with Server(slots=slots, precision=precision) as srv:
+        ids = [srv.add_mesh(R.Ps, R.Es, LEAF, FACTOR, ACA_TOL, SOLVER_TOL)[0] for R in reliefs]
+        # one untimed request per mesh (kernel set-up, allocator warm-up, footprint estimates)
+        for mid in ids:
+            srv.wait(srv.submit(mid, 1000.0, Ls, ("plane", DIRECTION)))
+        gaps = (np.random.default_rng(seed + 1).exponential(1.0 / rate, size=len(reqs)) if rate
+                else np.zeros(len(reqs)))
+        handles = [None] * len(reqs)
+        t_sub = [0.0] * len(reqs)
+
+        def feeder():
+            t_next = time.perf_counter()
+            for i, (m, f) in enumerate(reqs):
+                t_next += gaps[i]
+                dt = t_next - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                t_sub[i] = time.perf_counter()
+                handles[i] = srv.submit(ids[m], f, Ls, ("plane", DIRECTION))
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        res = [srv.wait(h) for h in handles]
+    done = [t_sub[i] + res[i][1]["latency_ms"] / 1e3 for i in range(len(reqs))]
+    makespan = max(done) - min(t_sub)
+    lat = [r[1]["latency_ms"] for r in res]
+    return len(reqs) / makespan, lat, res
+
+
+def served_sweep(args, Ls):
+    subdivs = tuple(int(x) for x in args.sweep_subdivs.split(","))
+    reliefs, reqs = sweep_workload(0, subdivs)
+    out = {"workload": SWEEP_WORKLOAD.format(subdivs="/".join(map(str, subdivs)),
+                                             sizes="/".join(str(len(R.Es)) for R in reliefs)),
+           "requests": len(reqs), "slots": args.slots}
+    thr, lat_sat, res_m = run_served("mixed", reliefs, reqs, Ls, args.slots, None, 0)
+    out["mixed"] = {"solves_per_s": thr, "offered": "all requests at t=0 (saturated)",
+                    "p50_ms_saturated": float(np.percentile(lat_sat, 50)),
+                    "p99_ms_saturated": float(np.percentile(lat_sat, 99))}
+    rate = 0.5 * thr
+    thr_l, lat_l, _ = run_served("mixed", reliefs, reqs, Ls, args.slots, rate, 0)
+    out["mixed"].update({"poisson_rate_per_s": rate, "solves_per_s_at_rate": thr_l,
+                         "p50_ms": float(np.percentile(lat_l, 50)), "p99_ms": float(np.percentile(lat_l, 99))})
+    if not args.no_fp64_sweep:
+        thr64, lat64, res_d = run_served("fp64", reliefs, reqs, Ls, args.slots, None, 0)
+        err = max(float(np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0])) for a, b in zip(res_m, res_d))
+        out["fp64"] = {"solves_per_s": thr64, "offered": "all requests at t=0 (saturated)",
+                       "p50_ms_saturated": float(np.percentile(lat64, 50)),
+                       "p99_ms_saturated": float(np.percentile(lat64, 99))}
+        out["speedup_mixed_over_fp64"] = thr / thr64
+        out["max_pressure_rel_err_mixed_vs_fp64"] = err
+    out["max_rel_residual"] = max(r[1]["rel_residual"] for r in res_m)
+    return out
+
+
 def workload(seed: int = 0):
     from acoustic_reliefs_gb300 import meshes
     R = meshes.relief_20k(seed)
@@ -304,6 +388,8 @@ def run_gpu(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if args.sweep_subdivs and world == 1:
+        line["served_sweep"] = served_sweep(args, Ls)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -316,6 +402,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--inner-tol", type=float, default=1e-6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep-subdivs", default="0,1,2",
+                    help="subdiv_top levels of the served sweep ('' to skip; 3 adds the 118680-triangle relief)")
+    ap.add_argument("--slots", type=int, default=4, help="server slots (concurrent requests) of the served sweep")
+    ap.add_argument("--no-fp64-sweep", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

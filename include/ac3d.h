@@ -158,6 +158,63 @@ void ac3d_partition_free(ac3d_partition* p);
 /* Library version string. */
 const char* ac3d_version(void);
 
+/* ---------------------------------------------------------------------------------------------
+ * Request server. No reference counterpart: the reference solves one frequency at a time inside
+ * DiffBEM (bem3d::gradient's frequency loop, adjoint.cpp:46-104). A server keeps registered
+ * meshes (tree, partition, geometry) on the device and runs `slots` solver contexts, each on its
+ * own CUDA stream and host thread, so the kernels of up to `slots` requests overlap on the GPU.
+ * A queued request is admitted when a slot is free and its estimated device footprint fits in
+ * what the admitted requests leave of the byte budget (first in, first out; a request that does
+ * not fit may be overtaken by later ones that do, at most AC3D_SERVE_MAX_BYPASS times). Each
+ * request's result does not depend on what runs beside it: every sum has a fixed order.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct ac3d_server ac3d_server;
+
+#define AC3D_REQ_QUEUED 0
+#define AC3D_REQ_RUNNING 1
+#define AC3D_REQ_DONE 2
+#define AC3D_REQ_FAILED 3
+#define AC3D_SERVE_MAX_BYPASS 8
+
+typedef struct ac3d_request_info {
+  int status;                  /* AC3D_OK or the error code of the request */
+  int slot;                    /* slot that ran it */
+  double queue_ms;             /* submit -> admitted */
+  double run_ms;               /* admitted -> result on the host */
+  double latency_ms;           /* submit -> result on the host */
+  long long footprint_bytes;   /* admission estimate */
+  long long hmat_bytes;        /* device bytes of the assembled H-matrix */
+  long long lr_entries, near_entries;
+  int iterations, outer_steps; /* BiCGSTAB iterations; refinement steps */
+  double rel_residual;         /* final FP64 |b - A x| / |b| */
+  double ms_assemble, ms_solve, ms_listener; /* device time of the phases */
+} ac3d_request_info;
+
+/* precision: AC3D_PREC_*; hbm_budget_bytes <= 0 takes 85% of the device memory free at creation. */
+int ac3d_server_create(ac3d_server** out, int slots, int precision, long long hbm_budget_bytes);
+/* Waits for every submitted request, then releases the slots, meshes and streams. */
+void ac3d_server_destroy(ac3d_server* srv);
+const char* ac3d_server_last_error(const ac3d_server* srv);
+/* Registers a mesh (set_mesh semantics: Es_out, if given, receives the tree-ordered connectivity
+ * the results refer to) with its H-matrix and solver parameters. */
+int ac3d_server_add_mesh(ac3d_server* srv, const double* Ps, int V, const int32_t* Es, int Ne, int cluster_size,
+                         double radius_factor, double aca_tol, double solver_tol, int32_t* Es_out, int* mesh_id);
+/* Queues a forward solve at `frequency` with incident field `incident_kind` / `incident_vec`
+ * (AC3D_INCIDENT_*) and pressures at the L receivers Ls (L x 3, copied). Fails with
+ * AC3D_ERR_RESOURCE if the request's footprint estimate exceeds the whole budget. */
+int ac3d_server_submit(ac3d_server* srv, int mesh_id, double frequency, int incident_kind, const double* incident_vec,
+                       const double* Ls, int L, long long* request);
+/* state: AC3D_REQ_* */
+int ac3d_server_poll(ac3d_server* srv, long long request, int* state);
+/* Blocks until the request finishes, copies its L complex pressures (2L doubles) into out and its
+ * record into info (either may be NULL), and forgets the request. Returns the request's status. */
+int ac3d_server_wait(ac3d_server* srv, long long request, double* out, ac3d_request_info* info);
+/* Admission rule of the server as a pure function (no GPU): given the footprints of the queued
+ * requests in arrival order, how often each was overtaken, the budget and the bytes in use,
+ * returns the queue index to admit next, or -1 if none may start now. */
+int ac3d_admit_next(const long long* footprints, const int* bypassed, int n_queued, long long budget,
+                    long long in_use, int n_running);
+
 #ifdef __cplusplus
 }
 #endif
