@@ -138,12 +138,24 @@ __device__ __forceinline__ void init_ring(uint64_t* full) {
   __syncthreads();
 }
 
+// Lanes per column and rows per lane of the dot pass for leaves of up to 32 RPL rows: a group of G
+// lanes shares one column, lane g summing rows g, g + G, g + 2G, ..., so one warp instruction
+// covers 32 / G columns and the cross-lane sum takes log2(G) shuffle levels.
+template <int RPL>
+struct DotShape {
+  static constexpr int G = RPL <= 2 ? 8 : RPL == 4 ? 16 : 32;
+  static constexpr int RPG = 32 * RPL / G;
+};
+
 // Dot pass: p[kptr[leaf] + k] = sum_rows S[k][row] x[leaf rows] for every column k of the leaf's
 // low-rank segment (region B).
 template <typename MT, typename VT, typename AT, int RPL>
 __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
                                                            const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ p,
                                                            const int* __restrict__ done) {
+  constexpr int G = DotShape<RPL>::G, RPG = DotShape<RPL>::RPG;
+  constexpr int CPW = 32 / G;             // columns per warp step
+  constexpr int STEP = kWarps * CPW;      // columns per CTA step
   extern __shared__ __align__(128) unsigned char dsmem[];
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
@@ -153,35 +165,37 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
   const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
   if (K == 0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  AT xr[RPL], xi[RPL];
+  const int g = lane % G, slot = lane / G;
+  AT xr[RPG], xi[RPG];
 #pragma unroll
-  for (int j = 0; j < RPL; j++) {
-    const int row = lane + 32 * j;
+  for (int t = 0; t < RPG; t++) {
+    const int row = g + G * t;
     cplx<VT> v = row < R ? x[ls + row] : cplx<VT>();
-    xr[j] = (AT)v.re;
-    xi[j] = (AT)v.im;
+    xr[t] = (AT)v.re;
+    xi[t] = (AT)v.im;
   }
   init_ring(full);
   cplx<AT>* out = p + k0;
   stream_leaf<MT>(stage, full, R, nullptr, 0, lrseg + V.b_seg[leaf], K, V.err,
                   [&](const cplx<MT>* S, int, int c0, int ncols, int, int, int) {
-                    // four columns per warp at a time: four independent shuffle reductions
-                    for (int j0 = warp; j0 < ncols; j0 += 4 * kWarps) {
-                      AT a[8];
+                    // two columns per lane in flight: j and j + STEP
+                    for (int jb = warp * CPW; jb < ncols; jb += 2 * STEP) {
+                      AT a[4];
 #pragma unroll
-                      for (int u = 0; u < 4; u++) {
-                        const int j = j0 + u * kWarps;
+                      for (int u = 0; u < 2; u++) {
+                        const int j = jb + slot + u * STEP;
                         AT ar = 0, ai = 0;
                         if (j < ncols) {
+                          const cplx<MT>* col = S + j * R;
 #pragma unroll
-                          for (int jr = 0; jr < RPL; jr++) {
-                            const int row = lane + 32 * jr;
+                          for (int t = 0; t < RPG; t++) {
+                            const int row = g + G * t;
                             if (row < R) {
-                              const cplx<MT> sv = S[j * R + row];
-                              ar = fma((AT)sv.re, xr[jr], ar);
-                              ar = fma(-(AT)sv.im, xi[jr], ar);
-                              ai = fma((AT)sv.re, xi[jr], ai);
-                              ai = fma((AT)sv.im, xr[jr], ai);
+                              const cplx<MT> sv = col[row];
+                              ar = fma((AT)sv.re, xr[t], ar);
+                              ar = fma(-(AT)sv.im, xi[t], ar);
+                              ai = fma((AT)sv.re, xi[t], ai);
+                              ai = fma((AT)sv.im, xr[t], ai);
                             }
                           }
                         }
@@ -189,19 +203,13 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
                         a[2 * u + 1] = ai;
                       }
 #pragma unroll
-                      for (int o = 16; o > 0; o >>= 1)
+                      for (int o = G / 2; o > 0; o >>= 1)
 #pragma unroll
-                        for (int u = 0; u < 8; u++) a[u] += __shfl_xor_sync(0xffffffffu, a[u], o);
-                      if (lane < 4) {
-                        const int j = j0 + lane * kWarps;
-                        AT vr = a[0], vi = a[1];
-#pragma unroll
-                        for (int u = 1; u < 4; u++)
-                          if (lane == u) {
-                            vr = a[2 * u];
-                            vi = a[2 * u + 1];
-                          }
-                        if (j < ncols) out[c0 + j] = cplx<AT>(vr, vi);
+                        for (int u = 0; u < 4; u++) a[u] += __shfl_xor_sync(0xffffffffu, a[u], o);
+                      if (g == 0) {
+                        const int j = jb + slot;
+                        if (j < ncols) out[c0 + j] = cplx<AT>(a[0], a[1]);
+                        if (j + STEP < ncols) out[c0 + j + STEP] = cplx<AT>(a[2], a[3]);
                       }
                     }
                   });
@@ -247,90 +255,186 @@ __global__ void __launch_bounds__(256) seg_reduce_kernel(const int* __restrict__
 
 // Gather pass: y[leaf rows] = -x/2 + S_A x[a_idx] + S_B t[b_idx] (+ transposed dense blocks), or
 // b - that; optional fused FP64 dot partials (conj(a).y, conj(y).b, |y|^2) per leaf.
+//
+// The segments stream through the copy ring in chunks of at most kThreads columns. Together with
+// each chunk's bulk copy, every thread gathers one column multiplier (x[idx] or t[idx]) into the
+// stage's multiplier buffer with cp.async; the stage's mbarrier expects the bulk copy's bytes plus
+// one arrival per thread, so a stage is ready only when its columns and multipliers have both
+// landed, kStages chunks after they were requested. The column index for the next refill is
+// loaded one chunk ahead. The compute uses the dot pass's layout: G lanes per column, each lane
+// summing RPG rows, 32 / G columns per warp step; the column slots of a warp are summed at the end.
 template <typename MT, typename VT, typename AT, bool TRANS, int RPL>
 __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
     SegView V, const cplx<MT>* __restrict__ near, const cplx<MT>* __restrict__ lrseg, const cplx<AT>* __restrict__ t,
     const cplx<VT>* __restrict__ x, cplx<VT>* __restrict__ y, const cplx<VT>* __restrict__ bminus,
     const cplx<VT>* __restrict__ dot_a, const cplx<VT>* __restrict__ dot_b, double* partials,
     double* red5, unsigned* ticket, const int* __restrict__ done) {
+  static_assert(sizeof(cplx<VT>) == sizeof(cplx<AT>), "multipliers are copied as raw elements");
+  constexpr int G = DotShape<RPL>::G, RPG = DotShape<RPL>::RPG;
+  constexpr int CPW = 32 / G;         // columns per warp step
+  constexpr int STEP = kWarps * CPW;  // columns per CTA step
   extern __shared__ __align__(128) unsigned char dsmem[];
   __shared__ bool s_last;
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ __align__(16) unsigned char zraw[kStages * kThreads * sizeof(cplx<AT>)];
+  auto zbuf = reinterpret_cast<cplx<AT>(*)[kThreads]>(zraw);
   __shared__ double sdot[kWarps][5];
   if (done && *done) return;
   const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  AT ar[RPL], ai[RPL];
-#pragma unroll
-  for (int j = 0; j < RPL; j++) ar[j] = ai[j] = 0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane % G, slot = lane / G;
 
   const int a_cols = TRANS ? 0 : V.a_kptr[leaf + 1] - V.a_kptr[leaf];
   const int* a_idx = TRANS ? nullptr : V.a_idx + V.a_kptr[leaf];
   const int b_cols = V.b_kptr[leaf + 1] - V.b_kptr[leaf];
   const int* b_idx = V.b_idx + V.b_kptr[leaf];
-  // multiplier of column jb + 8 lane of a chunk: x[idx] (near region) or t[idx] (low-rank region)
-  auto fetch = [&](int region, int c0, int ncols, int jb, AT& zr, AT& zim) {
-    zr = 0;
-    zim = 0;
-    const int jl = jb + kWarps * lane;
-    if (jl < ncols) {
-      const int zi = (region == 0 ? a_idx : b_idx)[c0 + jl];
-      if (zi >= 0) {  // -1: padding column
-        if (region == 0) {
-          const cplx<VT> z = x[zi];
-          zr = (AT)z.re;
-          zim = (AT)z.im;
-        } else {
-          const cplx<AT> z = t[zi];
-          zr = z.re;
-          zim = z.im;
+  const cplx<MT>* a_ptr = TRANS ? nullptr : near + V.a_seg[leaf];
+  const cplx<MT>* b_ptr = lrseg + V.b_seg[leaf];
+  // columns per chunk: even (16-byte aligned chunks), at most one multiplier per thread
+  const int cpc = min(kThreads, max(2, (int)(kStageBytes / sizeof(cplx<MT>)) / R & ~1));
+  const int na = (a_cols + cpc - 1) / cpc, nb = (b_cols + cpc - 1) / cpc;
+  const int nch = na + nb;
+  struct Chunk {
+    const cplx<MT>* src;
+    const int* idx;
+    const cplx<AT>* z;  // multiplier source
+    int ncols;
+  };
+  auto chunk = [&](int c) {
+    Chunk k;
+    if (c < na) {
+      const int c0 = c * cpc;
+      k.ncols = min(cpc, a_cols - c0);
+      k.src = a_ptr + (long long)c0 * R;
+      k.idx = a_idx + c0;
+      k.z = reinterpret_cast<const cplx<AT>*>(x);
+    } else {
+      const int c0 = (c - na) * cpc;
+      k.ncols = min(cpc, b_cols - c0);
+      k.src = b_ptr + (long long)c0 * R;
+      k.idx = b_idx + c0;
+      k.z = t;
+    }
+    return k;
+  };
+  // this thread's column index in chunk c (-1: none or padding)
+  auto col_index = [&](int c) { 
+    if (c >= nch) return -1;
+    const Chunk k = chunk(c);
+    return tid < k.ncols ? k.idx[tid] : -1;
+  };
+  // issue this thread's part of chunk c into stage s: multiplier gather, then its arrival
+  auto issue = [&](int c, int s, int zi) {
+    const Chunk k = chunk(c);
+    if (tid < k.ncols) {
+      if (zi >= 0)
+        cp_async_elem<sizeof(cplx<AT>)>(&zbuf[s][tid], k.z + zi);
+      else
+        zbuf[s][tid] = cplx<AT>();
+    }
+    cp_async_arrive_noinc(&full[s]);
+    if (tid == 0) {
+      const uint32_t bytes = (uint32_t)(k.ncols * R * sizeof(cplx<MT>));
+      mbar_expect_tx(&full[s], bytes);
+      bulk_copy_g2s(stage[s], k.src, bytes, &full[s]);
+    }
+  };
+
+  if (tid == 0) {
+    for (int st = 0; st < kStages; st++) mbar_init(&full[st], 1 + kThreads);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  {
+    int zi[kStages];
+#pragma unroll
+    for (int c = 0; c < kStages; c++) zi[c] = col_index(c);
+#pragma unroll
+    for (int c = 0; c < kStages; c++)
+      if (c < nch) issue(c, c, zi[c]);
+  }
+  int next_zi = col_index(kStages);  // column index of the next refill, loaded one chunk ahead
+
+  AT ar[RPG], ai[RPG];
+#pragma unroll
+  for (int q = 0; q < RPG; q++) ar[q] = ai[q] = 0;
+  bool ok = true;
+  int c = 0;
+  for (; c < nch; c++) {
+    const int s = c % kStages;
+    const bool got = mbar_wait_bounded(&full[s], (uint32_t)(c / kStages) & 1u);
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    const int ncols = chunk(c).ncols;
+    const cplx<MT>* S = (const cplx<MT>*)stage[s];
+    const cplx<AT>* Z = zbuf[s];
+    for (int jb = warp * CPW; jb < ncols; jb += 2 * STEP) {
+#pragma unroll
+      for (int u = 0; u < 2; u++) {
+        const int j = jb + slot + u * STEP;
+        if (j < ncols) {
+          const cplx<AT> z = Z[j];
+          const cplx<MT>* col = S + j * R;
+#pragma unroll
+          for (int q = 0; q < RPG; q++) {
+            const int row = g + G * q;
+            if (row < R) {
+              const cplx<MT> sv = col[row];
+              ar[q] = fma((AT)sv.re, z.re, ar[q]);
+              ar[q] = fma(-(AT)sv.im, z.im, ar[q]);
+              ai[q] = fma((AT)sv.re, z.im, ai[q]);
+              ai[q] = fma((AT)sv.im, z.re, ai[q]);
+            }
+          }
         }
       }
     }
-  };
-  init_ring(full);
-  AT nzr = 0, nzi = 0;  // prefetched multipliers of the first batch of the next chunk
-  bool have_next = false;
-  stream_leaf<MT>(stage, full, R, TRANS ? nullptr : near + V.a_seg[leaf], a_cols, lrseg + V.b_seg[leaf], b_cols,
-                  V.err, [&](const cplx<MT>* S, int region, int c0, int ncols, int nreg, int nc0, int nnc) {
-                    for (int jb = warp; jb < ncols; jb += 32 * kWarps) {
-                      AT zr, zim;
-                      if (jb == warp && have_next) {
-                        zr = nzr;
-                        zim = nzi;
-                      } else {
-                        fetch(region, c0, ncols, jb, zr, zim);
-                      }
-                      if (jb + 32 * kWarps >= ncols) {  // last batch: prefetch the next chunk's first
-                        have_next = nnc > 0;
-                        if (have_next) fetch(nreg, nc0, nnc, warp, nzr, nzi);
-                      }
-                      const int nl = min(32, (ncols - jb + kWarps - 1) / kWarps);
-                      for (int l = 0; l < nl; l++) {
-                        const AT br = __shfl_sync(0xffffffffu, zr, l), bi = __shfl_sync(0xffffffffu, zim, l);
-                        const int j = jb + kWarps * l;
+    __syncthreads();  // stage s and its multipliers are consumed
+    if (c + kStages < nch) {
+      fence_proxy_async();
+      const int zi = next_zi;
+      next_zi = col_index(c + kStages + 1);
+      issue(c + kStages, s, zi);
+    }
+  }
+  if (!ok) {
+    // record the failure and let the copies already issued land before the CTA exits
+    if (tid == 0) {
+      atomicExch(V.err, 1);
+      for (int cc = c; cc < min(nch, c + kStages); cc++)
+        mbar_wait_bounded(&full[cc % kStages], (uint32_t)(cc / kStages) & 1u);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  // sum the column slots of the warp: lanes with equal g hold the same rows
 #pragma unroll
-                        for (int jr = 0; jr < RPL; jr++) {
-                          const int row = lane + 32 * jr;
-                          if (row < R) {
-                            const cplx<MT> sv = S[j * R + row];
-                            ar[jr] = fma((AT)sv.re, br, ar[jr]);
-                            ar[jr] = fma(-(AT)sv.im, bi, ar[jr]);
-                            ai[jr] = fma((AT)sv.re, bi, ai[jr]);
-                            ai[jr] = fma((AT)sv.im, br, ai[jr]);
-                          }
-                        }
-                      }
-                    }
-                    if (warp >= ncols) {  // a warp with no column here still prefetches for the next
-                      have_next = nnc > 0;
-                      if (have_next) fetch(nreg, nc0, nnc, warp, nzr, nzi);
-                    }
-                  });
+  for (int o = G; o < 32; o <<= 1)
+#pragma unroll
+    for (int q = 0; q < RPG; q++) {
+      ar[q] += __shfl_xor_sync(0xffffffffu, ar[q], o);
+      ai[q] += __shfl_xor_sync(0xffffffffu, ai[q], o);
+    }
+  // per-warp row sums in the ring memory (all stages are consumed), then the transposed dense
+  // blocks below this column leaf, read column-wise (lane = column of the leaf)
+  cplx<AT>* part = (cplx<AT>*)stage;
+  __syncthreads();
+  if (slot == 0) {
+#pragma unroll
+    for (int q = 0; q < RPG; q++) {
+      const int row = g + G * q;
+      if (row < R) part[warp * R + row] = cplx<AT>(ar[q], ai[q]);
+    }
+  }
+  __syncwarp();
   if (TRANS) {
-    // dense blocks below this column leaf, read column-wise (lane = column of the leaf)
+    AT tr[RPL], ti[RPL];
+#pragma unroll
+    for (int jr = 0; jr < RPL; jr++) tr[jr] = ti[jr] = 0;
     for (int it = V.trn_ptr[leaf] + warp; it < V.trn_ptr[leaf + 1]; it += kWarps) {
       const int b = V.trn[it];
       const int4 blk = V.blocks_d[b];
@@ -341,22 +445,22 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
         const int col = lane + 32 * jr;
         if (col < R) {
           const cplx<MT>* Dc = near + V.near_off[b] + (long long)col * m;
-          for (int r = 0; r < m; r++) cmac<AT>(ar[jr], ai[jr], Dc[r], xs[r]);
+          for (int r = 0; r < m; r++) cmac<AT>(tr[jr], ti[jr], Dc[r], xs[r]);
         }
       }
     }
-  }
-  // combine the warps in fixed order (reusing the ring memory) and apply -x/2
-  cplx<AT>* part = (cplx<AT>*)stage;
-  __syncthreads();
 #pragma unroll
-  for (int jr = 0; jr < RPL; jr++) {
-    const int row = lane + 32 * jr;
-    if (row < R) part[warp * R + row] = cplx<AT>(ar[jr], ai[jr]);
+    for (int jr = 0; jr < RPL; jr++) {
+      const int col = lane + 32 * jr;
+      if (col < R) {
+        cplx<AT>& pc = part[warp * R + col];
+        pc = cplx<AT>(pc.re + tr[jr], pc.im + ti[jr]);
+      }
+    }
   }
   __syncthreads();
   double d[5] = {0, 0, 0, 0, 0};
-  for (int r = threadIdx.x; r < R; r += kThreads) {
+  for (int r = tid; r < R; r += kThreads) {
     AT sr = 0, si = 0;
     for (int w = 0; w < kWarps; w++) {
       sr += part[w * R + r].re;
@@ -390,33 +494,33 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
     if (lane == 0)
       for (int i = 0; i < 5; i++) sdot[warp][i] = d[i];
     __syncthreads();
-    if (threadIdx.x < 5) {
-      double s = 0;
-      for (int w = 0; w < kWarps; w++) s += sdot[w][threadIdx.x];
-      partials[(size_t)leaf * 5 + threadIdx.x] = s;
+    if (tid < 5) {
+      double sum = 0;
+      for (int w = 0; w < kWarps; w++) sum += sdot[w][tid];
+      partials[(size_t)leaf * 5 + tid] = sum;
     }
     if (red5) {
       // the last CTA to finish reduces all leaves' partials in fixed order into red5
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+      if (tid == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
       __syncthreads();
       if (s_last) {
         __threadfence();
         double acc[5] = {0, 0, 0, 0, 0};
-        for (int l = threadIdx.x; l < (int)gridDim.x; l += kThreads)
+        for (int l = tid; l < (int)gridDim.x; l += kThreads)
           for (int i = 0; i < 5; i++) acc[i] += __ldcg(&partials[(size_t)l * 5 + i]);
         for (int i = 0; i < 5; i++) acc[i] = warp_sum(acc[i]);
         __syncthreads();
         if (lane == 0)
           for (int i = 0; i < 5; i++) sdot[warp][i] = acc[i];
         __syncthreads();
-        if (threadIdx.x < 5) {
+        if (tid < 5) {
           double sum = 0;
-          for (int w = 0; w < kWarps; w++) sum += sdot[w][threadIdx.x];
-          red5[threadIdx.x] = sum;
+          for (int w = 0; w < kWarps; w++) sum += sdot[w][tid];
+          red5[tid] = sum;
         }
-        if (threadIdx.x == 0) *ticket = 0u;
+        if (tid == 0) *ticket = 0u;
       }
     }
   }
@@ -440,6 +544,13 @@ template <typename MT, typename VT, typename AT, int RPL>
 static void set_smem_attrs_rpl() {
   AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, VT, AT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kRingBytes));
+  // the largest shared-memory carveout, so that four CTAs of the ring size fit on an SM
+  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, VT, AT, RPL>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 100));
+  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, false, RPL>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, true, RPL>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, false, RPL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
   AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, true, RPL>,

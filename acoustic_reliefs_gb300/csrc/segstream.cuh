@@ -53,6 +53,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Per-thread asynchronous gather of one 8- or 16-byte element into shared memory (src aligned to
+// its size). Completion is reported to an mbarrier by cp_async_arrive_noinc.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
+  static_assert(BYTES == 8 || BYTES == 16, "8 or 16 bytes");
+  if constexpr (BYTES == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+// One arrival on the mbarrier once every cp.async this thread issued before has landed (the
+// arrival counts against the barrier's expected count: no increment).
+__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Bounded wait on a phase of an mbarrier; false if it did not complete within kSpinLimit polls.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
   for (uint32_t i = 0; i < kSpinLimit; i++)
