@@ -143,6 +143,7 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
   H->maxk = c->maxk;
   const size_t cs = prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
   H->near.alloc((size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s);
+  if (prec != PREC_FP64) H->xdf.alloc((size_t)c->m->Ne * sizeof(cd), s);
   AC3D_CUDA(cudaMemsetAsync(H->near.p, 0, (size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s));
   launch_near_assembly(c->m->G, c->m->DP, *H, s);
   H->err.alloc(16, s);
@@ -726,6 +727,7 @@ std::shared_ptr<MeshState> build_mesh_state(const double* Ps, int V, const int32
       }
     // device partition
     DevPartition& DP = mp->DP;
+    DP.ne = Ne;
     DP.nleaf = (int)mp->P.leaf_start.size() - 1;
     DP.nd = (int)mp->P.direct.size() / 4;
     DP.na = (int)mp->P.approx.size() / 4;

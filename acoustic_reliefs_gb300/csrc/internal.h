@@ -109,6 +109,7 @@ void build_leaf_lists(Partition& P, int maxk);
 // Device views
 // ------------------------------------------------------------------------------------------
 struct DevPartition {
+  int ne = 0;  // elements
   int nleaf = 0, nd = 0, na = 0;
   int naca = 0;  // admissible blocks for the CTA ACA kernel (aca_order[0, naca)); the rest are
                  // small (m, n <= 64) and run one per warp
@@ -180,7 +181,8 @@ struct DevHMat {
   DevBuf ticket;          // unsigned: gather-pass completion ticket (zero between launches)
   int64_t task_cap = 0;   // upper bound of the number of stored terms
   DevBuf tvec;            // intermediate V x per term (complex, vector precision)
-  DevBuf tvec64;          // FP64 intermediate for refinement residuals
+  DevBuf tvec64;          // FP64 / double-float intermediate for refinement residuals
+  DevBuf xdf;             // double-float copy of the residual matvec input (FP32 storage only)
   DevBuf pool_used;       // unsigned long long
   int64_t pool_cap = 0;
   int64_t pool_used_host = 0;
@@ -189,7 +191,7 @@ struct DevHMat {
   size_t bytes() const {
     return near.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
            tvec.bytes + tvec64.bytes + useg.bytes + vseg.bytes + uidx.bytes + vidx.bytes + kpos_f.bytes +
-           kpos_t.bytes + pbuf.bytes + kseg_f.bytes + kseg_t.bytes + seg_f.bytes + seg_t.bytes;
+           kpos_t.bytes + pbuf.bytes + kseg_f.bytes + kseg_t.bytes + seg_f.bytes + seg_t.bytes + xdf.bytes;
   }
 };
 

@@ -15,6 +15,7 @@
 // sum has a fixed order, so results are bit-reproducible.
 #include <atomic>
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 #include "internal.h"
@@ -27,12 +28,73 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 }  // namespace
 
-template <typename AT, typename A, typename X>
-__device__ __forceinline__ void cmac(AT& ar, AT& ai, const A& a, const X& x) {
-  ar = fma((AT)a.re, (AT)x.re, ar);
-  ar = fma(-(AT)a.im, (AT)x.im, ar);
-  ai = fma((AT)a.re, (AT)x.im, ai);
-  ai = fma((AT)a.im, (AT)x.re, ai);
+// Double-float: the unevaluated sum hi + lo of two FP32 numbers, about 48 significant bits, used
+// for the FP64-vector residual of iterative refinement so that it runs on the FP32 pipes (GB300's
+// FP64 rate is a small fraction of its FP32 rate). Error-free transformations: two_sum (Knuth),
+// two_prod by FMA (the double-double arithmetic of Dekker 1971, Hida-Li-Bailey 2001). The _rn
+// intrinsics keep the compiler from contracting the exact splits into FMAs.
+struct df32 {
+  float hi, lo;
+  __host__ __device__ df32(float h = 0.f, float l = 0.f) : hi(h), lo(l) {}
+};
+
+__device__ __forceinline__ df32 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return df32(s, e);
+}
+__device__ __forceinline__ df32 df_fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return df32(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df32 df_add(df32 x, df32 y) {
+  const df32 s = df_two_sum(x.hi, y.hi);
+  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+// acc + a z for a float a: the product's rounding error and a z.lo go to the low word, which is
+// renormalised when accumulators are combined (df_add).
+__device__ __forceinline__ void df_mac(df32& acc, float a, df32 z) {
+  const float p = __fmul_rn(a, z.hi);
+  const float pe = __fmaf_rn(a, z.lo, __fmaf_rn(a, z.hi, -p));
+  const df32 s = df_two_sum(acc.hi, p);
+  acc = df32(s.hi, __fadd_rn(acc.lo, __fadd_rn(s.lo, pe)));
+}
+
+// Accumulator arithmetic of the matvec passes: plain FP32 / FP64, or double-float.
+template <typename AT, typename MT>
+__device__ __forceinline__ void acc_mac(AT& ar, AT& ai, const cplx<MT>& a, const AT& zr, const AT& zi) {
+  ar = fma((AT)a.re, zr, ar);
+  ar = fma(-(AT)a.im, zi, ar);
+  ai = fma((AT)a.re, zi, ai);
+  ai = fma((AT)a.im, zr, ai);
+}
+__device__ __forceinline__ void acc_mac(df32& ar, df32& ai, const cplx<float>& a, const df32& zr, const df32& zi) {
+  df_mac(ar, a.re, zr);
+  df_mac(ar, -a.im, zi);
+  df_mac(ai, a.re, zi);
+  df_mac(ai, a.im, zr);
+}
+template <typename AT>
+__device__ __forceinline__ AT acc_add(AT a, AT b) { return a + b; }
+__device__ __forceinline__ df32 acc_add(df32 a, df32 b) { return df_add(a, b); }
+template <typename AT>
+__device__ __forceinline__ AT acc_shfl_xor(AT v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ df32 acc_shfl_xor(df32 v, int o) {
+  return df32(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+template <typename VT, typename AT>
+__device__ __forceinline__ VT acc_to(AT v) { return (VT)v; }
+template <>
+__device__ __forceinline__ double acc_to<double, df32>(df32 v) { return (double)v.hi + (double)v.lo; }
+
+// x (FP64) -> double-float multipliers
+__global__ void to_df_kernel(int n, const cd* __restrict__ x, cplx<df32>* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cd v = x[i];
+  const float rh = __double2float_rn(v.re), ih = __double2float_rn(v.im);
+  out[i] = cplx<df32>(df32(rh, __double2float_rn(v.re - (double)rh)), df32(ih, __double2float_rn(v.im - (double)ih)));
 }
 
 struct SegView {
@@ -149,9 +211,9 @@ struct DotShape {
 
 // Dot pass: p[kptr[leaf] + k] = sum_rows S[k][row] x[leaf rows] for every column k of the leaf's
 // low-rank segment (region B).
-template <typename MT, typename VT, typename AT, int RPL>
+template <typename MT, typename AT, int RPL>
 __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const cplx<MT>* __restrict__ lrseg,
-                                                           const cplx<VT>* __restrict__ x, cplx<AT>* __restrict__ p,
+                                                           const cplx<AT>* __restrict__ xm, cplx<AT>* __restrict__ p,
                                                            const int* __restrict__ done) {
   constexpr int G = DotShape<RPL>::G, RPG = DotShape<RPL>::RPG;
   constexpr int CPW = 32 / G;             // columns per warp step
@@ -170,9 +232,9 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
 #pragma unroll
   for (int t = 0; t < RPG; t++) {
     const int row = g + G * t;
-    cplx<VT> v = row < R ? x[ls + row] : cplx<VT>();
-    xr[t] = (AT)v.re;
-    xi[t] = (AT)v.im;
+    const cplx<AT> v = row < R ? xm[ls + row] : cplx<AT>();
+    xr[t] = v.re;
+    xi[t] = v.im;
   }
   init_ring(full);
   cplx<AT>* out = p + k0;
@@ -190,13 +252,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
 #pragma unroll
                           for (int t = 0; t < RPG; t++) {
                             const int row = g + G * t;
-                            if (row < R) {
-                              const cplx<MT> sv = col[row];
-                              ar = fma((AT)sv.re, xr[t], ar);
-                              ar = fma(-(AT)sv.im, xi[t], ar);
-                              ai = fma((AT)sv.re, xi[t], ai);
-                              ai = fma((AT)sv.im, xr[t], ai);
-                            }
+                            if (row < R) acc_mac(ar, ai, col[row], xr[t], xi[t]);
                           }
                         }
                         a[2 * u] = ar;
@@ -205,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
 #pragma unroll
                       for (int o = G / 2; o > 0; o >>= 1)
 #pragma unroll
-                        for (int u = 0; u < 4; u++) a[u] += __shfl_xor_sync(0xffffffffu, a[u], o);
+                        for (int u = 0; u < 4; u++) a[u] = acc_add(a[u], acc_shfl_xor(a[u], o));
                       if (g == 0) {
                         const int j = jb + slot;
                         if (j < ncols) out[c0 + j] = cplx<AT>(a[0], a[1]);
@@ -236,19 +292,19 @@ __global__ void __launch_bounds__(256) seg_reduce_kernel(const int* __restrict__
   for (; e + 3 < e1; e += 4) {
     const int k0 = kpos[e], k1 = kpos[e + 1], k2 = kpos[e + 2], k3 = kpos[e + 3];
     const cplx<AT> v0 = p[k0 + q], v1 = p[k1 + q], v2 = p[k2 + q], v3 = p[k3 + q];
-    sr += v0.re;
-    si += v0.im;
-    sr += v1.re;
-    si += v1.im;
-    sr += v2.re;
-    si += v2.im;
-    sr += v3.re;
-    si += v3.im;
+    sr = acc_add(sr, v0.re);
+    si = acc_add(si, v0.im);
+    sr = acc_add(sr, v1.re);
+    si = acc_add(si, v1.im);
+    sr = acc_add(sr, v2.re);
+    si = acc_add(si, v2.im);
+    sr = acc_add(sr, v3.re);
+    si = acc_add(si, v3.im);
   }
   for (; e < e1; e++) {
     const cplx<AT> v = p[kpos[e] + q];
-    sr += v.re;
-    si += v.im;
+    sr = acc_add(sr, v.re);
+    si = acc_add(si, v.im);
   }
   t[i] = cplx<AT>(sr, si);
 }
@@ -266,10 +322,10 @@ __global__ void __launch_bounds__(256) seg_reduce_kernel(const int* __restrict__
 template <typename MT, typename VT, typename AT, bool TRANS, int RPL>
 __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
     SegView V, const cplx<MT>* __restrict__ near, const cplx<MT>* __restrict__ lrseg, const cplx<AT>* __restrict__ t,
-    const cplx<VT>* __restrict__ x, cplx<VT>* __restrict__ y, const cplx<VT>* __restrict__ bminus,
+    const cplx<VT>* __restrict__ x, const cplx<AT>* __restrict__ xm, cplx<VT>* __restrict__ y,
+    const cplx<VT>* __restrict__ bminus,
     const cplx<VT>* __restrict__ dot_a, const cplx<VT>* __restrict__ dot_b, double* partials,
     double* red5, unsigned* ticket, const int* __restrict__ done) {
-  static_assert(sizeof(cplx<VT>) == sizeof(cplx<AT>), "multipliers are copied as raw elements");
   constexpr int G = DotShape<RPL>::G, RPG = DotShape<RPL>::RPG;
   constexpr int CPW = 32 / G;         // columns per warp step
   constexpr int STEP = kWarps * CPW;  // columns per CTA step
@@ -309,7 +365,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
       k.ncols = min(cpc, a_cols - c0);
       k.src = a_ptr + (long long)c0 * R;
       k.idx = a_idx + c0;
-      k.z = reinterpret_cast<const cplx<AT>*>(x);
+      k.z = xm;
     } else {
       const int c0 = (c - na) * cpc;
       k.ncols = min(cpc, b_cols - c0);
@@ -382,13 +438,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
 #pragma unroll
           for (int q = 0; q < RPG; q++) {
             const int row = g + G * q;
-            if (row < R) {
-              const cplx<MT> sv = col[row];
-              ar[q] = fma((AT)sv.re, z.re, ar[q]);
-              ar[q] = fma(-(AT)sv.im, z.im, ar[q]);
-              ai[q] = fma((AT)sv.re, z.im, ai[q]);
-              ai[q] = fma((AT)sv.im, z.re, ai[q]);
-            }
+            if (row < R) acc_mac(ar[q], ai[q], col[row], z.re, z.im);
           }
         }
       }
@@ -416,8 +466,8 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   for (int o = G; o < 32; o <<= 1)
 #pragma unroll
     for (int q = 0; q < RPG; q++) {
-      ar[q] += __shfl_xor_sync(0xffffffffu, ar[q], o);
-      ai[q] += __shfl_xor_sync(0xffffffffu, ai[q], o);
+      ar[q] = acc_add(ar[q], acc_shfl_xor(ar[q], o));
+      ai[q] = acc_add(ai[q], acc_shfl_xor(ai[q], o));
     }
   // per-warp row sums in the ring memory (all stages are consumed), then the transposed dense
   // blocks below this column leaf, read column-wise (lane = column of the leaf)
@@ -439,13 +489,16 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
       const int b = V.trn[it];
       const int4 blk = V.blocks_d[b];
       const int m = blk.y - blk.x;
-      const cplx<VT>* xs = x + blk.x;
+      const cplx<AT>* xs = xm + blk.x;
 #pragma unroll
       for (int jr = 0; jr < RPL; jr++) {
         const int col = lane + 32 * jr;
         if (col < R) {
           const cplx<MT>* Dc = near + V.near_off[b] + (long long)col * m;
-          for (int r = 0; r < m; r++) cmac<AT>(tr[jr], ti[jr], Dc[r], xs[r]);
+          for (int r = 0; r < m; r++) {
+            const cplx<AT> z = xs[r];
+            acc_mac(tr[jr], ti[jr], Dc[r], z.re, z.im);
+          }
         }
       }
     }
@@ -454,7 +507,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
       const int col = lane + 32 * jr;
       if (col < R) {
         cplx<AT>& pc = part[warp * R + col];
-        pc = cplx<AT>(pc.re + tr[jr], pc.im + ti[jr]);
+        pc = cplx<AT>(acc_add(pc.re, tr[jr]), acc_add(pc.im, ti[jr]));
       }
     }
   }
@@ -463,18 +516,18 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   for (int r = tid; r < R; r += kThreads) {
     AT sr = 0, si = 0;
     for (int w = 0; w < kWarps; w++) {
-      sr += part[w * R + r].re;
-      si += part[w * R + r].im;
+      sr = acc_add(sr, part[w * R + r].re);
+      si = acc_add(si, part[w * R + r].im);
     }
     const cplx<VT> xv = x[ls + r];
-    AT yr = sr - AT(0.5) * (AT)xv.re;
-    AT yi = si - AT(0.5) * (AT)xv.im;
+    VT yr = acc_to<VT>(sr) - VT(0.5) * xv.re;
+    VT yi = acc_to<VT>(si) - VT(0.5) * xv.im;
     if (bminus) {
       const cplx<VT> bv = bminus[ls + r];
-      yr = (AT)bv.re - yr;
-      yi = (AT)bv.im - yi;
+      yr = bv.re - yr;
+      yi = bv.im - yi;
     }
-    const cplx<VT> o((VT)yr, (VT)yi);
+    const cplx<VT> o(yr, yi);
     y[ls + r] = o;
     const double oyr = (double)o.re, oyi = (double)o.im;
     if (dot_a) {  // conj(a) . y
@@ -542,10 +595,10 @@ constexpr size_t kRingBytes = (size_t)kStages * kStageBytes;
 
 template <typename MT, typename VT, typename AT, int RPL>
 static void set_smem_attrs_rpl() {
-  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, VT, AT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, AT, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kRingBytes));
   // the largest shared-memory carveout, so that four CTAs of the ring size fit on an SM
-  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, VT, AT, RPL>, cudaFuncAttributePreferredSharedMemoryCarveout,
+  AC3D_CUDA(cudaFuncSetAttribute(seg_dot_kernel<MT, AT, RPL>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  100));
   AC3D_CUDA(cudaFuncSetAttribute(seg_gather_kernel<MT, VT, AT, false, RPL>,
                                  cudaFuncAttributePreferredSharedMemoryCarveout, 100));
@@ -570,7 +623,7 @@ void prepare_matvec_kernels() {
   static std::once_flag once;
   std::call_once(once, [] {
     set_smem_attrs<float, float, float>();
-    set_smem_attrs<float, double, double>();
+    set_smem_attrs<float, double, df32>();
     set_smem_attrs<double, double, double>();
   });
 }
@@ -592,6 +645,14 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
   const cplx<MT>* vseg = H.vseg.as<cplx<MT>>();
   cplx<AT>* t = (cplx<AT>*)tvec;
   cplx<AT>* p = H.pbuf.as<cplx<AT>>();
+  // column multipliers taken from x, in the accumulator type
+  const cplx<AT>* xm = (const cplx<AT>*)x;
+  if constexpr (std::is_same<AT, df32>::value) {
+    note_launch();
+    to_df_kernel<<<(DP.ne + 255) / 256, 256, 0, s>>>(DP.ne, (const cd*)x, H.xdf.as<cplx<df32>>());
+    AC3D_CUDA(cudaGetLastError());
+    xm = H.xdf.as<cplx<df32>>();
+  }
   if (DP.na > 0) {
     // dot pass over the segments on the input side: V by column leaf (forward), U by row leaf
     SegView d = v;
@@ -599,8 +660,7 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
     d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
     d.order = tr ? H.order_rows.as<int>() : H.order_cols.as<int>();
     note_launch();
-    seg_dot_kernel<MT, VT, AT, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, (const cplx<VT>*)x,
-                                                                            p, done);
+    seg_dot_kernel<MT, AT, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, xm, p, done);
     AC3D_CUDA(cudaGetLastError());
     note_launch();
     seg_reduce_kernel<AT><<<(int)((H.task_cap + 255) / 256), 256, 0, s>>>(
@@ -616,11 +676,11 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
   note_launch();
   if (tr)
     seg_gather_kernel<MT, VT, AT, true, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
-        v, H.near.as<cplx<MT>>(), vseg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
+        v, H.near.as<cplx<MT>>(), vseg, t, (const cplx<VT>*)x, xm, (cplx<VT>*)y, (const cplx<VT>*)bminus,
         (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
   else
     seg_gather_kernel<MT, VT, AT, false, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
-        v, H.near.as<cplx<MT>>(), useg, t, (const cplx<VT>*)x, (cplx<VT>*)y, (const cplx<VT>*)bminus,
+        v, H.near.as<cplx<MT>>(), useg, t, (const cplx<VT>*)x, xm, (cplx<VT>*)y, (const cplx<VT>*)bminus,
         (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
   AC3D_CUDA(cudaGetLastError());
 }
@@ -645,7 +705,8 @@ void launch_matvec_ex(const DevPartition& DP, const DevHMat& H, bool transposed,
     if (!vec64) throw Error(3, "internal: FP64 H-matrix needs FP64 vectors");
     mv_rpl<double, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
   } else if (vec64) {
-    mv_rpl<float, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
+    // FP32 H-matrix with FP64 vectors (refinement residuals): double-float arithmetic
+    mv_rpl<float, double, df32>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
   } else {
     mv_rpl<float, float, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s);
   }
