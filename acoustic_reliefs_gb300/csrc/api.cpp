@@ -746,15 +746,21 @@ std::shared_ptr<MeshState> build_mesh_state(const double* Ps, int V, const int32
     std::vector<long long> no(mp->P.near_off.begin(), mp->P.near_off.end());
     upload(DP.near_off, no, s);
     {
-      // large blocks first (CTA kernel, by decreasing m + n), then small ones (warp kernel)
-      std::vector<int> big, small;
+      // blocks for the CTA kernel first, then the warp kernels by largest side (256, 128, 64), each
+      // group by decreasing m + n (longest first)
+      std::vector<int> grp[4];
       for (int b : mp->P.aca_order) {
         const int* q = &mp->P.approx[4 * b];
-        ((q[1] - q[0]) <= 64 && (q[3] - q[2]) <= 64 ? small : big).push_back(b);
+        const int side = std::max(q[1] - q[0], q[3] - q[2]);
+        const int g = (side > kWarpAcaMaxDim || maxk > kWarpAcaTerms) ? 0 : side > 128 ? 1 : side > 64 ? 2 : 3;
+        grp[g].push_back(b);
       }
-      DP.naca = (int)big.size();
-      big.insert(big.end(), small.begin(), small.end());
-      upload(DP.aca_order, big, s);
+      std::vector<int> all;
+      for (int g = 0; g < 4; g++) {
+        DP.aca_split[g] = (int)grp[g].size();
+        all.insert(all.end(), grp[g].begin(), grp[g].end());
+      }
+      upload(DP.aca_order, all, s);
     }
     upload(DP.near_seg, std::vector<long long>(mp->P.near_seg.begin(), mp->P.near_seg.end()), s);
     upload(DP.didx_ptr, mp->P.didx_ptr, s);

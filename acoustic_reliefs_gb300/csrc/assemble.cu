@@ -282,12 +282,13 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Warp-per-block ACA for small blocks (m, n <= 64): the same sequence as aca_kernel (pivot rules,
-// stop rule, dropped converging term, zero terms not stored, exactly-zero blocks skipped) with
-// warp shuffles in place of block barriers. Each lane owns rows / columns l and l + 32.
+// Warp-per-block ACA for blocks of at most 32 LPL rows and columns: the same sequence as
+// aca_kernel (pivot rules, stop rule, dropped converging term, zero terms not stored, exactly-zero
+// blocks skipped) with warp shuffles in place of block barriers. Lane l owns rows and columns
+// l + 32 k (k < LPL) and keeps the current term's u and v there in registers; the earlier terms
+// are read from the pool four at a time. Norms and cross terms are summed in the storage type R
+// (the FP64 path is unchanged); the error estimate is accumulated in FP64.
 // ------------------------------------------------------------------------------------------
-constexpr int kWarpAcaMax = 64;
-
 template <typename R>
 __device__ __forceinline__ void warp_argmax(R& val, int& idx) {
 #pragma unroll
@@ -301,22 +302,44 @@ __device__ __forceinline__ void warp_argmax(R& val, int& idx) {
   }
 }
 
-template <typename R, typename P4>
-__global__ void __launch_bounds__(256) aca_warp_kernel(AcaArgs<R, P4> A, int nblocks) {
-  __shared__ cplx<R> s_uq[8][kWarpAcaMax];
-  __shared__ cplx<R> s_vq[8][kWarpAcaMax];
-  __shared__ long long s_toff[8][kWarpAcaMax];
+template <typename R>
+__device__ __forceinline__ R warp_sum_r(R v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// acc -= sum_{p < nst} coef[p] * pool[toff[p] + off]: loads issued four at a time
+template <typename R>
+__device__ __forceinline__ void sub_terms(cplx<R>& acc, const cplx<R>* coef, const cplx<R>* __restrict__ pool,
+                                          const long long* toff, long long off, int nst) {
+  int p = 0;
+  for (; p + 4 <= nst; p += 4) {
+    const cplx<R> a0 = pool[toff[p] + off], a1 = pool[toff[p + 1] + off];
+    const cplx<R> a2 = pool[toff[p + 2] + off], a3 = pool[toff[p + 3] + off];
+    cfms(acc, coef[p], a0);
+    cfms(acc, coef[p + 1], a1);
+    cfms(acc, coef[p + 2], a2);
+    cfms(acc, coef[p + 3], a3);
+  }
+  for (; p < nst; p++) cfms(acc, coef[p], pool[toff[p] + off]);
+}
+
+template <typename R, typename P4, int LPL>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) aca_warp_kernel(AcaArgs<R, P4> A, int nblocks) {
+  __shared__ __align__(16) unsigned char s_raw[8 * kWarpAcaTerms * (2 * sizeof(cplx<R>) + sizeof(long long))];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int bi = blockIdx.x * 8 + warp;
   if (bi >= nblocks) return;
+  cplx<R>* uq = reinterpret_cast<cplx<R>*>(s_raw) + warp * kWarpAcaTerms;
+  cplx<R>* vq = reinterpret_cast<cplx<R>*>(s_raw) + (8 + warp) * kWarpAcaTerms;
+  long long* toff = reinterpret_cast<long long*>(s_raw + 16 * kWarpAcaTerms * sizeof(cplx<R>)) + warp * kWarpAcaTerms;
   const int b = A.order[bi];
   const int4 q = A.blocks[b];
   const int rs = q.x, cs = q.z, m = q.y - q.x, n = q.w - q.z;
   int iter_lim = min(A.maxk, min(m - 1, n - 1));
   if (iter_lim < 0) iter_lim = 0;
-  cplx<R>* uq = s_uq[warp];
-  cplx<R>* vq = s_vq[warp];
-  long long* toff = s_toff[warp];
+  if (iter_lim > kWarpAcaTerms) iter_lim = kWarpAcaTerms;  // the host routes only blocks that fit
 
   if (A.zero_guard && iter_lim > 0) {  // exactly-zero block (see aca_kernel)
     bool zero = false;
@@ -341,11 +364,12 @@ __global__ void __launch_bounds__(256) aca_warp_kernel(AcaArgs<R, P4> A, int nbl
     }
   }
 
-  unsigned long long used = 1ull;  // row 0
+  unsigned used_l = lane == 0 ? 1u : 0u;  // bit k: row lane + 32 k is used (row 0 first)
   double err = 0;
   int i = 0, iter = 0, nst = 0;
   bool need_alloc = true;
   long long base = 0;
+  cplx<R> u_l[LPL], v_l[LPL];
   while (iter < iter_lim) {
     if (need_alloc) {
       unsigned long long bb = 0;
@@ -369,70 +393,92 @@ __global__ void __launch_bounds__(256) aca_warp_kernel(AcaArgs<R, P4> A, int nbl
     const P4 pi = A.rowpts[rs + i];
     R best = R(-1);
     int bidx = 0;
-    for (int c = lane; c < n; c += 32) {
-      cplx<R> v = entry_far<R>(A.k, A.G, pi, cs + c);
-      for (int p = 0; p < nst; p++) cfms(v, uq[p], A.pool[toff[p] + m + c]);
-      vnew[c] = v;
-      const R a = abs2(v);
-      if (a > best) {
-        best = a;
-        bidx = c;
+#pragma unroll
+    for (int k = 0; k < LPL; k++) {
+      const int c = lane + 32 * k;
+      if (c < n) {
+        cplx<R> v = entry_far<R>(A.k, A.G, pi, cs + c);
+        sub_terms(v, uq, A.pool, toff, (long long)m + c, nst);
+        v_l[k] = v;
+        const R a = abs2(v);
+        if (a > best) {
+          best = a;
+          bidx = c;
+        }
       }
     }
     warp_argmax<R>(best, bidx);
     const int j = bidx;
-    __syncwarp();
-    const cplx<R> vj = vnew[j];
+    cplx<R> mine = v_l[0];
+#pragma unroll
+    for (int k = 1; k < LPL; k++)
+      if (k == (j >> 5)) mine = v_l[k];
+    const cplx<R> vj(__shfl_sync(0xffffffffu, mine.re, j & 31), __shfl_sync(0xffffffffu, mine.im, j & 31));
     for (int p = lane; p < nst; p += 32) vq[p] = A.pool[toff[p] + m + j];
     __syncwarp();
     const bool keep = A.zero_guard && vj.re == R(0) && vj.im == R(0);
-    double vn = 0;
-    for (int c = lane; c < n; c += 32) {
-      cplx<R> v = vnew[c];
-      if (!keep) v = cdiv(v, vj);
-      vnew[c] = v;
-      vn += (double)v.re * (double)v.re + (double)v.im * (double)v.im;
+    R vn = 0;
+#pragma unroll
+    for (int k = 0; k < LPL; k++) {
+      const int c = lane + 32 * k;
+      if (c < n) {
+        cplx<R> v = v_l[k];
+        if (!keep) v = cdiv(v, vj);
+        v_l[k] = v;
+        vnew[c] = v;
+        vn += abs2(v);
+      }
     }
     // column residual
-    double un = 0;
-    for (int r = lane; r < m; r += 32) {
-      cplx<R> u = entry_far<R>(A.k, A.G, A.rowpts[rs + r], cs + j);
-      for (int p = 0; p < nst; p++) cfms(u, A.pool[toff[p] + r], vq[p]);
-      unew[r] = u;
-      un += (double)u.re * (double)u.re + (double)u.im * (double)u.im;
+    R un = 0;
+#pragma unroll
+    for (int k = 0; k < LPL; k++) {
+      const int r = lane + 32 * k;
+      if (r < m) {
+        cplx<R> u = entry_far<R>(A.k, A.G, A.rowpts[rs + r], cs + j);
+        sub_terms(u, vq, A.pool, toff, (long long)r, nst);
+        u_l[k] = u;
+        unew[r] = u;
+        un += abs2(u);
+      }
     }
-    __syncwarp();
-    // cross terms
-    double dots = 0;
+    // cross terms sum_q |u^T U_q| |v V_q^T|
+    R dots = 0;
     for (int p = 0; p < nst; p++) {
       const cplx<R>* Up = A.pool + toff[p];
       const cplx<R>* Vp = Up + m;
       cplx<R> ud(0, 0), vd(0, 0);
-      for (int r = lane; r < m; r += 32) cfma(ud, unew[r], Up[r]);
-      for (int c = lane; c < n; c += 32) cfma(vd, vnew[c], Vp[c]);
-      const double udr = warp_sum((double)ud.re), udi = warp_sum((double)ud.im);
-      const double vdr = warp_sum((double)vd.re), vdi = warp_sum((double)vd.im);
+#pragma unroll
+      for (int k = 0; k < LPL; k++) {
+        const int r = lane + 32 * k;
+        if (r < m) cfma(ud, u_l[k], Up[r]);
+        if (r < n) cfma(vd, v_l[k], Vp[r]);
+      }
+      const R udr = warp_sum_r(ud.re), udi = warp_sum_r(ud.im);
+      const R vdr = warp_sum_r(vd.re), vdi = warp_sum_r(vd.im);
       dots += sqrt(udr * udr + udi * udi) * sqrt(vdr * vdr + vdi * vdi);
     }
-    un = warp_sum(un);
-    vn = warp_sum(vn);
-    err += un * vn + 2 * dots;
-    if (sqrt(un * vn / err) <= A.eps) break;
-    const bool zero_term = (un == 0.0) || (vn == 0.0);
+    const double unt = (double)warp_sum_r(un), vnt = (double)warp_sum_r(vn);
+    err += unt * vnt + 2 * (double)dots;
+    if (sqrt(unt * vnt / err) <= A.eps) break;
+    const bool zero_term = (unt == 0.0) || (vnt == 0.0);
     // next row pivot over unused rows
     best = R(-1);
     bidx = 0;
-    for (int r = lane; r < m; r += 32) {
-      if ((used >> r) & 1ull) continue;
-      const R a = abs2(unew[r]);
-      if (a > best) {
-        best = a;
-        bidx = r;
+#pragma unroll
+    for (int k = 0; k < LPL; k++) {
+      const int r = lane + 32 * k;
+      if (r < m && !((used_l >> k) & 1u)) {
+        const R a = abs2(u_l[k]);
+        if (a > best) {
+          best = a;
+          bidx = r;
+        }
       }
     }
     warp_argmax<R>(best, bidx);
     i = bidx;
-    used |= 1ull << i;
+    if (lane == (i & 31)) used_l |= 1u << (i >> 5);
     if (!zero_term) {
       if (lane == 0) {
         toff[nst] = base;
@@ -495,12 +541,29 @@ void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat&
   AC3D_CUDA(cudaGetLastError());
 }
 
-template <typename R, typename P4>
+template <typename R, typename P4, int LPL>
 static void aca_launch_warp(const AcaArgs<R, P4>& a, int nblocks, cudaStream_t s) {
   if (nblocks <= 0) return;
   note_launch();
-  aca_warp_kernel<R, P4><<<(nblocks + 7) / 8, 256, 0, s>>>(a, nblocks);
+  aca_warp_kernel<R, P4, LPL><<<(nblocks + 7) / 8, 256, 0, s>>>(a, nblocks);
   AC3D_CUDA(cudaGetLastError());
+}
+
+// aca_order = [CTA blocks | warp blocks up to 256 | up to 128 | up to 64], counts in DP.aca_split
+template <typename R, typename P4>
+static void aca_launch_all(AcaArgs<R, P4> a, const DevPartition& DP, int max_rows, cudaStream_t s,
+                           cudaStream_t s_small) {
+  // two streams with about equal work: the CTA blocks then the blocks up to 128 on s, the blocks
+  // up to 256 then those up to 64 on s_small
+  const int* order = DP.aca_order.as<int>();
+  const int o1 = DP.aca_split[0], o2 = o1 + DP.aca_split[1], o3 = o2 + DP.aca_split[2];
+  if (DP.aca_split[0] > 0) aca_launch_t(a, DP.aca_split[0], max_rows, s);
+  a.order = order + o1;
+  aca_launch_warp<R, P4, 8>(a, DP.aca_split[1], s_small);
+  a.order = order + o2;
+  aca_launch_warp<R, P4, 4>(a, DP.aca_split[2], s);
+  a.order = order + o3;
+  aca_launch_warp<R, P4, 2>(a, DP.aca_split[3], s_small);
 }
 
 template <typename R, typename P4>
@@ -524,17 +587,13 @@ void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double
                                G.cen.as<double4>(), H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cd>(),
                                H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
                                H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
-    if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
-    a.order = DP.aca_order.as<int>() + DP.naca;
-    aca_launch_warp(a, DP.na - DP.naca, s_small);
+    aca_launch_all(a, DP, max_rows, s, s_small);
   } else {
     AcaArgs<float, float4> a{geo_view<float>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
                              G.cen32.as<float4>(), (float)H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cf>(),
                              H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
                              H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
-    if (DP.naca > 0) aca_launch_t(a, DP.naca, max_rows, s);
-    a.order = DP.aca_order.as<int>() + DP.naca;
-    aca_launch_warp(a, DP.na - DP.naca, s_small);
+    aca_launch_all(a, DP, max_rows, s, s_small);
   }
 }
 

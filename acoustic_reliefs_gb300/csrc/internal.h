@@ -111,8 +111,9 @@ void build_leaf_lists(Partition& P, int maxk);
 struct DevPartition {
   int ne = 0;  // elements
   int nleaf = 0, nd = 0, na = 0;
-  int naca = 0;  // admissible blocks for the CTA ACA kernel (aca_order[0, naca)); the rest are
-                 // small (m, n <= 64) and run one per warp
+  // aca_order is split into blocks for the CTA ACA kernel, then warp-per-block ACA for blocks of
+  // at most 256, 128 and 64 rows and columns; aca_split holds the four counts
+  int aca_split[4] = {0, 0, 0, 0};
   int max_leaf = 0;
   DevBuf near_seg, didx_ptr, didx;
   DevBuf blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
@@ -156,6 +157,10 @@ struct MeshState {
 };
 
 enum Precision { PREC_MIXED = 0, PREC_FP64 = 1 };
+
+// Warp-per-block ACA: largest block side and largest number of iterations it handles.
+constexpr int kWarpAcaMaxDim = 256;
+constexpr int kWarpAcaTerms = 128;
 
 // An assembled H-matrix of (K - I/2) at one wavenumber.
 struct DevHMat {

@@ -41,7 +41,7 @@ __device__ __forceinline__ void reduce_partials(const double* partials, int n, d
   __shared__ double sd[kVecWarps][5];
   double d[5] = {0, 0, 0, 0, 0};
   for (int i = threadIdx.x; i < n; i += blockDim.x)
-    for (int c = 0; c < 5; c++) d[c] += partials[(size_t)i * 5 + c];
+    for (int c = 0; c < 5; c++) d[c] += __ldcg(&partials[(size_t)i * 5 + c]);  // written by other CTAs
   block_sums(d, 5, sd);
   for (int c = 0; c < 5; c++) {
     double s = 0;
@@ -88,6 +88,8 @@ __global__ void k_scalar_init(KState* st, const double* partials, int n, double 
     st->done = s[4] == 0.0 ? 1 : 0;
     st->restart = 0;
     st->restarts = 0;
+    for (int c = 0; c < 5; c++) st->rsum[c] = s[c];
+    st->ticket = 0u;
   }
 }
 
@@ -156,9 +158,13 @@ __global__ void __launch_bounds__(kVecThreads) kf_p(KState* st, const double* pa
                                                     const cplx<VT>* __restrict__ r, cplx<VT>* p, cplx<VT>* v,
                                                     cplx<VT>* rhat) {
   if (st->done) return;
-  double s[5];
-  reduce_partials(partials, nparts, s);
-  const RhoStep o = rho_step(st, s);
+  // the scalars once per CTA (FP64 division is slow): every CTA gets the same values
+  __shared__ RhoStep so;
+  if (threadIdx.x == 0) so = rho_step(st, st->rsum);
+  __syncthreads();
+  const RhoStep o = so;
+  (void)partials;
+  (void)nparts;
   if (o.stop) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       st->rnorm2 = o.rr;
@@ -196,14 +202,18 @@ __global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* re
                                                     const cplx<VT>* __restrict__ r, const cplx<VT>* __restrict__ v,
                                                     cplx<VT>* s) {
   if (st->done) return;
-  double d[5];
-  for (int i = 0; i < 5; i++) d[i] = red5[i];
-  double ar, ai;
-  if (d[0] == 0.0 && d[1] == 0.0) {
+  __shared__ double sa[3];
+  if (threadIdx.x == 0) {
+    const double d0 = red5[0], d1 = red5[1];
+    sa[2] = (d0 == 0.0 && d1 == 0.0) ? 1.0 : 0.0;
+    if (sa[2] == 0.0) cdivd(st->rho_new_re, st->rho_new_im, d0, d1, sa[0], sa[1]);
+  }
+  __syncthreads();
+  if (sa[2] != 0.0) {
     if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 3;
     return;
   }
-  cdivd(st->rho_new_re, st->rho_new_im, d[0], d[1], ar, ai);
+  const double ar = sa[0], ai = sa[1];
   const VT a_r = (VT)ar, a_i = (VT)ai;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const cplx<VT> ri = r[i], vi = v[i];
@@ -222,13 +232,15 @@ __global__ void __launch_bounds__(kVecThreads) kf_xr(KState* st, const double* r
                                                      cplx<VT>* r, const cplx<VT>* __restrict__ t,
                                                      const cplx<VT>* __restrict__ rhat, double* out_partials) {
   if (st->done) return;
-  double d5[5];
-  for (int i = 0; i < 5; i++) d5[i] = red5[i];
-  double wr_d = 0, wi_d = 0;
-  if (d5[4] > 0.0) {
-    wr_d = d5[2] / d5[4];
-    wi_d = d5[3] / d5[4];
+  __shared__ double sw[2];
+  __shared__ bool s_last;
+  if (threadIdx.x == 0) {
+    const double d2 = red5[2], d3 = red5[3], d4 = red5[4];
+    sw[0] = d4 > 0.0 ? d2 / d4 : 0.0;
+    sw[1] = d4 > 0.0 ? d3 / d4 : 0.0;
   }
+  __syncthreads();
+  const double wr_d = sw[0], wi_d = sw[1];
   const double ar_d = st->alpha_new_re, ai_d = st->alpha_new_im;
   const VT ar = (VT)ar_d, ai = (VT)ai_d, wr = (VT)wr_d, wi = (VT)wi_d;
   double d[5] = {0, 0, 0, 0, 0};
@@ -245,6 +257,20 @@ __global__ void __launch_bounds__(kVecThreads) kf_xr(KState* st, const double* r
     d[4] += (double)ri.re * ri.re + (double)ri.im * ri.im;
   }
   write_partials(d, out_partials);
+  // the last CTA to finish reduces the partials in fixed order for the next kf_p
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&st->ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    double tot[5];
+    reduce_partials(out_partials, gridDim.x, tot);
+    if (threadIdx.x == 0) {
+      for (int c = 0; c < 5; c++) st->rsum[c] = tot[c];
+      st->ticket = 0u;
+    }
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->rho_old_re = st->rho_re;
     st->rho_old_im = st->rho_im;

@@ -18,6 +18,9 @@ struct KState {
   int restart;   // this iteration restarts with rhat = r
   int restarts;
   int pad;
+  double rsum[5];   // fixed-order totals of the latest residual partials: (rhat, r), -, -, |r|^2
+  unsigned ticket;  // CTA completion counter of kf_xr (zero between launches)
+  int pad2;
 };
 
 // Device vectors of one solve (complex, FP32 or FP64 according to the solve).
