@@ -218,6 +218,18 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def measured_traffic():
+    """DRAM bytes of one matvec of this workload from the committed ncu capture (one pass of
+    dram__bytes_read.sum + dram__bytes_write.sum over the dot, reduce and gather kernels)."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "hmatvec_relief20k_ncu.md")):
+            if line.startswith("traffic_bytes_per_matvec:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def cpu_baseline_sample(R, Ls, threads=None):
     """One full FP64 solve by the oracle (the reference algorithm restated in C++/OpenMP)."""
     import oracle
@@ -382,13 +394,15 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(y_h.nbytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "H-matrix matvec (phase1 + gather)",
+                     "frac": achieved / peak, "traffic": measured_traffic(),
+                     "traffic_source": "profiles/hmatvec_relief20k_ncu.md (ncu, one matvec of this workload)",
+                     "kernel": "H-matrix matvec (dot + reduce + gather passes)",
                      "bytes_per_launch": int(mv_bytes), "ms_per_launch": mv_ms, "peak_kind": peak_kind},
         "clocks": clk.summary(),
     }
     if cpu:
         line["cpu_baseline"] = cpu
-    if args.sweep_subdivs and world == 1:
+    if args.sweep_subdivs not in ("", "none") and world == 1:
         line["served_sweep"] = served_sweep(args, Ls)
     print(json.dumps(line), flush=True)
     return 0
@@ -403,7 +417,7 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=1e-6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep-subdivs", default="0,1,2",
-                    help="subdiv_top levels of the served sweep ('' to skip; 3 adds the 118680-triangle relief)")
+                    help="subdiv_top levels of the served sweep ('none' to skip; 3 adds the 118680-triangle relief)")
     ap.add_argument("--slots", type=int, default=4, help="server slots (concurrent requests) of the served sweep")
     ap.add_argument("--no-fp64-sweep", action="store_true")
     args = ap.parse_args()
