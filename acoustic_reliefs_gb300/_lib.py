@@ -41,6 +41,7 @@ SIGNATURES = {
     "ac3d_pressures": (_I, [_P, _D, _P, _I, _P]),
     "ac3d_pressures_dev": (_I, [_P, _D, _P, _I, _P, _P]),
     "ac3d_surface_values": (_I, [_P, _D, _P]),
+    "ac3d_solve_multi": (_I, [_P, _D, _I, _P, _I, _P, _I, _P, _P]),
     "ac3d_band_value": (_I, [_P, _D, _P]),
     "ac3d_values": (_I, [_P, _P]),
     "ac3d_value": (_I, [_P, _P, _P]),

@@ -225,6 +225,29 @@ class DiffBEM:
             self._check(_L.lib().ac3d_pressures(self._h, float(frequency), _L.ptr(Ls), len(Ls), _L.ptr(out)))
         return _cplx(out)
 
+    def pvals_multi(self, frequency, vecs, listeners=None, kind: str = "plane", surface: bool = False):
+        """Pressures for several incident fields at one frequency, solved as one block against one
+        H-matrix (ac3d_solve_multi). vecs: (nrhs, 3) plane-wave directions or point-source
+        positions. Returns (nrhs, L) complex128, and the (nrhs, Ne) surface solutions if `surface`."""
+        V = _f64(vecs).reshape(-1, 3)
+        k = {"point": _L.INCIDENT_POINT, "plane": _L.INCIDENT_PLANE}[kind]
+        if listeners is None:
+            n = ctypes.c_int()
+            self._check(_L.lib().ac3d_num_listeners(self._h, ctypes.byref(n)))
+            Ls, nL = None, n.value
+        else:
+            Ls = _f64(listeners).reshape(-1, 3)
+            nL = len(Ls)
+        out = np.zeros((len(V), 2 * nL))
+        ne = 0 if self._Es is None else len(self._Es)
+        xs = np.zeros((len(V), 2 * max(ne, 1))) if surface else None
+        self._check(_L.lib().ac3d_solve_multi(self._h, float(frequency), k, _L.ptr(V), len(V), _L.ptr(Ls),
+                                              0 if Ls is None else nL, _L.ptr(out), _L.ptr(xs)))
+        p = out.view(np.complex128).copy()
+        if surface:
+            return p, xs[:, :2 * ne].copy().view(np.complex128)
+        return p
+
     def surface_vals(self, frequency) -> np.ndarray:
         """acoustics3d.cpp:282-315: the surface solution in tree order."""
         n = 0 if self._Es is None else len(self._Es)

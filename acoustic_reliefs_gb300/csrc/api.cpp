@@ -21,6 +21,7 @@
 #include "internal.h"
 #include "krylov.h"
 #include "listener.h"
+#include "multi.h"
 
 namespace ac3d {
 
@@ -465,6 +466,145 @@ void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   c->stats.outer_steps += outer;
   c->stats.rel_residual = bn2 > 0 ? std::sqrt(rn2 / bn2) : 0.0;
   if (rn2 > tol * tol * bn2) c->stats.converged = 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// Block solve: up to 16 right-hand sides of one H-matrix (FP32 storage), FP32 block BiCGSTAB
+// inside per-column FP64 iterative refinement. b64 / x64: element-major Ne x nrb complex FP64.
+// ------------------------------------------------------------------------------------------
+struct BlockWork {
+  DevBuf kv, parts, vparts, red, tick, pbuf, tbuf, tolb, state, r64, xcol, bcol, rcol, zcol;
+};
+
+int run_block_krylov(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vector<int>& done) {
+  cudaStream_t s = c->stream;
+  const int maxit = c->maxit > 0 ? c->maxit : 2 * B.n;
+  mkrylov_enqueue_init(B, maxit, s);
+  cudaGraph_t graph;
+  const long long before = g_kernel_launches.load();
+  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  mkrylov_enqueue_iterations(B, c->m->DP, H, c->chunk, s);
+  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
+  const long long nodes = g_kernel_launches.load() - before;
+  g_kernel_launches.fetch_sub(nodes);
+  cudaGraphExec_t exec;
+  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  AC3D_CUDA(cudaGraphDestroy(graph));
+  int head[4] = {0, 0, 0, 0};  // iter, maxit, done_all, nrb
+  const int max_launch = maxit / c->chunk + 2;
+  for (int launched = 0; launched < max_launch; launched++) {
+    AC3D_CUDA(cudaGraphLaunch(exec, s));
+    note_launch(nodes);
+    AC3D_CUDA(cudaMemcpyAsync(head, B.state, sizeof(head), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    if (head[2]) break;
+  }
+  AC3D_CUDA(cudaGraphExecDestroy(exec));
+  KStateM st;
+  AC3D_CUDA(cudaMemcpy(&st, B.state, sizeof(KStateM), cudaMemcpyDeviceToHost));
+  done.assign(B.nrb, 0);
+  for (int j = 0; j < B.nrb; j++) done[j] = st.col[j].done;
+  c->stats.matvecs += 2 * st.iter;
+  return st.iter;
+}
+
+// |b - A x|^2 of one column (contiguous FP64 vectors) with the double-float residual matvec
+double column_residual2(ac3d_ctx* c, const DevHMat& H, const cd* b, const cd* x, cd* r) {
+  return reduce_norm2_residual(c, H, false, b, x, r);
+}
+
+double column_norm2(ac3d_ctx* c, const cd* v) {
+  cudaStream_t s = c->stream;
+  const int np = launch_norm2_64(c->m->Ne, v, c->partials.as<double>(), s);
+  launch_reduce5(c->partials.as<double>(), np, c->red.as<double>(), s);
+  AC3D_CUDA(cudaMemcpyAsync(c->h_red, c->red.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  return c->h_red[4];
+}
+
+void solve_block(ac3d_ctx* c, DevHMat& H, int nrb, int nr, const cd* b64, cd* x64, BlockWork& W) {
+  cudaStream_t s = c->stream;
+  ensure_work(c);
+  prepare_multi_kernels();
+  const int n = c->m->Ne, nleaf = c->m->DP.nleaf;
+  const size_t blk32 = (size_t)n * nrb * sizeof(cf);
+  W.kv.ensure(8 * blk32, s);
+  MultiBufs B;
+  B.n = n;
+  B.nrb = nrb;
+  void** slots[8] = {&B.b, &B.x, &B.r, &B.rhat, &B.p, &B.v, &B.s, &B.t};
+  for (int i = 0; i < 8; i++) *slots[i] = (char*)W.kv.p + (size_t)i * blk32;
+  W.parts.ensure((size_t)(std::max(nleaf, 1184) + 1024) * 5 * nrb * sizeof(double), s);
+  W.vparts.ensure((size_t)(1184 + 64 + 1) * 5 * nrb * sizeof(double), s);
+  W.red.ensure((size_t)5 * nrb * sizeof(double), s);
+  if (!W.tick.p) {
+    W.tick.alloc((1024 + 64) * sizeof(unsigned), s);
+    AC3D_CUDA(cudaMemsetAsync(W.tick.p, 0, (1024 + 64) * sizeof(unsigned), s));
+  }
+  W.pbuf.ensure(std::max<size_t>(H.pbuf.bytes / sizeof(cd), 1) * nrb * sizeof(cf), s);
+  W.tbuf.ensure((size_t)std::max<int64_t>(H.task_cap, 1) * nrb * sizeof(cf), s);
+  W.tolb.ensure((size_t)nrb * sizeof(double), s);
+  W.state.ensure(sizeof(KStateM), s);
+  W.r64.ensure((size_t)n * nrb * sizeof(cd), s);
+  for (DevBuf* b : {&W.xcol, &W.bcol, &W.rcol, &W.zcol}) b->ensure((size_t)n * sizeof(cd), s);
+  AC3D_CUDA(cudaMemsetAsync(W.zcol.p, 0, (size_t)n * sizeof(cd), s));
+  B.partials = W.parts.as<double>();
+  B.vpartials = W.vparts.as<double>();
+  B.red = W.red.as<double>();
+  B.ticket = W.tick.as<unsigned>();
+  B.pbuf = W.pbuf.p;
+  B.tbuf = W.tbuf.p;
+  B.tol = W.tolb.as<double>();
+  B.state = W.state.as<KStateM>();
+
+  const double tol = c->solver_tol;
+  AC3D_CUDA(cudaMemsetAsync(x64, 0, (size_t)n * nrb * sizeof(cd), s));
+  AC3D_CUDA(cudaMemcpyAsync(W.r64.p, b64, (size_t)n * nrb * sizeof(cd), cudaMemcpyDeviceToDevice, s));
+  std::vector<double> bn2(nrb, 0.0), rn2(nrb, 0.0);
+  for (int j = 0; j < nr; j++) {
+    launch_block_get(n, nrb, j, b64, W.bcol.p, s);
+    bn2[j] = rn2[j] = column_norm2(c, W.bcol.as<cd>());
+  }
+  int outer = 0, iters = 0;
+  std::vector<int> done;
+  std::vector<double> tin(nrb, 1.0);
+  while (outer < c->max_outer) {
+    bool any = false;
+    for (int j = 0; j < nrb; j++) {
+      const bool act = j < nr && rn2[j] > tol * tol * bn2[j];
+      if (act) {
+        any = true;
+        tin[j] = std::max(c->inner_tol, 0.3 * tol * std::sqrt(bn2[j] / rn2[j]));
+      } else {
+        tin[j] = 1.0;
+        launch_block_set(n, nrb, j, W.zcol.p, W.r64.p, s);  // converged or padding: zero right-hand side
+      }
+    }
+    if (!any) break;
+    AC3D_CUDA(cudaMemcpyAsync(W.tolb.p, tin.data(), nrb * sizeof(double), cudaMemcpyHostToDevice, s));
+    launch_to32(n * nrb, W.r64.p, B.b, s);
+    iters += run_block_krylov(c, H, B, done);
+    launch_add32(n * nrb, x64, B.x, s);
+    for (int j = 0; j < nr; j++) {
+      if (!(rn2[j] > tol * tol * bn2[j])) continue;
+      launch_block_get(n, nrb, j, x64, W.xcol.p, s);
+      launch_block_get(n, nrb, j, b64, W.bcol.p, s);
+      rn2[j] = column_residual2(c, H, W.bcol.as<cd>(), W.xcol.as<cd>(), W.rcol.as<cd>());
+      launch_block_set(n, nrb, j, W.rcol.p, W.r64.p, s);
+    }
+    outer++;
+  }
+  check_pipeline(c, H);
+  c->stats.iterations += iters;
+  c->stats.outer_steps += outer;
+  double worst = 0;
+  for (int j = 0; j < nr; j++) {
+    const double rr = bn2[j] > 0 ? std::sqrt(rn2[j] / bn2[j]) : 0.0;
+    worst = std::max(worst, rr);
+    if (rn2[j] > tol * tol * bn2[j]) c->stats.converged = 0;
+  }
+  c->stats.rel_residual = std::max(c->stats.rel_residual, worst);
+  c->stats.solves += nr;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1070,6 +1210,82 @@ int ac3d_pressures_dev(ac3d_ctx* c, double f, const double* Ls_dev, int L, doubl
     AC3D_CUDA(cudaEventRecord(ev, s));
     AC3D_CUDA(cudaStreamWaitEvent(us, ev, 0));
     AC3D_CUDA(cudaEventDestroy(ev));
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+  });
+}
+
+int ac3d_solve_multi(ac3d_ctx* c, double f, int kind, const double* vecs, int nrhs, const double* Ls, int L,
+                     double* p_out, double* x_out) {
+  if (!c || !vecs || nrhs < 1 || !(f > 0) || (kind != AC3D_INCIDENT_POINT && kind != AC3D_INCIDENT_PLANE) ||
+      (Ls && L < 1))
+    return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    if (c->listener_mode == AC3D_LISTENER_ACA && p_out)
+      throw Error(AC3D_ERR_ARG, "block solves evaluate receivers exactly (listener mode 'dense')");
+    reset_stats(c);
+    cudaStream_t s = c->stream;
+    ensure_base_geometry(c);
+    const double k = wavenumber(f);
+    const int n = c->m->Ne;
+    GpuTimer ta(s);
+    auto H = assemble(c, k, c->prec);
+    c->stats.ms_assemble += ta.stop();
+    ensure_work(c);
+    const double4* recv = c->Ls_dev.as<double4>();
+    int nL = (int)c->Ls.size() / 3;
+    if (Ls) {
+      upload_receivers(c, Ls, L, c->tmp_recv);
+      recv = c->tmp_recv.as<double4>();
+      nL = L;
+    }
+    DevBuf ycol, b64, x64;
+    ycol.alloc((size_t)nL * sizeof(cd), s);
+    BlockWork W;
+    GpuTimer ts(s);
+    for (int start = 0; start < nrhs; start += kMaxRhs) {
+      const int nr = std::min(kMaxRhs, nrhs - start);
+      const int nrb = nr <= 4 ? 4 : nr <= 8 ? 8 : 16;
+      b64.ensure((size_t)n * nrb * sizeof(cd), s);
+      x64.ensure((size_t)n * nrb * sizeof(cd), s);
+      AC3D_CUDA(cudaMemsetAsync(b64.p, 0, (size_t)n * nrb * sizeof(cd), s));
+      for (int j = 0; j < nr; j++) {
+        double v[3];
+        const double* w = vecs + 3 * (size_t)(start + j);
+        const double nrm = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        if (kind == AC3D_INCIDENT_PLANE && !(nrm > 0)) throw Error(AC3D_ERR_ARG, "zero plane-wave direction");
+        for (int d = 0; d < 3; d++) v[d] = kind == AC3D_INCIDENT_PLANE ? w[d] / nrm : w[d];
+        // b = -incident field (adjoint.cpp:95)
+        launch_rhs(c->m->G, 1, k, kind, v, c->b64.p, s);
+        launch_negate64(n, c->b64.p, s);
+        launch_block_set(n, nrb, j, c->b64.p, b64.p, s);
+      }
+      if (c->prec == AC3D_PREC_FP64) {
+        // FP64 storage: one right-hand side at a time through the FP64 solver
+        for (int j = 0; j < nr; j++) {
+          launch_block_get(n, nrb, j, b64.p, c->b64.p, s);
+          solve(c, *H, c->b64.as<cd>(), c->x64.as<cd>(), false);
+          c->stats.solves++;
+          launch_block_set(n, nrb, j, c->x64.p, x64.p, s);
+        }
+      } else {
+        solve_block(c, *H, nrb, nr, b64.as<cd>(), x64.as<cd>(), W);
+      }
+      for (int j = 0; j < nr; j++) {
+        launch_block_get(n, nrb, j, x64.p, c->x64.p, s);
+        if (x_out)
+          AC3D_CUDA(cudaMemcpyAsync(x_out + 2 * (size_t)n * (start + j), c->x64.p, (size_t)n * sizeof(cd),
+                                    cudaMemcpyDeviceToHost, s));
+        if (p_out) {
+          launch_far_field(c->m->G, c->prec, recv, nL, k, c->x64.as<cd>(), ycol.as<cd>(), c->ff_scratch, s);
+          AC3D_CUDA(cudaMemcpyAsync(p_out + 2 * (size_t)nL * (start + j), ycol.p, (size_t)nL * sizeof(cd),
+                                    cudaMemcpyDeviceToHost, s));
+        }
+        AC3D_CUDA(cudaStreamSynchronize(s));
+      }
+    }
+    c->stats.ms_solve += ts.stop();
+    c->last_H = std::move(H);
     if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
   });
 }

@@ -97,109 +97,6 @@ __global__ void to_df_kernel(int n, const cd* __restrict__ x, cplx<df32>* out) {
   out[i] = cplx<df32>(df32(rh, __double2float_rn(v.re - (double)rh)), df32(ih, __double2float_rn(v.im - (double)ih)));
 }
 
-struct SegView {
-  const int* leaf_start;
-  const int* order;  // CTA -> leaf, leaves by decreasing work
-  // region A: near segments (forward gather only)
-  const long long* a_seg;
-  const int* a_kptr;
-  const int* a_idx;
-  // region B: low-rank segments
-  const long long* b_seg;
-  const int* b_kptr;
-  const int* b_idx;
-  // transposed dense blocks
-  const int4* blocks_d;
-  const long long* near_off;
-  const int* trn_ptr;
-  const int* trn;
-  int* err;
-};
-
-// Iterates the chunks of the (up to two) regions of one leaf through the copy ring and calls
-// fn(stage_ptr, region, first_column, columns, next_region, next_first_column, next_columns) for
-// each chunk, all threads together (next_columns = 0 after the last chunk), so that the callback
-// can prefetch what the next chunk needs while it computes this one.
-template <typename MT, typename F>
-__device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes], uint64_t* full, int R,
-                                            const cplx<MT>* a_ptr, int a_cols, const cplx<MT>* b_ptr, int b_cols,
-                                            int* err, F&& fn) {
-  const int cpc = max(2, (int)(kStageBytes / sizeof(cplx<MT>)) / R & ~1);  // columns per chunk, even
-  const int na = (a_cols + cpc - 1) / cpc, nb = (b_cols + cpc - 1) / cpc;
-  const int nch = na + nb;
-  auto chunk = [&](int c, const cplx<MT>*& src, int& region, int& c0, int& ncols) {
-    if (c < na) {
-      region = 0;
-      c0 = c * cpc;
-      ncols = min(cpc, a_cols - c0);
-      src = a_ptr + (long long)c0 * R;
-    } else {
-      region = 1;
-      c0 = (c - na) * cpc;
-      ncols = min(cpc, b_cols - c0);
-      src = b_ptr + (long long)c0 * R;
-    }
-  };
-  if (threadIdx.x == 0) {
-    for (int c = 0; c < min(nch, kStages); c++) {
-      const cplx<MT>* src;
-      int region, c0, ncols;
-      chunk(c, src, region, c0, ncols);
-      const uint32_t bytes = (uint32_t)(ncols * R * sizeof(cplx<MT>));
-      mbar_expect_tx(&full[c], bytes);
-      bulk_copy_g2s(stage[c], src, bytes, &full[c]);
-    }
-  }
-  bool ok = true;
-  int c = 0;
-  for (; c < nch; c++) {
-    const int s = c % kStages;
-    const uint32_t parity = (uint32_t)(c / kStages) & 1u;
-    const bool got = mbar_wait_bounded(&full[s], parity);
-    if (__syncthreads_or(!got)) {
-      ok = false;
-      break;
-    }
-    const cplx<MT>* src;
-    int region, c0, ncols;
-    chunk(c, src, region, c0, ncols);
-    int nregion = 0, nc0 = 0, nncols = 0;
-    if (c + 1 < nch) {
-      const cplx<MT>* nsrc;
-      chunk(c + 1, nsrc, nregion, nc0, nncols);
-    }
-    fn((const cplx<MT>*)stage[s], region, c0, ncols, nregion, nc0, nncols);
-    __syncthreads();  // every warp is done with stage s
-    if (threadIdx.x == 0 && c + kStages < nch) {
-      fence_proxy_async();
-      const cplx<MT>* src2;
-      int region2, c02, ncols2;
-      chunk(c + kStages, src2, region2, c02, ncols2);
-      const uint32_t bytes = (uint32_t)(ncols2 * R * sizeof(cplx<MT>));
-      mbar_expect_tx(&full[s], bytes);
-      bulk_copy_g2s(stage[s], src2, bytes, &full[s]);
-    }
-  }
-  if (!ok) {
-    // record the failure and let the copies already issued land before the CTA exits
-    if (threadIdx.x == 0) {
-      atomicExch(err, 1);
-      for (int cc = c; cc < min(nch, c + kStages); cc++)
-        mbar_wait_bounded(&full[cc % kStages], (uint32_t)(cc / kStages) & 1u);
-    }
-    __syncthreads();
-  }
-  return ok;
-}
-
-__device__ __forceinline__ void init_ring(uint64_t* full) {
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; s++) mbar_init(&full[s], 1);
-    fence_barrier_init();
-  }
-  __syncthreads();
-}
-
 // Lanes per column and rows per lane of the dot pass for leaves of up to 32 RPL rows: a group of G
 // lanes shares one column, lane g summing rows g, g + G, g + 2G, ..., so one warp instruction
 // covers 32 / G columns and the cross-lane sum takes log2(G) shuffle levels.

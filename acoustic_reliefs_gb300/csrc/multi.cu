@@ -1,0 +1,754 @@
+// Block (multi-right-hand-side) H-matrix matvec and block BiCGSTAB.
+//
+// Up to 16 right-hand sides of one frequency (incidence directions) share one H-matrix. Block
+// vectors hold nrb complex FP32 values per element, element-major (Ne x nrb), so every matrix
+// byte streamed from HBM serves nrb products. The passes follow the single-vector matvec
+// (matvec.cu) over the same per-leaf segments and copy ring: dot pass over the V segments,
+// per-term reduce, gather pass over the near and U segments. Forward orientation only.
+//
+// Block BiCGSTAB: nrb independent BiCGSTAB recurrences (van der Vorst 1992) sharing the matvecs,
+// with per-column scalars, FP64 dot products reduced in fixed order, and per-column convergence;
+// a column that has converged (or broken down) is frozen while the others continue.
+#include <algorithm>
+#include <mutex>
+
+#include "common.cuh"
+#include "internal.h"
+#include "multi.h"
+#include "segstream.cuh"
+
+namespace ac3d {
+
+namespace {
+constexpr int kMT = 256;          // threads per CTA
+constexpr int kMW = kMT / 32;     // warps per CTA
+constexpr int kMPieces = 512;     // gather: multiplier values per chunk (columns x nrb)
+constexpr int kGroup = 32;        // CTAs per first-level reduction group
+}  // namespace
+
+// Fixed-order two-level reduction of per-CTA partial vectors (part[blockIdx.x][NV]): the last CTA
+// of each group of 32 sums its group into gpart, the last group to finish sums the group totals
+// into out[NV]. tickets: one counter per group plus one, zero between launches (reset here).
+template <int NV>
+__device__ __forceinline__ void grid_reduce(const double* part, double* gpart, unsigned* tickets, double* out) {
+  __shared__ bool s_last;
+  const int g = blockIdx.x / kGroup, ng = (gridDim.x + kGroup - 1) / kGroup;
+  const int gsize = min(kGroup, (int)gridDim.x - g * kGroup);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&tickets[g], 1u) == (unsigned)(gsize - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int v = threadIdx.x; v < NV; v += blockDim.x) {
+    double a = 0;
+#pragma unroll 8
+    for (int i = 0; i < gsize; i++) a += __ldcg(&part[(size_t)(g * kGroup + i) * NV + v]);
+    gpart[(size_t)g * NV + v] = a;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tickets[g] = 0u;
+    s_last = atomicAdd(&tickets[ng], 1u) == (unsigned)(ng - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int v = threadIdx.x; v < NV; v += blockDim.x) {
+    double a = 0;
+#pragma unroll 8
+    for (int i = 0; i < ng; i++) a += __ldcg(&gpart[(size_t)i * NV + v]);
+    out[v] = a;
+  }
+  if (threadIdx.x == 0) tickets[ng] = 0u;
+}
+
+// Sums d[c] (c < 5) over the threads of the CTA that share a column j = tid % NRB and writes the
+// CTA's partials part[blockIdx.x][c][j].
+template <int NRB>
+__device__ __forceinline__ void cta_partials(double d[5], double* part) {
+  __shared__ double sred[kMW][5][NRB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 5; c++)
+#pragma unroll
+    for (int o = NRB; o < 32; o <<= 1) d[c] += __shfl_xor_sync(0xffffffffu, d[c], o);
+  if (lane < NRB)
+    for (int c = 0; c < 5; c++) sred[warp][c][lane] = d[c];
+  __syncthreads();
+  for (int v = threadIdx.x; v < 5 * NRB; v += blockDim.x) {
+    double a = 0;
+    for (int w = 0; w < kMW; w++) a += sred[w][v / NRB][v % NRB];
+    part[(size_t)blockIdx.x * 5 * NRB + v] = a;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Matvec passes
+// ------------------------------------------------------------------------------------------
+// Dot pass: P[k][j] = sum_rows V[row][k] X[row][j]. Lane (j = lane % NRB, h = lane / NRB) holds
+// X[row][j] for rows h, h + H, ... (H = 32 / NRB); one warp per segment column.
+template <int NRB, int RPL>
+__global__ void __launch_bounds__(kMT) mseg_dot_kernel(SegView V, const cf* __restrict__ seg,
+                                                       const cf* __restrict__ X, cf* __restrict__ P,
+                                                       const int* __restrict__ done) {
+  constexpr int H = 32 / NRB;
+  constexpr int RPH = (32 * RPL + H - 1) / H;
+  extern __shared__ __align__(128) unsigned char dsmem[];
+  auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
+  __shared__ __align__(8) uint64_t full[kStages];
+  if (done && *done) return;
+  const int leaf = V.order[blockIdx.x];
+  const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
+  const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
+  if (K == 0) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int j = lane % NRB, h = lane / NRB;
+  float xr[RPH], xi[RPH];
+#pragma unroll
+  for (int t = 0; t < RPH; t++) {
+    const int row = h + H * t;
+    const cf v = row < R ? X[(size_t)(ls + row) * NRB + j] : cf();
+    xr[t] = v.re;
+    xi[t] = v.im;
+  }
+  init_ring(full);
+  cf* out = P + (size_t)k0 * NRB;
+  stream_leaf<float>(stage, full, R, nullptr, 0, seg + V.b_seg[leaf], K, V.err,
+                     [&](const cf* S, int, int c0, int ncols, int, int, int) {
+                       for (int c = warp; c < ncols; c += kMW) {
+                         const cf* col = S + c * R;
+                         float ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;  // two chains for ILP
+#pragma unroll
+                         for (int t = 0; t < RPH; t++) {
+                           const int row = h + H * t;
+                           if (row < R) {
+                             const cf v = col[row];
+                             float& ar = (t & 1) ? ar1 : ar0;
+                             float& ai = (t & 1) ? ai1 : ai0;
+                             ar = fmaf(v.re, xr[t], ar);
+                             ar = fmaf(-v.im, xi[t], ar);
+                             ai = fmaf(v.re, xi[t], ai);
+                             ai = fmaf(v.im, xr[t], ai);
+                           }
+                         }
+                         float ar = ar0 + ar1, ai = ai0 + ai1;
+#pragma unroll
+                         for (int o = NRB; o < 32; o <<= 1) {
+                           ar += __shfl_xor_sync(0xffffffffu, ar, o);
+                           ai += __shfl_xor_sync(0xffffffffu, ai, o);
+                         }
+                         if (h == 0) out[(size_t)(c0 + c) * NRB + j] = cf(ar, ai);
+                       }
+                     });
+}
+
+// T[task][j] = sum over the task's block entries of P[kpos[e] + q][j], in leaf order.
+template <int NRB>
+__global__ void __launch_bounds__(256) mseg_reduce_kernel(const int* __restrict__ task_b,
+                                                          const int* __restrict__ t_off, int ntask_cap,
+                                                          const int* __restrict__ t_total,
+                                                          const int* __restrict__ ent_ptr,
+                                                          const int* __restrict__ kpos, const cf* __restrict__ P,
+                                                          cf* __restrict__ T, const int* __restrict__ done) {
+  if (done && *done) return;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int task = (int)(i / NRB), j = (int)(i % NRB);
+  if (task >= ntask_cap || task >= *t_total) return;
+  const int b = task_b[task];
+  const int q = task - t_off[b];
+  float sr = 0, si = 0;
+  for (int e = ent_ptr[b]; e < ent_ptr[b + 1]; e++) {
+    const cf v = P[(size_t)(kpos[e] + q) * NRB + j];
+    sr += v.re;
+    si += v.im;
+  }
+  T[(size_t)task * NRB + j] = cf(sr, si);
+}
+
+// Gather pass: Y[rows][j] = -X/2 + near X[idx] + U T[idx], with per-column dot partials. Warp w
+// owns rows w + 8 (h + H i); lane (j, h). With every chunk's bulk copy each thread gathers (at
+// most) one 16-byte piece of a column's multiplier row (two of its nrb values) by cp.async into
+// the stage's multiplier buffer; the stage's mbarrier expects the copy bytes and one arrival per
+// thread, as in the single-vector gather pass.
+template <int NRB, int RPL>
+__global__ void __launch_bounds__(kMT) mseg_gather_kernel(SegView V, const cf* __restrict__ near,
+                                                          const cf* __restrict__ lrseg, const cf* __restrict__ T,
+                                                          const cf* __restrict__ X, cf* __restrict__ Y,
+                                                          const cf* __restrict__ dot_a, const cf* __restrict__ dot_b,
+                                                          double* part, double* gpart, unsigned* tickets,
+                                                          double* red, const int* __restrict__ done) {
+  constexpr int H = 32 / NRB;
+  constexpr int RPW = (4 * RPL + H - 1) / H;  // rows per lane
+  constexpr int CMAX = kMPieces / NRB;        // columns per chunk at most
+  constexpr int PPC = NRB / 2;                // 16-byte pieces per multiplier row
+  extern __shared__ __align__(128) unsigned char dsmem[];
+  auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
+  __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ __align__(16) unsigned char zraw[kStages * kMPieces * sizeof(cf)];
+  auto zbuf = reinterpret_cast<cf(*)[kMPieces]>(zraw);
+  if (done && *done) return;
+  const int leaf = V.order[blockIdx.x];
+  const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int j = lane % NRB, h = lane / NRB;
+
+  const int a_cols = V.a_kptr[leaf + 1] - V.a_kptr[leaf];
+  const int* a_idx = V.a_idx + V.a_kptr[leaf];
+  const int b_cols = V.b_kptr[leaf + 1] - V.b_kptr[leaf];
+  const int* b_idx = V.b_idx + V.b_kptr[leaf];
+  const cf* a_ptr = near + V.a_seg[leaf];
+  const cf* b_ptr = lrseg + V.b_seg[leaf];
+  const int cpc = min(CMAX, max(2, (int)(kStageBytes / sizeof(cf)) / R & ~1));
+  const int na = (a_cols + cpc - 1) / cpc, nb = (b_cols + cpc - 1) / cpc;
+  const int nch = na + nb;
+  struct Chunk {
+    const cf* src;
+    const int* idx;
+    const cf* z;
+    int ncols;
+  };
+  auto chunk = [&](int c) {
+    Chunk k;
+    if (c < na) {
+      const int c0 = c * cpc;
+      k.ncols = min(cpc, a_cols - c0);
+      k.src = a_ptr + (long long)c0 * R;
+      k.idx = a_idx + c0;
+      k.z = X;
+    } else {
+      const int c0 = (c - na) * cpc;
+      k.ncols = min(cpc, b_cols - c0);
+      k.src = b_ptr + (long long)c0 * R;
+      k.idx = b_idx + c0;
+      k.z = T;
+    }
+    return k;
+  };
+  // this thread's piece: column tid / PPC, values 2 (tid % PPC) and 2 (tid % PPC) + 1
+  const int pcol = tid / PPC, ppos = 2 * (tid % PPC);
+  auto col_index = [&](int c) {
+    if (c >= nch) return -1;
+    const Chunk k = chunk(c);
+    return pcol < k.ncols ? k.idx[pcol] : -1;
+  };
+  auto issue = [&](int c, int s, int zi) {
+    const Chunk k = chunk(c);
+    if (pcol < k.ncols) {
+      cf* dst = &zbuf[s][pcol * NRB + ppos];
+      if (zi >= 0) {
+        cp_async_elem<16>(dst, k.z + (size_t)zi * NRB + ppos);
+      } else {
+        dst[0] = cf();
+        dst[1] = cf();
+      }
+    }
+    cp_async_arrive_noinc(&full[s]);
+    if (tid == 0) {
+      const uint32_t bytes = (uint32_t)(k.ncols * R * sizeof(cf));
+      mbar_expect_tx(&full[s], bytes);
+      bulk_copy_g2s(stage[s], k.src, bytes, &full[s]);
+    }
+  };
+
+  if (tid == 0) {
+    for (int st = 0; st < kStages; st++) mbar_init(&full[st], 1 + kMT);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  {
+    int zi[kStages];
+#pragma unroll
+    for (int c = 0; c < kStages; c++) zi[c] = col_index(c);
+#pragma unroll
+    for (int c = 0; c < kStages; c++)
+      if (c < nch) issue(c, c, zi[c]);
+  }
+  int next_zi = col_index(kStages);
+
+  float ar[RPW], ai[RPW];
+#pragma unroll
+  for (int i = 0; i < RPW; i++) ar[i] = ai[i] = 0.f;
+  bool ok = true;
+  int c = 0;
+  for (; c < nch; c++) {
+    const int s = c % kStages;
+    const bool got = mbar_wait_bounded(&full[s], (uint32_t)(c / kStages) & 1u);
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    const int ncols = chunk(c).ncols;
+    const cf* S = (const cf*)stage[s];
+    const cf* Z = zbuf[s];
+    for (int cc = 0; cc < ncols; cc++) {
+      const cf z = Z[cc * NRB + j];
+      const cf* col = S + cc * R;
+#pragma unroll
+      for (int i = 0; i < RPW; i++) {
+        const int row = warp + kMW * (h + H * i);
+        if (row < R) {
+          const cf u = col[row];
+          ar[i] = fmaf(u.re, z.re, ar[i]);
+          ar[i] = fmaf(-u.im, z.im, ar[i]);
+          ai[i] = fmaf(u.re, z.im, ai[i]);
+          ai[i] = fmaf(u.im, z.re, ai[i]);
+        }
+      }
+    }
+    __syncthreads();  // stage s and its multipliers are consumed
+    if (c + kStages < nch) {
+      fence_proxy_async();
+      const int zi = next_zi;
+      next_zi = col_index(c + kStages + 1);
+      issue(c + kStages, s, zi);
+    }
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicExch(V.err, 1);
+      for (int cc = c; cc < min(nch, c + kStages); cc++)
+        mbar_wait_bounded(&full[cc % kStages], (uint32_t)(cc / kStages) & 1u);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  double d[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < RPW; i++) {
+    const int row = warp + kMW * (h + H * i);
+    if (row < R) {
+      const size_t e = (size_t)(ls + row) * NRB + j;
+      const cf xv = X[e];
+      const cf o(ar[i] - 0.5f * xv.re, ai[i] - 0.5f * xv.im);
+      Y[e] = o;
+      const double oyr = o.re, oyi = o.im;
+      if (dot_a) {
+        const cf a = dot_a[e];
+        d[0] += (double)a.re * oyr + (double)a.im * oyi;
+        d[1] += (double)a.re * oyi - (double)a.im * oyr;
+      }
+      if (dot_b) {
+        const cf bb = dot_b[e];
+        d[2] += oyr * (double)bb.re + oyi * (double)bb.im;
+        d[3] += oyr * (double)bb.im - oyi * (double)bb.re;
+      }
+      d[4] += oyr * oyr + oyi * oyi;
+    }
+  }
+  if (part) {
+    cta_partials<NRB>(d, part);
+    grid_reduce<5 * NRB>(part, gpart, tickets, red);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Block BiCGSTAB vector steps (element-major block vectors, column j = index % NRB)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void cdiv64(double ar, double ai, double br, double bi, double& cr, double& ci) {
+  const double s = fabs(br) + fabs(bi);
+  const double xr = br / s, xi = bi / s, yr = ar / s, yi = ai / s;
+  const double d = xr * xr + xi * xi;
+  cr = (yr * xr + yi * xi) / d;
+  ci = (yi * xr - yr * xi) / d;
+}
+
+template <int NRB>
+__global__ void __launch_bounds__(kMT) mk_init(int n, const cf* __restrict__ b, cf* x, cf* r, cf* rhat, cf* p,
+                                               cf* v, double* part) {
+  double d[5] = {0, 0, 0, 0, 0};
+  const long long m = (long long)n * NRB;
+  for (long long i = (long long)blockIdx.x * kMT + threadIdx.x; i < m; i += (long long)gridDim.x * kMT) {
+    const cf bi = b[i];
+    x[i] = cf();
+    r[i] = bi;
+    rhat[i] = bi;
+    p[i] = cf();
+    v[i] = cf();
+    d[4] += (double)bi.re * bi.re + (double)bi.im * bi.im;
+  }
+  cta_partials<NRB>(d, part);
+}
+
+template <int NRB>
+__global__ void mk_scalar_init(KStateM* st, const double* __restrict__ part, int nparts,
+                               const double* __restrict__ tol, int maxit, double* rtot) {
+  const int j = threadIdx.x;
+  if (j == 0) {
+    st->iter = 0;
+    st->maxit = maxit;
+    st->nrb = NRB;
+    st->ticket = 0u;
+  }
+  if (j < NRB) {
+    double s = 0;
+    for (int i = 0; i < nparts; i++) s += part[(size_t)i * 5 * NRB + 4 * NRB + j];
+    KCol& k = st->col[j];
+    k.bnorm2 = k.rnorm2 = k.rhat2 = s;
+    k.tol2 = tol[j] * tol[j] * s;
+    k.rho_re = k.alpha_re = k.omega_re = 1.0;
+    k.rho_im = k.alpha_im = k.omega_im = 0.0;
+    k.rho_new_re = 1.0;
+    k.rho_new_im = 0.0;
+    for (int c = 0; c < 5; c++) rtot[c * NRB + j] = 0.0;
+    rtot[0 * NRB + j] = s;  // (rhat, r) = |b|^2 at the start
+    rtot[4 * NRB + j] = s;
+    k.done = s == 0.0 ? 1 : 0;
+    k.restart = 0;
+    k.restarts = 0;
+  }
+  __syncthreads();
+  if (j == 0) {
+    int all = 1;
+    for (int c = 0; c < NRB; c++) all &= st->col[c].done != 0;
+    st->done_all = all;
+  }
+}
+
+// Per-column scalars shared by the CTAs of one vector kernel (computed by threads 0..NRB-1).
+struct MScal {
+  double a_re, a_im, b_re, b_im;
+  int active, restart;
+};
+
+// start of an iteration: per-column convergence test, rho, beta; p = r + beta (p - omega v)
+template <int NRB>
+__global__ void __launch_bounds__(kMT) mkf_p(KStateM* st, const double* __restrict__ rtot, int n,
+                                             const cf* __restrict__ r, cf* p, cf* v, cf* rhat) {
+  __shared__ MScal sc[NRB];
+  __shared__ int s_any;
+  if (st->done_all) return;
+  const int t = threadIdx.x;
+  if (t == 0) s_any = 0;
+  __syncthreads();
+  if (t < NRB) {
+    const KCol& k = st->col[t];
+    MScal o{0, 0, 0, 0, 0, 0};
+    int stop_code = 0;
+    if (k.done == 0) {
+      const double rr = rtot[4 * NRB + t];
+      if (!(rr > k.tol2)) {
+        stop_code = 1;
+      } else if (st->iter >= st->maxit) {
+        stop_code = 2;
+      } else {
+        double rho_re = rtot[0 * NRB + t], rho_im = rtot[1 * NRB + t];
+        o.active = 1;
+        if (rho_re * rho_re + rho_im * rho_im <= 1e-24 * k.rhat2 * rr) {
+          o.restart = 1;
+          rho_re = rr;
+          rho_im = 0.0;
+        } else {
+          double q1r, q1i, q2r, q2i;
+          cdiv64(rho_re, rho_im, k.rho_re, k.rho_im, q1r, q1i);
+          cdiv64(k.alpha_re, k.alpha_im, k.omega_re, k.omega_im, q2r, q2i);
+          o.b_re = q1r * q2r - q1i * q2i;
+          o.b_im = q1r * q2i + q1i * q2r;
+          o.a_re = k.omega_re;  // omega for the p update
+          o.a_im = k.omega_im;
+        }
+        if (blockIdx.x == 0) {
+          KCol& kw = st->col[t];
+          kw.rnorm2 = rr;
+          kw.rho_new_re = rho_re;
+          kw.rho_new_im = rho_im;
+          kw.restart = o.restart;
+          if (o.restart) kw.restarts++;
+        }
+      }
+      if (stop_code && blockIdx.x == 0) {
+        st->col[t].rnorm2 = rr;
+        st->col[t].done = stop_code;
+      }
+    }
+    sc[t] = o;
+    if (o.active) atomicOr(&s_any, 1);
+  }
+  __syncthreads();
+  if (!s_any) {
+    if (blockIdx.x == 0 && t == 0) st->done_all = 1;
+    return;
+  }
+  const long long m = (long long)n * NRB;
+  for (long long i = (long long)blockIdx.x * kMT + t; i < m; i += (long long)gridDim.x * kMT) {
+    const MScal& o = sc[i % NRB];
+    if (!o.active) continue;
+    const cf ri = r[i];
+    if (o.restart) {
+      rhat[i] = ri;
+      p[i] = ri;
+      v[i] = cf();
+    } else {
+      const float br = (float)o.b_re, bi = (float)o.b_im, wr = (float)o.a_re, wi = (float)o.a_im;
+      const cf pi = p[i], vi = v[i];
+      const float tr = pi.re - (wr * vi.re - wi * vi.im);
+      const float ti = pi.im - (wr * vi.im + wi * vi.re);
+      p[i] = cf(ri.re + br * tr - bi * ti, ri.im + br * ti + bi * tr);
+    }
+  }
+}
+
+// alpha = rho / (rhat, v); s = r - alpha v
+template <int NRB>
+__global__ void __launch_bounds__(kMT) mkf_s(KStateM* st, const double* __restrict__ red, int n,
+                                             const cf* __restrict__ r, const cf* __restrict__ v, cf* s) {
+  __shared__ MScal sc[NRB];
+  if (st->done_all) return;
+  const int t = threadIdx.x;
+  if (t < NRB) {
+    MScal o{0, 0, 0, 0, 0, 0};
+    const KCol& k = st->col[t];
+    if (k.done == 0) {
+      const double d0 = red[0 * NRB + t], d1 = red[1 * NRB + t];
+      if (d0 == 0.0 && d1 == 0.0) {
+        if (blockIdx.x == 0) st->col[t].done = 3;
+      } else {
+        cdiv64(k.rho_new_re, k.rho_new_im, d0, d1, o.a_re, o.a_im);
+        o.active = 1;
+        if (blockIdx.x == 0) {
+          st->col[t].alpha_re = o.a_re;  // the alpha of this iteration (alpha of the last one is
+          st->col[t].alpha_im = o.a_im;  // no longer needed: beta was formed in mkf_p)
+        }
+      }
+    }
+    sc[t] = o;
+  }
+  __syncthreads();
+  const long long m = (long long)n * NRB;
+  for (long long i = (long long)blockIdx.x * kMT + t; i < m; i += (long long)gridDim.x * kMT) {
+    const MScal& o = sc[i % NRB];
+    if (!o.active) continue;
+    const float ar = (float)o.a_re, ai = (float)o.a_im;
+    const cf ri = r[i], vi = v[i];
+    s[i] = cf(ri.re - (ar * vi.re - ai * vi.im), ri.im - (ar * vi.im + ai * vi.re));
+  }
+}
+
+// omega = (t, s) / (t, t); x += alpha p + omega s; r = s - omega t; per-column residual partials
+template <int NRB>
+__global__ void __launch_bounds__(kMT) mkf_xr(KStateM* st, const double* __restrict__ red, int n, cf* x,
+                                              const cf* __restrict__ p, const cf* __restrict__ s, cf* r,
+                                              const cf* __restrict__ tv, const cf* __restrict__ rhat, double* part,
+                                              double* gpart, unsigned* tickets, double* rtot) {
+  __shared__ MScal sc[NRB];
+  if (st->done_all) return;
+  const int t = threadIdx.x;
+  if (t < NRB) {
+    MScal o{0, 0, 0, 0, 0, 0};
+    const KCol& k = st->col[t];
+    if (k.done == 0) {
+      const double d2 = red[2 * NRB + t], d3 = red[3 * NRB + t], d4 = red[4 * NRB + t];
+      o.b_re = d4 > 0.0 ? d2 / d4 : 0.0;  // omega
+      o.b_im = d4 > 0.0 ? d3 / d4 : 0.0;
+      o.a_re = k.alpha_re;
+      o.a_im = k.alpha_im;
+      o.active = 1;
+    }
+    sc[t] = o;
+  }
+  __syncthreads();
+  double d[5] = {0, 0, 0, 0, 0};
+  const long long m = (long long)n * NRB;
+  for (long long i = (long long)blockIdx.x * kMT + t; i < m; i += (long long)gridDim.x * kMT) {
+    const MScal& o = sc[i % NRB];
+    if (!o.active) continue;
+    const float ar = (float)o.a_re, ai = (float)o.a_im, wr = (float)o.b_re, wi = (float)o.b_im;
+    const cf pi = p[i], si = s[i], ti = tv[i], hi = rhat[i];
+    cf xi = x[i];
+    xi.re += (ar * pi.re - ai * pi.im) + (wr * si.re - wi * si.im);
+    xi.im += (ar * pi.im + ai * pi.re) + (wr * si.im + wi * si.re);
+    x[i] = xi;
+    const cf ri(si.re - (wr * ti.re - wi * ti.im), si.im - (wr * ti.im + wi * ti.re));
+    r[i] = ri;
+    d[0] += (double)hi.re * ri.re + (double)hi.im * ri.im;
+    d[1] += (double)hi.re * ri.im - (double)hi.im * ri.re;
+    d[4] += (double)ri.re * ri.re + (double)ri.im * ri.im;
+  }
+  cta_partials<NRB>(d, part);
+  // commit this iteration's scalars before the reduction (only CTA 0 writes them)
+  if (blockIdx.x == 0 && t < NRB && sc[t].active) {
+    KCol& k = st->col[t];
+    k.rho_re = k.rho_new_re;
+    k.rho_im = k.rho_new_im;
+    k.omega_re = sc[t].b_re;
+    k.omega_im = sc[t].b_im;
+    if (k.restart) k.rhat2 = k.rnorm2;
+  }
+  if (blockIdx.x == 0 && t == 0) st->iter++;
+  // the residual totals for the next mkf_p (frozen columns contribute zeros and are not read)
+  grid_reduce<5 * NRB>(part, gpart, tickets, rtot);
+}
+
+__global__ void block_get_kernel(int n, int nrb, int j, const cd* __restrict__ block, cd* col) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) col[i] = block[(size_t)i * nrb + j];
+}
+__global__ void block_set_kernel(int n, int nrb, int j, const cd* __restrict__ col, cd* block) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) block[(size_t)i * nrb + j] = col[i];
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------
+int multi_vec_grid(int n, int nrb) {
+  const long long g = ((long long)n * nrb + kMT - 1) / kMT;
+  return (int)std::max<long long>(1, std::min<long long>(g, 1184));
+}
+
+constexpr size_t kMRing = (size_t)kStages * kStageBytes;
+
+template <int NRB, int RPL>
+static void set_multi_attrs() {
+  AC3D_CUDA(cudaFuncSetAttribute(mseg_dot_kernel<NRB, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMRing));
+  AC3D_CUDA(cudaFuncSetAttribute(mseg_gather_kernel<NRB, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kMRing));
+  AC3D_CUDA(cudaFuncSetAttribute(mseg_dot_kernel<NRB, RPL>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  AC3D_CUDA(cudaFuncSetAttribute(mseg_gather_kernel<NRB, RPL>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+}
+
+void prepare_multi_kernels() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    set_multi_attrs<4, 1>();
+    set_multi_attrs<4, 2>();
+    set_multi_attrs<8, 1>();
+    set_multi_attrs<8, 2>();
+    set_multi_attrs<16, 1>();
+    set_multi_attrs<16, 2>();
+  });
+}
+
+template <int NRB, int RPL>
+static void mmv_t(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, const void* x, void* y,
+                  const void* dot_a, const void* dot_b, const int* done, cudaStream_t s) {
+  SegView v{};
+  v.leaf_start = DP.leaf_start.as<int>();
+  v.a_seg = DP.near_seg.as<long long>();
+  v.a_kptr = DP.didx_ptr.as<int>();
+  v.a_idx = DP.didx.as<int>();
+  v.err = H.err.as<int>();
+  cf* P = (cf*)B.pbuf;
+  cf* T = (cf*)B.tbuf;
+  if (DP.na > 0) {
+    SegView d = v;
+    d.b_seg = H.seg_t.as<long long>();
+    d.b_kptr = H.kseg_t.as<int>();
+    d.order = H.order_cols.as<int>();
+    note_launch();
+    mseg_dot_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(d, H.vseg.as<cf>(), (const cf*)x, P, done);
+    AC3D_CUDA(cudaGetLastError());
+    note_launch();
+    const long long thr = H.task_cap * NRB;
+    mseg_reduce_kernel<NRB><<<(int)((thr + 255) / 256), 256, 0, s>>>(
+        H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na, DP.blk_tr_ptr.as<int>(),
+        H.kpos_t.as<int>(), P, T, done);
+    AC3D_CUDA(cudaGetLastError());
+  }
+  v.b_seg = H.seg_f.as<long long>();
+  v.b_kptr = H.kseg_f.as<int>();
+  v.b_idx = H.uidx.as<int>();
+  v.order = H.order_rows.as<int>();
+  const bool dots = dot_a || dot_b;
+  note_launch();
+  mseg_gather_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(
+      v, H.near.as<cf>(), H.useg.as<cf>(), T, (const cf*)x, (cf*)y, (const cf*)dot_a, (const cf*)dot_b,
+      dots ? B.partials : nullptr, B.partials + (size_t)std::max(DP.nleaf, 1184) * 5 * NRB, B.ticket, B.red, done);
+  if (DP.nleaf > 1024 * kGroup) throw Error(1, "block solves support at most 32768 leaf clusters");
+  AC3D_CUDA(cudaGetLastError());
+}
+
+template <int NRB>
+static void mmv_rpl(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, const void* x, void* y,
+                    const void* dot_a, const void* dot_b, const int* done, cudaStream_t s) {
+  if (DP.max_leaf <= 32)
+    mmv_t<NRB, 1>(DP, H, B, x, y, dot_a, dot_b, done, s);
+  else if (DP.max_leaf <= 64)
+    mmv_t<NRB, 2>(DP, H, B, x, y, dot_a, dot_b, done, s);
+  else
+    throw Error(1, "block solves need leaf clusters of at most 64 elements");
+}
+
+void launch_mmatvec(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, const void* x, void* y,
+                    const void* dot_a, const void* dot_b, const int* done, cudaStream_t s) {
+  if (H.prec == PREC_FP64) throw Error(3, "internal: block matvec needs FP32 storage");
+  switch (B.nrb) {
+    case 4: mmv_rpl<4>(DP, H, B, x, y, dot_a, dot_b, done, s); break;
+    case 8: mmv_rpl<8>(DP, H, B, x, y, dot_a, dot_b, done, s); break;
+    case 16: mmv_rpl<16>(DP, H, B, x, y, dot_a, dot_b, done, s); break;
+    default: throw Error(3, "internal: block width must be 4, 8 or 16");
+  }
+}
+
+// Partial buffers: matvec partials (max(nleaf, 1184) CTAs) then its group totals (1024 groups);
+// vector partials (1184 CTAs), their group totals (64 groups), then the residual totals. Tickets:
+// 1024 for the matvec groups, then 64 for the vector groups.
+static double* vtotals(const MultiBufs& B, int nrb) {
+  return B.vpartials + (size_t)(1184 + 64) * 5 * nrb;
+}
+
+template <int NRB>
+static void mk_init_t(const MultiBufs& B, int maxit, cudaStream_t s) {
+  const int G = multi_vec_grid(B.n, NRB);
+  note_launch();
+  mk_init<NRB><<<G, kMT, 0, s>>>(B.n, (const cf*)B.b, (cf*)B.x, (cf*)B.r, (cf*)B.rhat, (cf*)B.p, (cf*)B.v,
+                                 B.vpartials);
+  AC3D_CUDA(cudaGetLastError());
+  note_launch();
+  mk_scalar_init<NRB><<<1, 32, 0, s>>>(B.state, B.vpartials, G, B.tol, maxit, vtotals(B, NRB));
+  AC3D_CUDA(cudaGetLastError());
+}
+
+void mkrylov_enqueue_init(const MultiBufs& B, int maxit, cudaStream_t s) {
+  switch (B.nrb) {
+    case 4: mk_init_t<4>(B, maxit, s); break;
+    case 8: mk_init_t<8>(B, maxit, s); break;
+    default: mk_init_t<16>(B, maxit, s); break;
+  }
+}
+
+template <int NRB>
+static void mk_iter_t(const MultiBufs& B, const DevPartition& DP, const DevHMat& H, cudaStream_t s) {
+  const int n = B.n, G = multi_vec_grid(n, NRB);
+  KStateM* st = B.state;
+  const int* done = &st->done_all;
+  double* vpart = B.vpartials;
+  double* vgpart = B.vpartials + (size_t)1184 * 5 * NRB;
+  double* vtot = vtotals(B, NRB);
+  unsigned* vtick = B.ticket + 1024;
+  note_launch();
+  mkf_p<NRB><<<G, kMT, 0, s>>>(st, vtot, n, (const cf*)B.r, (cf*)B.p, (cf*)B.v, (cf*)B.rhat);
+  launch_mmatvec(DP, H, B, B.p, B.v, B.rhat, nullptr, done, s);
+  note_launch();
+  mkf_s<NRB><<<G, kMT, 0, s>>>(st, B.red, n, (const cf*)B.r, (const cf*)B.v, (cf*)B.s);
+  launch_mmatvec(DP, H, B, B.s, B.t, nullptr, B.s, done, s);
+  note_launch();
+  mkf_xr<NRB><<<G, kMT, 0, s>>>(st, B.red, n, (cf*)B.x, (const cf*)B.p, (const cf*)B.s, (cf*)B.r,
+                                (const cf*)B.t, (const cf*)B.rhat, vpart, vgpart, vtick, vtot);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+void mkrylov_enqueue_iterations(const MultiBufs& B, const DevPartition& DP, const DevHMat& H, int count,
+                                cudaStream_t s) {
+  for (int i = 0; i < count; i++) {
+    switch (B.nrb) {
+      case 4: mk_iter_t<4>(B, DP, H, s); break;
+      case 8: mk_iter_t<8>(B, DP, H, s); break;
+      default: mk_iter_t<16>(B, DP, H, s); break;
+    }
+  }
+}
+
+void launch_block_get(int n, int nrb, int j, const void* block, void* col, cudaStream_t s) {
+  note_launch();
+  block_get_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, nrb, j, (const cd*)block, (cd*)col);
+  AC3D_CUDA(cudaGetLastError());
+}
+void launch_block_set(int n, int nrb, int j, const void* col, void* block, cudaStream_t s) {
+  note_launch();
+  block_set_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, nrb, j, (const cd*)col, (cd*)block);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+}  // namespace ac3d

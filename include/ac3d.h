@@ -101,6 +101,15 @@ int ac3d_pressures(ac3d_ctx* ctx, double frequency, const double* Ls, int L, dou
  * ordered after `stream` (a cudaStream_t), which waits for completion. Ls_dev may be NULL
  * (context receivers). No host copies of inputs or outputs. */
 int ac3d_pressures_dev(ac3d_ctx* ctx, double frequency, const double* Ls_dev, int L, double* out_dev, void* stream);
+/* Forward solves of nrhs incident fields at one frequency against one H-matrix: block BiCGSTAB
+ * over up to 16 right-hand sides at a time (more run in batches of 16), each matrix byte read once
+ * per matvec for the whole block. kind: AC3D_INCIDENT_*; vecs: nrhs x 3 (plane-wave directions or
+ * point-source positions). p_out (nrhs x L complex) receives the pressures at the receivers Ls
+ * (L x 3; NULL: the context's receivers), x_out (nrhs x Ne complex, tree order) the surface
+ * solutions; either may be NULL. No reference counterpart: the reference solves one right-hand
+ * side at a time (bem3d::gradient, adjoint.cpp:92-95; DiffBEM::pvals, acoustics3d.cpp:236-280). */
+int ac3d_solve_multi(ac3d_ctx* ctx, double frequency, int kind, const double* vecs, int nrhs, const double* Ls, int L,
+                     double* p_out, double* x_out);
 /* surface_vals(frequency) -- acoustics3d.cpp:282-315; out receives Ne complex values. */
 int ac3d_surface_values(ac3d_ctx* ctx, double frequency, double* out);
 /* band_value(freq_band) -- acoustics3d.cpp:162-176. */
