@@ -64,6 +64,7 @@ SIGNATURES = {
     "ac3d_server_poll": (_I, [_P, ctypes.c_longlong, ctypes.POINTER(_I)]),
     "ac3d_server_wait": (_I, [_P, ctypes.c_longlong, _P, _P]),
     "ac3d_admit_next": (_I, [_P, _P, _I, ctypes.c_longlong, ctypes.c_longlong, _I]),
+    "ac3d_tensor_selftest": (_I, [_P, _P, _I, _P]),
 }
 
 

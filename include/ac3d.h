@@ -166,6 +166,11 @@ int ac3d_partition_get(const ac3d_partition* p, int32_t* order, int32_t* direct,
 void ac3d_partition_free(ac3d_partition* p);
 /* Library version string. */
 const char* ac3d_version(void);
+/* Self-check of the tensor-core product of the block matvec: D (128 x 32) = A (128 x K) B^T with
+ * B (32 x K), all row-major FP32 host arrays, K a multiple of 8 up to 128, formed by one CTA with
+ * tcgen05.mma (TF32 operands split in three products, FP32 accumulation in tensor memory). No
+ * reference counterpart. */
+int ac3d_tensor_selftest(const float* A, const float* B, int K, float* D);
 
 /* ---------------------------------------------------------------------------------------------
  * Request server. No reference counterpart: the reference solves one frequency at a time inside
