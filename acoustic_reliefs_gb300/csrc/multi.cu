@@ -159,7 +159,22 @@ __global__ void __launch_bounds__(256) mseg_reduce_kernel(const int* __restrict_
   const int b = task_b[task];
   const int q = task - t_off[b];
   float sr = 0, si = 0;
-  for (int e = ent_ptr[b]; e < ent_ptr[b + 1]; e++) {
+  const int e1 = ent_ptr[b + 1];
+  int e = ent_ptr[b];
+  for (; e + 3 < e1; e += 4) {  // four independent loads in flight, summed in entry order
+    const int k0 = kpos[e], k1 = kpos[e + 1], k2 = kpos[e + 2], k3 = kpos[e + 3];
+    const cf v0 = P[(size_t)(k0 + q) * NRB + j], v1 = P[(size_t)(k1 + q) * NRB + j];
+    const cf v2 = P[(size_t)(k2 + q) * NRB + j], v3 = P[(size_t)(k3 + q) * NRB + j];
+    sr += v0.re;
+    si += v0.im;
+    sr += v1.re;
+    si += v1.im;
+    sr += v2.re;
+    si += v2.im;
+    sr += v3.re;
+    si += v3.im;
+  }
+  for (; e < e1; e++) {
     const cf v = P[(size_t)(kpos[e] + q) * NRB + j];
     sr += v.re;
     si += v.im;
@@ -167,8 +182,11 @@ __global__ void __launch_bounds__(256) mseg_reduce_kernel(const int* __restrict_
   T[(size_t)task * NRB + j] = cf(sr, si);
 }
 
-// Gather pass: Y[rows][j] = -X/2 + near X[idx] + U T[idx], with per-column dot partials. Warp w
-// owns rows w + 8 (h + H i); lane (j, h). With every chunk's bulk copy each thread gathers (at
+// Gather pass: Y[rows][j] = -X/2 + near X[idx] + U T[idx], with per-column dot partials. Lane l
+// owns rows l + 32 q of the leaf and accumulates all NRB right-hand sides of them; warp w takes the
+// chunk columns w, w + 8, ..., so each segment element read from shared memory feeds 4 NRB FMAs
+// against the column's multiplier row (read as broadcast 16-byte loads). The warps' partial tiles
+// are summed once per leaf in fixed order. With every chunk's bulk copy each thread gathers (at
 // most) one 16-byte piece of a column's multiplier row (two of its nrb values) by cp.async into
 // the stage's multiplier buffer; the stage's mbarrier expects the copy bytes and one arrival per
 // thread, as in the single-vector gather pass.
@@ -179,8 +197,6 @@ __global__ void __launch_bounds__(kMT) mseg_gather_kernel(SegView V, const cf* _
                                                           const cf* __restrict__ dot_a, const cf* __restrict__ dot_b,
                                                           double* part, double* gpart, unsigned* tickets,
                                                           double* red, const int* __restrict__ done) {
-  constexpr int H = 32 / NRB;
-  constexpr int RPW = (4 * RPL + H - 1) / H;  // rows per lane
   constexpr int CMAX = kMPieces / NRB;        // columns per chunk at most
   constexpr int PPC = NRB / 2;                // 16-byte pieces per multiplier row
   extern __shared__ __align__(128) unsigned char dsmem[];
@@ -192,7 +208,6 @@ __global__ void __launch_bounds__(kMT) mseg_gather_kernel(SegView V, const cf* _
   const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int j = lane % NRB, h = lane / NRB;
 
   const int a_cols = V.a_kptr[leaf + 1] - V.a_kptr[leaf];
   const int* a_idx = V.a_idx + V.a_kptr[leaf];
@@ -267,9 +282,11 @@ __global__ void __launch_bounds__(kMT) mseg_gather_kernel(SegView V, const cf* _
   }
   int next_zi = col_index(kStages);
 
-  float ar[RPW], ai[RPW];
+  float ar[RPL][NRB], ai[RPL][NRB];
 #pragma unroll
-  for (int i = 0; i < RPW; i++) ar[i] = ai[i] = 0.f;
+  for (int q = 0; q < RPL; q++)
+#pragma unroll
+    for (int jj = 0; jj < NRB; jj++) ar[q][jj] = ai[q][jj] = 0.f;
   bool ok = true;
   int c = 0;
   for (; c < nch; c++) {
@@ -282,18 +299,28 @@ __global__ void __launch_bounds__(kMT) mseg_gather_kernel(SegView V, const cf* _
     const int ncols = chunk(c).ncols;
     const cf* S = (const cf*)stage[s];
     const cf* Z = zbuf[s];
-    for (int cc = 0; cc < ncols; cc++) {
-      const cf z = Z[cc * NRB + j];
+    for (int cc = warp; cc < ncols; cc += kMW) {
       const cf* col = S + cc * R;
+      cf u[RPL];
 #pragma unroll
-      for (int i = 0; i < RPW; i++) {
-        const int row = warp + kMW * (h + H * i);
-        if (row < R) {
-          const cf u = col[row];
-          ar[i] = fmaf(u.re, z.re, ar[i]);
-          ar[i] = fmaf(-u.im, z.im, ar[i]);
-          ai[i] = fmaf(u.re, z.im, ai[i]);
-          ai[i] = fmaf(u.im, z.re, ai[i]);
+      for (int q = 0; q < RPL; q++) {
+        const int row = lane + 32 * q;
+        u[q] = row < R ? col[row] : cf();
+      }
+      const float4* z4 = reinterpret_cast<const float4*>(Z + cc * NRB);
+#pragma unroll
+      for (int jj = 0; jj < NRB / 2; jj++) {
+        const float4 zz = z4[jj];  // multipliers 2 jj and 2 jj + 1
+#pragma unroll
+        for (int q = 0; q < RPL; q++) {
+          ar[q][2 * jj] = fmaf(u[q].re, zz.x, ar[q][2 * jj]);
+          ar[q][2 * jj] = fmaf(-u[q].im, zz.y, ar[q][2 * jj]);
+          ai[q][2 * jj] = fmaf(u[q].re, zz.y, ai[q][2 * jj]);
+          ai[q][2 * jj] = fmaf(u[q].im, zz.x, ai[q][2 * jj]);
+          ar[q][2 * jj + 1] = fmaf(u[q].re, zz.z, ar[q][2 * jj + 1]);
+          ar[q][2 * jj + 1] = fmaf(-u[q].im, zz.w, ar[q][2 * jj + 1]);
+          ai[q][2 * jj + 1] = fmaf(u[q].re, zz.w, ai[q][2 * jj + 1]);
+          ai[q][2 * jj + 1] = fmaf(u[q].im, zz.z, ai[q][2 * jj + 1]);
         }
       }
     }
@@ -314,14 +341,38 @@ __global__ void __launch_bounds__(kMT) mseg_gather_kernel(SegView V, const cf* _
     cp_async_wait_all();
     __syncthreads();
   }
-  double d[5] = {0, 0, 0, 0, 0};
+  // sum the warps' tiles in fixed order through four slots in the ring memory (all stages are
+  // consumed): slot w = warp w + warp w + 4, then slot 0 + 1 + 2 + 3
+  cf* tile = (cf*)stage;
+  const int tsz = R * NRB;
+  __syncthreads();
+  for (int round = 0; round < 2; round++) {
+    if ((warp >> 2) == round) {
+      cf* dst = tile + (warp & 3) * tsz;
 #pragma unroll
-  for (int i = 0; i < RPW; i++) {
-    const int row = warp + kMW * (h + H * i);
-    if (row < R) {
-      const size_t e = (size_t)(ls + row) * NRB + j;
+      for (int q = 0; q < RPL; q++) {
+        const int row = lane + 32 * q;
+        if (row < R) {
+#pragma unroll
+          for (int jj = 0; jj < NRB; jj++) {
+            cf v(ar[q][jj], ai[q][jj]);
+            if (round) v = cf(dst[row * NRB + jj].re + v.re, dst[row * NRB + jj].im + v.im);
+            dst[row * NRB + jj] = v;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  double d[5] = {0, 0, 0, 0, 0};
+  for (int i = tid; i < tsz; i += kMT) {  // column j = tid % NRB for every i of this thread
+    const int row = i / NRB;
+    {
+      const cf t0 = tile[i], t1 = tile[tsz + i], t2 = tile[2 * tsz + i], t3 = tile[3 * tsz + i];
+      const float sr = ((t0.re + t1.re) + t2.re) + t3.re, si = ((t0.im + t1.im) + t2.im) + t3.im;
+      const size_t e = (size_t)(ls + row) * NRB + i % NRB;
       const cf xv = X[e];
-      const cf o(ar[i] - 0.5f * xv.re, ai[i] - 0.5f * xv.im);
+      const cf o(sr - 0.5f * xv.re, si - 0.5f * xv.im);
       Y[e] = o;
       const double oyr = o.re, oyi = o.im;
       if (dot_a) {

@@ -364,6 +364,27 @@ def run_gpu(args):
     err64 = float(np.linalg.norm(y_mixed - y64) / np.linalg.norm(y64))
     st64 = f64.stats()
 
+    # block solve: 16 incidence directions of the same frequency against one H-matrix
+    multi = None
+    if args.multi_rhs > 0:
+        rng = np.random.default_rng(1)
+        dirs = rng.normal(size=(args.multi_rhs, 3))
+        dirs[:, 1] = -np.abs(dirs[:, 1]) - 0.5
+        dirs[0] = DIRECTION
+        dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+        bem.pvals_multi(FREQ, dirs, Ls)  # warm-up
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            P = bem.pvals_multi(FREQ, dirs, Ls)
+        dt = (time.perf_counter() - t0) / reps
+        stm = bem.stats()
+        multi = {"solves_per_s": args.multi_rhs / dt, "ms_per_block": 1e3 * dt, "rhs": args.multi_rhs,
+                 "block_iterations": stm["iterations"], "refinement_steps": stm["outer_steps"],
+                 "max_rel_residual": stm["rel_residual"],
+                 "pressure_rel_err_vs_single_solve": float(np.linalg.norm(P[0] - y_mixed) / np.linalg.norm(y_mixed)),
+                 "note": "host API call (ac3d_solve_multi), assembly + block BiCGSTAB + receivers per block"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, cores, ycpu, info = cpu_baseline_sample(R, Ls)
@@ -402,6 +423,8 @@ def run_gpu(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if multi:
+        line["multi_rhs"] = multi
     if args.sweep_subdivs not in ("", "none") and world == 1:
         line["served_sweep"] = served_sweep(args, Ls)
     print(json.dumps(line), flush=True)
@@ -420,6 +443,7 @@ def main():
                     help="subdiv_top levels of the served sweep ('none' to skip; 3 adds the 118680-triangle relief)")
     ap.add_argument("--slots", type=int, default=4, help="server slots (concurrent requests) of the served sweep")
     ap.add_argument("--no-fp64-sweep", action="store_true")
+    ap.add_argument("--multi-rhs", type=int, default=16, help="directions of the block-solve leg (0 to skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
