@@ -306,6 +306,7 @@ void ensure_work(ac3d_ctx* c) {
   cudaStream_t s = c->stream;
   const size_t n = (size_t)c->m->Ne;
   c->kv.ensure(8 * n * sizeof(cd), s);
+  c->kv32.ensure(2 * n * sizeof(cf), s);
   const int G = krylov_vec_grid(c->m->Ne);
   c->partials.ensure((size_t)(c->m->DP.nleaf + G) * 5 * sizeof(double) + 64, s);
   c->kstate.ensure(sizeof(KState), s);
@@ -326,6 +327,10 @@ KrylovBufs bufs(ac3d_ctx* c, int vec64) {
   char* base = (char*)c->kv.p;
   void** slots[8] = {&B.b, &B.x, &B.r, &B.rhat, &B.p, &B.v, &B.s, &B.t};
   for (int i = 0; i < 8; i++) *slots[i] = base + (size_t)i * c->m->Ne * es;
+  if (vec64 == 2) {
+    B.p32 = c->kv32.p;
+    B.s32 = (char*)c->kv32.p + (size_t)c->m->Ne * sizeof(cf);
+  }
   B.partials = c->partials.as<double>();
   B.nparts_r = krylov_vec_grid(c->m->Ne);
   B.nleaf = c->m->DP.nleaf;
@@ -440,8 +445,9 @@ void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
     if (done != 1) c->stats.converged = 0;
     return;
   }
-  // mixed precision: FP32 inner BiCGSTAB inside FP64 iterative refinement
-  KrylovBufs B = bufs(c, 0);
+  // mixed precision: inner BiCGSTAB with FP64 vectors and scalars on the FP32 H-matrix (FP32
+  // matvec arithmetic on FP32 shadows of p and s), inside FP64 iterative refinement
+  KrylovBufs B = bufs(c, 2);
   launch_zero64(n, x, s);
   // x = 0: the first residual is b itself
   launch_copy64(n, b, c->r64.p, s);
@@ -453,12 +459,12 @@ void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   double rn2 = bn2;
   int outer = 0;
   while (outer < c->max_outer && rn2 > tol * tol * bn2) {
-    launch_to32(n, c->r64.p, B.b, s);
+    launch_copy64(n, c->r64.p, B.b, s);
     double need = tol * std::sqrt(bn2 / rn2);
     double tin = std::max(c->inner_tol, 0.3 * need);
-    int it = run_krylov(c, H, B, tr, 0, tin, &done);
+    int it = run_krylov(c, H, B, tr, 2, tin, &done);
     c->stats.iterations += it;
-    launch_add32(n, x, B.x, s);
+    launch_add64(n, x, B.x, s);
     rn2 = reduce_norm2_residual(c, H, tr, b, x, c->r64.as<cd>());
     outer++;
     if (done == 3 && it == 0) break;
@@ -990,7 +996,7 @@ void ac3d_destroy(ac3d_ctx* c) {
   if (s) cudaStreamSynchronize(s);
   // every device buffer is released on the context stream, so all of them go before the stream
   c->last_H.reset();
-  DevBuf* bufs[] = {&c->kv, &c->partials, &c->kstate, &c->red, &c->b64, &c->x64, &c->r64, &c->ff_scratch,
+  DevBuf* bufs[] = {&c->kv, &c->kv32, &c->partials, &c->kstate, &c->red, &c->b64, &c->x64, &c->r64, &c->ff_scratch,
                     &c->adj_scratch, &c->tmp_recv, &c->Ls_dev, &c->d_h_off, &c->d_pair_elem, &c->d_pair_corner,
                     &c->d_pair_touch, &c->d_touch};
   for (DevBuf* b : bufs) b->release();

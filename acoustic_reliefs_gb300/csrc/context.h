@@ -53,6 +53,7 @@ struct ac3d_ctx {
 
   // work buffers
   ac3d::DevBuf kv, partials, kstate, red, b64, x64, r64, ff_scratch, adj_scratch, tmp_recv;
+  ac3d::DevBuf kv32;  // FP32 shadows of the Krylov p and s of the mixed-precision inner solve
   std::unique_ptr<ac3d::DevHMat> last_H;  // H-matrix of the latest forward solve (matvec timing)
   ac3d::KState* h_state = nullptr;  // pinned
   double* h_red = nullptr;    // pinned

@@ -156,7 +156,7 @@ __device__ __forceinline__ RhoStep rho_step(const KState* st, const double* s) {
 template <typename VT>
 __global__ void __launch_bounds__(kVecThreads) kf_p(KState* st, const double* partials, int nparts, int n,
                                                     const cplx<VT>* __restrict__ r, cplx<VT>* p, cplx<VT>* v,
-                                                    cplx<VT>* rhat) {
+                                                    cplx<VT>* rhat, cf* p32) {
   if (st->done) return;
   // the scalars once per CTA (FP64 division is slow): every CTA gets the same values
   __shared__ RhoStep so;
@@ -176,16 +176,19 @@ __global__ void __launch_bounds__(kVecThreads) kf_p(KState* st, const double* pa
   const VT wr = (VT)(o.restart ? 1.0 : st->omega_re), wi = (VT)(o.restart ? 0.0 : st->omega_im);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const cplx<VT> ri = r[i];
+    cplx<VT> pn;
     if (o.restart) {
       rhat[i] = ri;
-      p[i] = ri;
+      pn = ri;
       v[i] = cplx<VT>();
     } else {
       const cplx<VT> pi = p[i], vi = v[i];
       const VT tr = pi.re - (wr * vi.re - wi * vi.im);
       const VT ti = pi.im - (wr * vi.im + wi * vi.re);
-      p[i] = cplx<VT>(ri.re + br * tr - bi * ti, ri.im + br * ti + bi * tr);
+      pn = cplx<VT>(ri.re + br * tr - bi * ti, ri.im + br * ti + bi * tr);
     }
+    p[i] = pn;
+    if (p32) p32[i] = cf((float)pn.re, (float)pn.im);  // matvec input of the FP32-storage solve
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->rnorm2 = o.rr;
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(kVecThreads) kf_p(KState* st, const double* pa
 template <typename VT>
 __global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* red5, int n,
                                                     const cplx<VT>* __restrict__ r, const cplx<VT>* __restrict__ v,
-                                                    cplx<VT>* s) {
+                                                    cplx<VT>* s, cf* s32) {
   if (st->done) return;
   __shared__ double sa[3];
   if (threadIdx.x == 0) {
@@ -217,7 +220,9 @@ __global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* re
   const VT a_r = (VT)ar, a_i = (VT)ai;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const cplx<VT> ri = r[i], vi = v[i];
-    s[i] = cplx<VT>(ri.re - (a_r * vi.re - a_i * vi.im), ri.im - (a_r * vi.im + a_i * vi.re));
+    const cplx<VT> si(ri.re - (a_r * vi.re - a_i * vi.im), ri.im - (a_r * vi.im + a_i * vi.re));
+    s[i] = si;
+    if (s32) s32[i] = cf((float)si.re, (float)si.im);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->alpha_new_re = ar;
@@ -292,6 +297,12 @@ __global__ void k_to32(int n, const cd* __restrict__ a, cf* b) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     b[i] = cf((float)a[i].re, (float)a[i].im);
 }
+__global__ void k_add64(int n, cd* x, const cd* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i].re += d[i].re;
+    x[i].im += d[i].im;
+  }
+}
 __global__ void k_add32(int n, cd* x, const cf* __restrict__ d) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i].re += (double)d[i].re;
@@ -330,28 +341,33 @@ static int vec_grid(int n) {
   return g < 1 ? 1 : (g > 1184 ? 1184 : g);
 }
 
+// vec64: 0 FP32 vectors; 1 FP64 vectors and FP64 matvec arithmetic (FP64 storage); 2 FP64 vectors,
+// FP32 storage and FP32 matvec arithmetic on FP32 shadow copies of p and s (B.p32, B.s32)
 template <typename VT>
-static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, cudaStream_t s) {
+static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, int vec64,
+                              cudaStream_t s) {
   const int n = B.n, G = vec_grid(n);
-  const int vec64 = sizeof(VT) == 8;
+  cf* p32 = vec64 == 2 ? (cf*)B.p32 : nullptr;
+  cf* s32 = vec64 == 2 ? (cf*)B.s32 : nullptr;
   KState* st = B.state;
   // partials: xr / init write slots [0, G) of rpart; the matvec gathers write the per-leaf slots
   double* rpart = B.partials + (size_t)DP.nleaf * 5;
   note_launch();
   kf_p<VT><<<G, kVecThreads, 0, s>>>(st, rpart, G, n, (const cplx<VT>*)B.r, (cplx<VT>*)B.p, (cplx<VT>*)B.v,
-                                     (cplx<VT>*)B.rhat);
+                                     (cplx<VT>*)B.rhat, p32);
   MatvecEpilogue e1;
   e1.dot_a = B.rhat;
   e1.partials = B.partials;
   e1.red5 = B.red5;
-  launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s);
+  launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s, p32);
   note_launch();
-  kf_s<VT><<<G, kVecThreads, 0, s>>>(st, B.red5, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v, (cplx<VT>*)B.s);
+  kf_s<VT><<<G, kVecThreads, 0, s>>>(st, B.red5, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v, (cplx<VT>*)B.s,
+                                     s32);
   MatvecEpilogue e2;
   e2.dot_b = B.s;
   e2.partials = B.partials;
   e2.red5 = B.red5;
-  launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s);
+  launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s, s32);
   note_launch();
   kf_xr<VT><<<G, kVecThreads, 0, s>>>(st, B.red5, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p,
                                       (const cplx<VT>*)B.s, (cplx<VT>*)B.r, (const cplx<VT>*)B.t,
@@ -378,9 +394,9 @@ void krylov_enqueue_iterations(const KrylovBufs& B, const DevPartition& DP, cons
                                int count, cudaStream_t s) {
   for (int i = 0; i < count; i++) {
     if (vec64)
-      enqueue_iteration<double>(B, DP, H, tr, s);
+      enqueue_iteration<double>(B, DP, H, tr, vec64, s);
     else
-      enqueue_iteration<float>(B, DP, H, tr, s);
+      enqueue_iteration<float>(B, DP, H, tr, 0, s);
   }
 }
 
@@ -394,6 +410,11 @@ void launch_to32(int n, const void* a, void* b, cudaStream_t s) {
 void launch_add32(int n, void* x, const void* d, cudaStream_t s) {
   note_launch();
   k_add32<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)x, (const cf*)d);
+  AC3D_CUDA(cudaGetLastError());
+}
+void launch_add64(int n, void* x, const void* d, cudaStream_t s) {
+  note_launch();
+  k_add64<<<vec_grid(n), kVecThreads, 0, s>>>(n, (cd*)x, (const cd*)d);
   AC3D_CUDA(cudaGetLastError());
 }
 void launch_copy64(int n, const void* a, void* b, cudaStream_t s) {

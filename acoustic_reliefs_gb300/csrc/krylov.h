@@ -32,6 +32,7 @@ struct KrylovBufs {
   int nparts_r = 0;            // number of partials feeding the rho step (vector grid)
   int nleaf = 0;
   double* red5 = nullptr;      // fixed-order totals of the latest matvec's dot partials
+  void *p32 = nullptr, *s32 = nullptr;  // FP32 shadows of p and s (FP64 vectors on FP32 storage)
   KState* state = nullptr;
 };
 
@@ -41,9 +42,11 @@ void krylov_enqueue_iterations(const KrylovBufs& B, const DevPartition& DP, cons
 int krylov_vec_grid(int n);
 
 void launch_matvec_ex(const DevPartition& DP, const DevHMat& H, bool transposed, int vec64, const void* x, void* y,
-                      const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s);
+                      const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s,
+                      const void* x32 = nullptr);
 void launch_to32(int n, const void* a, void* b, cudaStream_t s);
 void launch_add32(int n, void* x, const void* d, cudaStream_t s);
+void launch_add64(int n, void* x, const void* d, cudaStream_t s);
 void launch_copy64(int n, const void* a, void* b, cudaStream_t s);
 void launch_zero64(int n, void* b, cudaStream_t s);
 void launch_negate64(int n, void* a, cudaStream_t s);

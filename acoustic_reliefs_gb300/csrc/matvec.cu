@@ -521,13 +521,14 @@ void prepare_matvec_kernels() {
   std::call_once(once, [] {
     set_smem_attrs<float, float, float>();
     set_smem_attrs<float, double, df32>();
+    set_smem_attrs<float, double, float>();
     set_smem_attrs<double, double, double>();
   });
 }
 
 template <typename MT, typename VT, typename AT, int RPL>
 static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* x, void* y, const void* bminus,
-                 const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s) {
+                 const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s, const void* x32) {
   SegView v;
   v.leaf_start = DP.leaf_start.as<int>();
   v.a_seg = DP.near_seg.as<long long>();
@@ -542,8 +543,9 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
   const cplx<MT>* vseg = H.vseg.as<cplx<MT>>();
   cplx<AT>* t = (cplx<AT>*)tvec;
   cplx<AT>* p = H.pbuf.as<cplx<AT>>();
-  // column multipliers taken from x, in the accumulator type
-  const cplx<AT>* xm = (const cplx<AT>*)x;
+  // column multipliers taken from x in the accumulator type: x itself, its FP32 shadow x32 (FP64
+  // vectors on FP32 arithmetic) or its double-float copy
+  const cplx<AT>* xm = x32 ? (const cplx<AT>*)x32 : (const cplx<AT>*)x;
   if constexpr (std::is_same<AT, df32>::value) {
     note_launch();
     to_df_kernel<<<(DP.ne + 255) / 256, 256, 0, s>>>(DP.ne, (const cd*)x, H.xdf.as<cplx<df32>>());
@@ -584,35 +586,42 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
 
 template <typename MT, typename VT, typename AT>
 static void mv_rpl(const DevPartition& DP, const DevHMat& H, bool tr, const void* x, void* y, const void* bminus,
-                   const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s) {
+                   const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s, const void* x32) {
   const int rpl = (DP.max_leaf + 31) / 32;
   if (rpl <= 1)
-    mv_t<MT, VT, AT, 1>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
+    mv_t<MT, VT, AT, 1>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
   else if (rpl <= 2)
-    mv_t<MT, VT, AT, 2>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
+    mv_t<MT, VT, AT, 2>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
   else if (rpl <= 4)
-    mv_t<MT, VT, AT, 4>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
+    mv_t<MT, VT, AT, 4>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
   else
-    mv_t<MT, VT, AT, 8>(DP, H, tr, x, y, bminus, ep, done, tvec, s);
+    mv_t<MT, VT, AT, 8>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
 }
 
+// vec64: 0 FP32 vectors; 1 FP64 vectors (FP64 storage: FP64 arithmetic; FP32 storage: the
+// double-float residual); 2 FP64 vectors on FP32 storage with FP32 arithmetic, the multipliers
+// taken from the FP32 shadow x32 of x
 void launch_matvec_ex(const DevPartition& DP, const DevHMat& H, bool transposed, int vec64, const void* x, void* y,
-                      const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s) {
+                      const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s,
+                      const void* x32) {
   if (H.prec == PREC_FP64) {
     if (!vec64) throw Error(3, "internal: FP64 H-matrix needs FP64 vectors");
-    mv_rpl<double, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
+    mv_rpl<double, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s, nullptr);
+  } else if (vec64 == 2) {
+    if (!x32) throw Error(3, "internal: FP32 shadow of the matvec input missing");
+    mv_rpl<float, double, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s, x32);
   } else if (vec64) {
     // FP32 H-matrix with FP64 vectors (refinement residuals): double-float arithmetic
-    mv_rpl<float, double, df32>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s);
+    mv_rpl<float, double, df32>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s, nullptr);
   } else {
-    mv_rpl<float, float, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s);
+    mv_rpl<float, float, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s, nullptr);
   }
 }
 
 void launch_matvec(const DevPartition& DP, const DevHMat& H, int ne, bool transposed, int vec64, const void* x,
                    void* y, const void* b_minus, const MatvecEpilogue& ep, cudaStream_t s) {
   (void)ne;
-  launch_matvec_ex(DP, H, transposed, vec64, x, y, b_minus, ep, nullptr, s);
+  launch_matvec_ex(DP, H, transposed, vec64, x, y, b_minus, ep, nullptr, s, nullptr);
 }
 
 int matvec_grid(const DevPartition& DP, bool) { return DP.nleaf; }
