@@ -10,8 +10,15 @@
 
 namespace ac3d {
 
-constexpr int kStages = 3;
-constexpr int kStageBytes = 16384;        // 16 KB per stage (multiple of 16)
+// Ring shape (stages x bytes); the defaults were chosen by measurement on GB300.
+#ifndef AC3D_RING_STAGES
+#define AC3D_RING_STAGES 3
+#endif
+#ifndef AC3D_STAGE_BYTES
+#define AC3D_STAGE_BYTES 16384
+#endif
+constexpr int kStages = AC3D_RING_STAGES;
+constexpr int kStageBytes = AC3D_STAGE_BYTES;  // bytes per stage (multiple of 16)
 constexpr uint32_t kSpinLimit = 1u << 26; // polls before a wait is declared failed
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
