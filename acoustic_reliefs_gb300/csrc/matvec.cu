@@ -209,15 +209,23 @@ __global__ void __launch_bounds__(256) seg_reduce_kernel(const int* __restrict__
 // Gather pass: y[leaf rows] = -x/2 + S_A x[a_idx] + S_B t[b_idx] (+ transposed dense blocks), or
 // b - that; optional fused FP64 dot partials (conj(a).y, conj(y).b, |y|^2) per leaf.
 //
-// The segments stream through the copy ring in chunks of at most kThreads columns. Together with
-// each chunk's bulk copy, every thread gathers one column multiplier (x[idx] or t[idx]) into the
-// stage's multiplier buffer with cp.async; the stage's mbarrier expects the bulk copy's bytes plus
-// one arrival per thread, so a stage is ready only when its columns and multipliers have both
-// landed, kStages chunks after they were requested. The column index for the next refill is
-// loaded one chunk ahead. The compute uses the dot pass's layout: G lanes per column, each lane
-// summing RPG rows, 32 / G columns per warp step; the column slots of a warp are summed at the end.
+// Warp-specialised: kWarps consumer warps compute, one producer warp feeds the copy ring. The
+// segments stream in chunks of at most kThreads columns. For each chunk the producer waits until
+// the consumers have released the stage (its "empty" mbarrier, one arrival per consumer warp),
+// gathers the chunk's column multipliers (x[idx] or t[idx]; each lane up to 8 columns, indices
+// loaded one chunk ahead) into the stage's multiplier buffer with cp.async, and issues the bulk
+// copy; the stage's "full" mbarrier expects the copy's bytes and one arrival per producer lane.
+// Consumers never wait for each other within the streaming loop. A padding column (index -1) is
+// zero in the segment, so it gathers any valid multiplier (element 0). The compute uses the dot
+// pass's layout: G lanes per column, each lane summing RPG rows, 32 / G columns per warp step.
+constexpr int kGatherThreads = kThreads + 32;
+#ifndef AC3D_GATHER_MIN_CTAS
+#define AC3D_GATHER_MIN_CTAS 4
+#endif
+constexpr int kProdCols = 8;  // multiplier columns per producer lane (kThreads / 32)
+
 template <typename MT, typename VT, typename AT, bool TRANS, int RPL>
-__global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
+__global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gather_kernel(
     SegView V, const cplx<MT>* __restrict__ near, const cplx<MT>* __restrict__ lrseg, const cplx<AT>* __restrict__ t,
     const cplx<VT>* __restrict__ x, const cplx<AT>* __restrict__ xm, cplx<VT>* __restrict__ y,
     const cplx<VT>* __restrict__ bminus,
@@ -226,10 +234,13 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   constexpr int G = DotShape<RPL>::G, RPG = DotShape<RPL>::RPG;
   constexpr int CPW = 32 / G;         // columns per warp step
   constexpr int STEP = kWarps * CPW;  // columns per CTA step
+  static_assert(kProdCols * 32 == kThreads, "producer lanes cover a chunk");
   extern __shared__ __align__(128) unsigned char dsmem[];
   __shared__ bool s_last;
+  __shared__ int s_fail;
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ __align__(8) uint64_t empty[kStages];
   __shared__ __align__(16) unsigned char zraw[kStages * kThreads * sizeof(cplx<AT>)];
   auto zbuf = reinterpret_cast<cplx<AT>(*)[kThreads]>(zraw);
   __shared__ double sdot[kWarps][5];
@@ -245,7 +256,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   const int* b_idx = V.b_idx + V.b_kptr[leaf];
   const cplx<MT>* a_ptr = TRANS ? nullptr : near + V.a_seg[leaf];
   const cplx<MT>* b_ptr = lrseg + V.b_seg[leaf];
-  // columns per chunk: even (16-byte aligned chunks), at most one multiplier per thread
+  // columns per chunk: even (16-byte aligned chunks), at most kThreads
   const int cpc = min(kThreads, max(2, (int)(kStageBytes / sizeof(cplx<MT>)) / R & ~1));
   const int na = (a_cols + cpc - 1) / cpc, nb = (b_cols + cpc - 1) / cpc;
   const int nch = na + nb;
@@ -272,92 +283,98 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
     }
     return k;
   };
-  // this thread's column index in chunk c (-1: none or padding)
-  auto col_index = [&](int c) { 
-    if (c >= nch) return -1;
-    const Chunk k = chunk(c);
-    return tid < k.ncols ? k.idx[tid] : -1;
-  };
-  // issue this thread's part of chunk c into stage s: multiplier gather, then its arrival
-  auto issue = [&](int c, int s, int zi) {
-    const Chunk k = chunk(c);
-    if (tid < k.ncols) {
-      if (zi >= 0)
-        cp_async_elem<sizeof(cplx<AT>)>(&zbuf[s][tid], k.z + zi);
-      else
-        zbuf[s][tid] = cplx<AT>();
-    }
-    cp_async_arrive_noinc(&full[s]);
-    if (tid == 0) {
-      const uint32_t bytes = (uint32_t)(k.ncols * R * sizeof(cplx<MT>));
-      mbar_expect_tx(&full[s], bytes);
-      bulk_copy_g2s(stage[s], k.src, bytes, &full[s]);
-    }
-  };
 
   if (tid == 0) {
-    for (int st = 0; st < kStages; st++) mbar_init(&full[st], 1 + kThreads);
+    for (int st = 0; st < kStages; st++) {
+      mbar_init(&full[st], 1 + 32);
+      mbar_init(&empty[st], kWarps);
+    }
+    s_fail = 0;
     fence_barrier_init();
   }
   __syncthreads();
-  {
-    int zi[kStages];
-#pragma unroll
-    for (int c = 0; c < kStages; c++) zi[c] = col_index(c);
-#pragma unroll
-    for (int c = 0; c < kStages; c++)
-      if (c < nch) issue(c, c, zi[c]);
-  }
-  int next_zi = col_index(kStages);  // column index of the next refill, loaded one chunk ahead
 
   AT ar[RPG], ai[RPG];
 #pragma unroll
   for (int q = 0; q < RPG; q++) ar[q] = ai[q] = 0;
-  bool ok = true;
-  int c = 0;
-  for (; c < nch; c++) {
-    const int s = c % kStages;
-    const bool got = mbar_wait_bounded(&full[s], (uint32_t)(c / kStages) & 1u);
-    if (__syncthreads_or(!got)) {
-      ok = false;
-      break;
+  if (warp == kWarps) {
+    // ---- producer warp
+    int nidx[kProdCols];
+    auto load_idx = [&](int c) {
+#pragma unroll
+      for (int u = 0; u < kProdCols; u++) nidx[u] = -1;
+      if (c < nch) {
+        const Chunk k = chunk(c);
+#pragma unroll
+        for (int u = 0; u < kProdCols; u++) {
+          const int col = lane + 32 * u;
+          if (col < k.ncols) nidx[u] = k.idx[col];
+        }
+      }
+    };
+    load_idx(0);
+    int c = 0;
+    for (; c < nch; c++) {
+      const int s = c % kStages;
+      if (c >= kStages) {
+        const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], (uint32_t)(c / kStages - 1) & 1u));
+        if (!got) {
+          if (lane == 0) atomicExch(&s_fail, 1);
+          break;
+        }
+      }
+      const Chunk k = chunk(c);
+#pragma unroll
+      for (int u = 0; u < kProdCols; u++) {
+        const int col = lane + 32 * u;
+        if (col < k.ncols) cp_async_elem<sizeof(cplx<AT>)>(&zbuf[s][col], k.z + max(nidx[u], 0));
+      }
+      cp_async_arrive_noinc(&full[s]);
+      if (lane == 0) {
+        fence_proxy_async();
+        const uint32_t bytes = (uint32_t)(k.ncols * R * sizeof(cplx<MT>));
+        mbar_expect_tx(&full[s], bytes);
+        bulk_copy_g2s(stage[s], k.src, bytes, &full[s]);
+      }
+      load_idx(c + 1);
     }
-    const int ncols = chunk(c).ncols;
-    const cplx<MT>* S = (const cplx<MT>*)stage[s];
-    const cplx<AT>* Z = zbuf[s];
-    for (int jb = warp * CPW; jb < ncols; jb += 2 * STEP) {
+    // every copy issued has landed before the CTA reuses or leaves the ring
+    cp_async_wait_all();
+    if (lane == 0)
+      for (int cc = max(0, c - kStages); cc < c; cc++) mbar_wait_bounded(&full[cc % kStages], (uint32_t)(cc / kStages) & 1u);
+  } else {
+    // ---- consumer warps
+    for (int c = 0; c < nch; c++) {
+      const int s = c % kStages;
+      const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (uint32_t)(c / kStages) & 1u));
+      if (!got) {
+        if (lane == 0) atomicExch(&s_fail, 1);
+        break;
+      }
+      const int ncols = chunk(c).ncols;
+      const cplx<MT>* S = (const cplx<MT>*)stage[s];
+      const cplx<AT>* Z = zbuf[s];
+      for (int jb = warp * CPW; jb < ncols; jb += 2 * STEP) {
 #pragma unroll
-      for (int u = 0; u < 2; u++) {
-        const int j = jb + slot + u * STEP;
-        if (j < ncols) {
-          const cplx<AT> z = Z[j];
-          const cplx<MT>* col = S + j * R;
+        for (int u = 0; u < 2; u++) {
+          const int j = jb + slot + u * STEP;
+          if (j < ncols) {
+            const cplx<AT> z = Z[j];
+            const cplx<MT>* col = S + j * R;
 #pragma unroll
-          for (int q = 0; q < RPG; q++) {
-            const int row = g + G * q;
-            if (row < R) acc_mac(ar[q], ai[q], col[row], z.re, z.im);
+            for (int q = 0; q < RPG; q++) {
+              const int row = g + G * q;
+              if (row < R) acc_mac(ar[q], ai[q], col[row], z.re, z.im);
+            }
           }
         }
       }
-    }
-    __syncthreads();  // stage s and its multipliers are consumed
-    if (c + kStages < nch) {
-      fence_proxy_async();
-      const int zi = next_zi;
-      next_zi = col_index(c + kStages + 1);
-      issue(c + kStages, s, zi);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);  // this warp is done with stage s
     }
   }
-  if (!ok) {
-    // record the failure and let the copies already issued land before the CTA exits
-    if (tid == 0) {
-      atomicExch(V.err, 1);
-      for (int cc = c; cc < min(nch, c + kStages); cc++)
-        mbar_wait_bounded(&full[cc % kStages], (uint32_t)(cc / kStages) & 1u);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-  }
+  __syncthreads();
+  if (s_fail && tid == 0) atomicExch(V.err, 1);
   // sum the column slots of the warp: lanes with equal g hold the same rows
 #pragma unroll
   for (int o = G; o < 32; o <<= 1)
@@ -369,8 +386,8 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   // per-warp row sums in the ring memory (all stages are consumed), then the transposed dense
   // blocks below this column leaf, read column-wise (lane = column of the leaf)
   cplx<AT>* part = (cplx<AT>*)stage;
-  __syncthreads();
-  if (slot == 0) {
+  const bool consumer = warp < kWarps;
+  if (consumer && slot == 0) {
 #pragma unroll
     for (int q = 0; q < RPG; q++) {
       const int row = g + G * q;
@@ -378,7 +395,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
     }
   }
   __syncwarp();
-  if (TRANS) {
+  if (TRANS && consumer) {
     AT tr[RPL], ti[RPL];
 #pragma unroll
     for (int jr = 0; jr < RPL; jr++) tr[jr] = ti[jr] = 0;
@@ -441,7 +458,7 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
   }
   if (partials) {
     for (int i = 0; i < 5; i++) d[i] = warp_sum(d[i]);
-    if (lane == 0)
+    if (lane == 0 && consumer)
       for (int i = 0; i < 5; i++) sdot[warp][i] = d[i];
     __syncthreads();
     if (tid < 5) {
@@ -458,11 +475,12 @@ __global__ void __launch_bounds__(kThreads, 4) seg_gather_kernel(
       if (s_last) {
         __threadfence();
         double acc[5] = {0, 0, 0, 0, 0};
-        for (int l = tid; l < (int)gridDim.x; l += kThreads)
-          for (int i = 0; i < 5; i++) acc[i] += __ldcg(&partials[(size_t)l * 5 + i]);
+        if (consumer)
+          for (int l = tid; l < (int)gridDim.x; l += kThreads)
+            for (int i = 0; i < 5; i++) acc[i] += __ldcg(&partials[(size_t)l * 5 + i]);
         for (int i = 0; i < 5; i++) acc[i] = warp_sum(acc[i]);
         __syncthreads();
-        if (lane == 0)
+        if (lane == 0 && consumer)
           for (int i = 0; i < 5; i++) sdot[warp][i] = acc[i];
         __syncthreads();
         if (tid < 5) {
@@ -574,11 +592,11 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
   v.order = tr ? H.order_cols.as<int>() : H.order_rows.as<int>();
   note_launch();
   if (tr)
-    seg_gather_kernel<MT, VT, AT, true, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
+    seg_gather_kernel<MT, VT, AT, true, RPL><<<DP.nleaf, kGatherThreads, kRingBytes, s>>>(
         v, H.near.as<cplx<MT>>(), vseg, t, (const cplx<VT>*)x, xm, (cplx<VT>*)y, (const cplx<VT>*)bminus,
         (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
   else
-    seg_gather_kernel<MT, VT, AT, false, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(
+    seg_gather_kernel<MT, VT, AT, false, RPL><<<DP.nleaf, kGatherThreads, kRingBytes, s>>>(
         v, H.near.as<cplx<MT>>(), useg, t, (const cplx<VT>*)x, xm, (cplx<VT>*)y, (const cplx<VT>*)bminus,
         (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
   AC3D_CUDA(cudaGetLastError());
