@@ -302,6 +302,14 @@ __device__ __forceinline__ void warp_argmax(R& val, int& idx) {
   }
 }
 
+// One out-of-line copy of the far-field entry for the warp kernel: its rows-per-lane loops are
+// unrolled, and inlining the 6-point evaluation (with sincos) at every unrolled site made the code
+// outgrow the instruction cache.
+template <typename R, typename P4>
+__device__ __noinline__ cplx<R> entry_far_call(R k, const GeoView<R>* G, P4 p, int e) {
+  return entry_far<R>(k, *G, p, e);
+}
+
 template <typename R>
 __device__ __forceinline__ R warp_sum_r(R v) {
 #pragma unroll
@@ -397,7 +405,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) aca_warp_kernel(A
     for (int k = 0; k < LPL; k++) {
       const int c = lane + 32 * k;
       if (c < n) {
-        cplx<R> v = entry_far<R>(A.k, A.G, pi, cs + c);
+        cplx<R> v = entry_far_call<R, P4>(A.k, &A.G, pi, cs + c);
         sub_terms(v, uq, A.pool, toff, (long long)m + c, nst);
         v_l[k] = v;
         const R a = abs2(v);
@@ -435,7 +443,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) aca_warp_kernel(A
     for (int k = 0; k < LPL; k++) {
       const int r = lane + 32 * k;
       if (r < m) {
-        cplx<R> u = entry_far<R>(A.k, A.G, A.rowpts[rs + r], cs + j);
+        cplx<R> u = entry_far_call<R, P4>(A.k, &A.G, A.rowpts[rs + r], cs + j);
         sub_terms(u, vq, A.pool, toff, (long long)r, nst);
         u_l[k] = u;
         unew[r] = u;
