@@ -48,7 +48,8 @@ SIGNATURES = {
     "ac3d_gradient": (_I, [_P, _P, _P, _P]),
     "ac3d_value_dev": (_I, [_P, _P, _P, _P]),
     "ac3d_gradient_dev": (_I, [_P, _P, _P, _P, _P]),
-    "ac3d_sphere": (_I, [_P, _I, _P, _I, _D, _I, _D, _I, _P]),
+    "ac3d_sphere": (_I, [_P, _I, _P, _I, _D, _I, _D, _I, _I, _P]),
+    "ac3d_set_actual": (_I, [_P, _I]),
     "ac3d_get_stats": (_I, [_P, _P]),
     "ac3d_matvec_timing": (_I, [_P, _I, _I, _P, _P]),
     "ac3d_far_field_noalloc": (_I, [_P, _I, _P, _I, _P, _D, _P, _I, _P, _P]),

@@ -60,7 +60,7 @@ class DiffBEM:
         self._h = h
         self._bands = list(bands)
         self.silent = False
-        self.use_actual = False
+        self._use_actual = False
         self._Hs: dict[int, int] = {}
         self._Ps = None
         self._Es = None
@@ -83,9 +83,15 @@ class DiffBEM:
     def _check(self, rc):
         _L.check(self._h, rc)
 
-    def _actual_unsupported(self):
-        if self.use_actual:
-            raise NotImplementedError("use_actual (dense QR path) is not provided by the GPU build")
+    @property
+    def use_actual(self) -> bool:
+        """acoustics3d.h:49: coefficient and gradient calls on the exact (all-dense, FP64) operator."""
+        return self._use_actual
+
+    @use_actual.setter
+    def use_actual(self, on) -> None:
+        self._check(_L.lib().ac3d_set_actual(self._h, int(bool(on))))
+        self._use_actual = bool(on)
 
     # -- extensions -----------------------------------------------------------------------------
     def set_precision(self, precision: str) -> None:
@@ -153,7 +159,6 @@ class DiffBEM:
 
     def value(self, x=None) -> float:
         """acoustics3d.cpp:109-160: band-mean diffusion coefficient (optionally at heights x)."""
-        self._actual_unsupported()
         c = ctypes.c_double()
         xx = None if x is None else _f64(x)
         self._check(_L.lib().ac3d_value(self._h, _L.ptr(xx), ctypes.byref(c)))
@@ -161,21 +166,18 @@ class DiffBEM:
 
     def band_value(self, freq_band) -> float:
         """acoustics3d.cpp:162-176."""
-        self._actual_unsupported()
         c = ctypes.c_double()
         self._check(_L.lib().ac3d_band_value(self._h, float(freq_band), ctypes.byref(c)))
         return c.value
 
     def values(self) -> list:
         """acoustics3d.cpp:178-197."""
-        self._actual_unsupported()
         out = np.zeros(len(self._bands))
         self._check(_L.lib().ac3d_values(self._h, _L.ptr(out)))
         return [float(v) for v in out]
 
     def gradient(self, x):
         """acoustics3d.cpp:199-234: (c, dc/dx), both summed over bands."""
-        self._actual_unsupported()
         xx = _f64(x)
         g = np.zeros(len(xx))
         c = ctypes.c_double()
@@ -185,13 +187,11 @@ class DiffBEM:
     def value_dev(self, x_ptr: int | None, c_ptr: int, stream: int = 0) -> None:
         """value(x) with x (HH float64, or None for the stored heights) and c (one float64) in device
         memory, ordered on the CUDA stream handle `stream`; c is the band mean."""
-        self._actual_unsupported()
         self._check(_L.lib().ac3d_value_dev(self._h, ctypes.c_void_p(x_ptr or 0), ctypes.c_void_p(c_ptr),
                                             ctypes.c_void_p(stream)))
 
     def gradient_dev(self, x_ptr: int, c_ptr: int, grad_ptr: int, stream: int = 0) -> None:
         """gradient(x) with x, c and grad (HH float64) in device memory; c and grad band-summed."""
-        self._actual_unsupported()
         self._check(_L.lib().ac3d_gradient_dev(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(c_ptr),
                                                ctypes.c_void_p(grad_ptr), ctypes.c_void_p(stream)))
 
@@ -291,9 +291,9 @@ class DiffBEM:
 
 def sphere(sphere_mesh, freq, LL=100, lrad=10, actual=False, *, precision: str = "fp64") -> np.ndarray:
     """sphere.h:28-85: scattered pressure of a plane wave e^{-ikx} on a mesh read from an OBJ path
-    (or given as an (Ps, Es) tuple), at LL receivers on a circle of radius lrad in the xz plane."""
-    if actual:
-        raise NotImplementedError("actual=True (dense QR path) is not provided by the GPU build")
+    (or given as an (Ps, Es) tuple), at LL receivers on a circle of radius lrad in the xz plane.
+    actual=True solves the exact operator (every leaf pair a dense FP64 block, BiCGSTAB to 1e-12)
+    where the reference uses a dense QR solve."""
     if isinstance(sphere_mesh, (tuple, list)):
         Ps, Es = sphere_mesh
     else:
@@ -303,7 +303,7 @@ def sphere(sphere_mesh, freq, LL=100, lrad=10, actual=False, *, precision: str =
     Es = _i32(Es).reshape(-1, 3)
     out = np.zeros(2 * int(LL))
     rc = _L.lib().ac3d_sphere(_L.ptr(Ps), len(Ps), _L.ptr(Es), len(Es), float(freq), int(LL), float(lrad),
-                              _PREC[precision], _L.ptr(out))
+                              _PREC[precision], int(bool(actual)), _L.ptr(out))
     if rc != _L.OK:
         raise AC3DError(rc, "sphere evaluation failed")
     return _cplx(out)

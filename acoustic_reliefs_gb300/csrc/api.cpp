@@ -449,24 +449,26 @@ void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   // matvec arithmetic on FP32 shadows of p and s), inside FP64 iterative refinement
   KrylovBufs B = bufs(c, 2);
   launch_zero64(n, x, s);
-  // x = 0: the first residual is b itself
+  // x = 0: the first residual is b itself. |b|^2 is read back without a wait (the first inner
+  // tolerance does not depend on it), so the host captures the inner solve's graph while the
+  // device still runs the assembly.
   launch_copy64(n, b, c->r64.p, s);
   const int nb = launch_norm2_64(n, b, c->partials.as<double>(), s);
   launch_reduce5(c->partials.as<double>(), nb, c->red.as<double>(), s);
-  AC3D_CUDA(cudaMemcpyAsync(c->h_red, c->red.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
-  AC3D_CUDA(cudaStreamSynchronize(s));
-  double bn2 = c->h_red[4];
-  double rn2 = bn2;
+  AC3D_CUDA(cudaMemcpyAsync(&c->h_red[5], c->red.as<double>() + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
+  double bn2 = 0.0, rn2 = 0.0;
   int outer = 0;
-  while (outer < c->max_outer && rn2 > tol * tol * bn2) {
+  while (outer < c->max_outer) {
     launch_copy64(n, c->r64.p, B.b, s);
-    double need = tol * std::sqrt(bn2 / rn2);
-    double tin = std::max(c->inner_tol, 0.3 * need);
-    int it = run_krylov(c, H, B, tr, 2, tin, &done);
+    const double need = outer == 0 ? tol : tol * std::sqrt(bn2 / rn2);
+    const double tin = std::max(c->inner_tol, 0.3 * need);
+    int it = run_krylov(c, H, B, tr, 2, tin, &done);  // ends with the stream synchronised
+    if (outer == 0) bn2 = c->h_red[5];
     c->stats.iterations += it;
     launch_add64(n, x, B.x, s);
     rn2 = reduce_norm2_residual(c, H, tr, b, x, c->r64.as<cd>());
     outer++;
+    if (rn2 <= tol * tol * bn2) break;
     if (done == 3 && it == 0) break;
   }
   c->stats.outer_steps += outer;
@@ -1001,6 +1003,7 @@ void ac3d_destroy(ac3d_ctx* c) {
                     &c->d_pair_touch, &c->d_touch};
   for (DevBuf* b : bufs) b->release();
   c->m.reset();  // a mesh shared with other contexts stays alive until its last user goes
+  c->m_dense.reset();
   if (c->side) {
     cudaStreamSynchronize(c->side);
     cudaStreamDestroy(c->side);
@@ -1068,6 +1071,9 @@ int ac3d_set_mesh(ac3d_ctx* c, const double* Ps, int V, const int32_t* Es, int N
   return guard(c, [&] {
     c->mesh_set = false;
     c->diff_set = false;
+    c->m_dense.reset();
+    c->Ps_in.assign(Ps, Ps + 3 * (size_t)V);
+    c->Es_in.assign(Es, Es + 3 * (size_t)Ne);
     std::shared_ptr<MeshState> m = build_mesh_state(Ps, V, Es, Ne, c->cluster_size, c->radius_factor, c->maxk,
                                                     c->stream);
     c->m = std::move(m);
@@ -1312,10 +1318,61 @@ int ac3d_surface_values(ac3d_ctx* c, double f, double* out) {
   });
 }
 
+// use_actual (adjoint.cpp:33-83,148-170): the reference builds the dense boundary and receiver
+// matrices and solves by QR. Here the coefficient / gradient calls run, for their duration, on
+// the same tree with every leaf pair a dense block, in FP64, with the exact receiver product and
+// BiCGSTAB to 1e-12 in place of the direct solve (pvals and surface_vals, as in the reference,
+// keep the H-matrix).
+constexpr double kActualTol = 1e-12;
+constexpr double kDenseFactor = 1e300;  // no pair of clusters is admissible
+
+int ac3d_set_actual(ac3d_ctx* c, int on) {
+  if (!c) return AC3D_ERR_ARG;
+  c->actual = on != 0;
+  return AC3D_OK;
+}
+
+struct ActualScope {
+  ac3d_ctx* c;
+  bool on;
+  std::shared_ptr<MeshState> m;
+  int prec = 0, listener = 0;
+  double tol = 0;
+  explicit ActualScope(ac3d_ctx* cc) : c(cc), on(cc->actual && cc->mesh_set) {
+    if (!on) return;
+    if (!c->m_dense) {
+      auto d = build_mesh_state(c->Ps_in.data(), c->m->V, c->Es_in.data(), c->m->Ne, c->cluster_size, kDenseFactor,
+                                c->maxk, c->stream);
+      if (d->Es != c->m->Es) throw Error(AC3D_ERR_STATE, "internal: dense partition has another element order");
+      c->m_dense = std::move(d);
+    }
+    if (c->m_dense->Ps0 != c->m->Ps0) {  // follow set_points
+      c->m_dense->Ps0 = c->m->Ps0;
+      c->m_dense->geom_base = false;
+    }
+    m = c->m;
+    prec = c->prec;
+    listener = c->listener_mode;
+    tol = c->solver_tol;
+    c->m = c->m_dense;
+    c->prec = AC3D_PREC_FP64;
+    c->listener_mode = AC3D_LISTENER_DENSE;
+    c->solver_tol = std::min(tol, kActualTol);
+  }
+  ~ActualScope() {
+    if (!on) return;
+    c->m = m;
+    c->prec = prec;
+    c->listener_mode = listener;
+    c->solver_tol = tol;
+  }
+};
+
 int ac3d_band_value(ac3d_ctx* c, double fb, double* cv) {
   if (!c || !cv) return AC3D_ERR_ARG;
   return guard(c, [&] {
     require_mesh(c);
+    ActualScope as(c);
     reset_stats(c);
     ensure_base_geometry(c);
     *cv = band_eval(c, fb, true, nullptr);
@@ -1326,6 +1383,7 @@ int ac3d_values(ac3d_ctx* c, double* out) {
   if (!c || !out) return AC3D_ERR_ARG;
   return guard(c, [&] {
     require_mesh(c);
+    ActualScope as(c);
     reset_stats(c);
     ensure_base_geometry(c);
     for (size_t b = 0; b < c->bands.size(); b++) out[b] = band_eval(c, c->bands[b], true, nullptr);
@@ -1336,6 +1394,7 @@ int ac3d_value(ac3d_ctx* c, const double* x, double* cv) {
   if (!c || !cv) return AC3D_ERR_ARG;
   return guard(c, [&] {
     require_mesh(c);
+    ActualScope as(c);
     reset_stats(c);
     upload_points(*c->m, heights_to_points(c, x), c->stream);
     c->m->geom_base = x == nullptr;
@@ -1351,6 +1410,7 @@ int ac3d_gradient(ac3d_ctx* c, const double* x, double* cv, double* grad) {
     require_mesh(c);
     if (!c->diff_set)
       throw Error(AC3D_ERR_STATE, "No differentiable points set. Set them using set_diff_pts or precompute.");
+    ActualScope as(c);
     reset_stats(c);
     cudaStream_t s = c->stream;
     upload_points(*c->m, heights_to_points(c, x), c->stream);
@@ -1371,6 +1431,7 @@ int ac3d_value_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, void* stream
   if (!c || !c_dev) return AC3D_ERR_ARG;
   return guard(c, [&] {
     require_mesh(c);
+    ActualScope as(c);
     cudaStream_t us = (cudaStream_t)stream;
     cudaStream_t s = c->stream;
     cudaEvent_t ev;
@@ -1404,6 +1465,7 @@ int ac3d_gradient_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, double* g
     require_mesh(c);
     if (!c->diff_set)
       throw Error(AC3D_ERR_STATE, "No differentiable points set. Set them using set_diff_pts or precompute.");
+    ActualScope as(c);
     cudaStream_t us = (cudaStream_t)stream;
     cudaStream_t s = c->stream;
     cudaEvent_t ev;
@@ -1429,13 +1491,16 @@ int ac3d_gradient_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, double* g
 }
 
 int ac3d_sphere(const double* Ps, int V, const int32_t* Es, int Ne, double freq, int LL, double lrad, int precision,
-                double* out) {
+                int actual, double* out) {
   if (!Ps || !Es || !out || LL < 1) return AC3D_ERR_ARG;
   const double band = freq;
   const double src[3] = {1.0, 0.0, 0.0};
   ac3d_ctx* c = nullptr;
-  // sphere.h:32,43,51: leaf 128, factor 1.5, tolerances 1e-10
-  int rc = ac3d_create(&c, 128, 1.5, &band, 1, 1, 1e-10, 1e-10, 1e-10, src, 1.0, 5.0, 0);
+  // sphere.h:32,43,51: leaf 128, factor 1.5, tolerances 1e-10. actual (sphere.h:65-69, dense QR):
+  // every leaf pair a dense block, FP64, BiCGSTAB to 1e-12
+  int rc = actual ? ac3d_create(&c, 128, kDenseFactor, &band, 1, 1, 1e-10, 1e-10, kActualTol, src, 1.0, 5.0, 0)
+                  : ac3d_create(&c, 128, 1.5, &band, 1, 1, 1e-10, 1e-10, 1e-10, src, 1.0, 5.0, 0);
+  if (actual) precision = AC3D_PREC_FP64;
   if (rc) return rc;
   std::vector<int32_t> Eo(3 * (size_t)Ne);
   std::vector<double> L(3 * (size_t)LL, 0.0);
@@ -1510,22 +1575,23 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     cudaStream_t s = c->stream;
     const DevHMat& H = *c->last_H;
     ensure_work(c);
-    const int vec64 = H.prec == PREC_FP64 ? 1 : 0;
+    // the variant the solve runs: FP64 vectors on the FP64 H-matrix; FP64 vectors with their FP32
+    // shadows (FP32 arithmetic) on the FP32 H-matrix
+    const int vec64 = H.prec == PREC_FP64 ? 1 : 2;
     KrylovBufs B = bufs(c, vec64);
-    // x = the last solution rounded to the vector precision, y = scratch
-    if (vec64)
-      launch_copy64(c->m->Ne, c->x64.p, B.p, s);
-    else
-      launch_to32(c->m->Ne, c->x64.p, B.p, s);
+    // x = the last solution, y = scratch
+    launch_copy64(c->m->Ne, c->x64.p, B.p, s);
+    if (vec64 == 2) launch_to32(c->m->Ne, c->x64.p, B.p32, s);
     MatvecEpilogue ep;
-    launch_matvec(c->m->DP, H, c->m->Ne, transposed != 0, vec64, B.p, B.v, nullptr, ep, s);  // warm-up
+    auto one = [&] {
+      launch_matvec_ex(c->m->DP, H, transposed != 0, vec64, B.p, B.v, nullptr, ep, nullptr, s, B.p32);
+    };
+    one();  // warm-up
     cudaEvent_t e0, e1;
     AC3D_CUDA(cudaEventCreate(&e0));
     AC3D_CUDA(cudaEventCreate(&e1));
     AC3D_CUDA(cudaEventRecord(e0, s));
-    for (int i = 0; i < iters; i++)
-      launch_matvec(c->m->DP, H, c->m->Ne, transposed != 0, vec64, (i & 1) ? B.v : B.p, (i & 1) ? B.t : B.v, nullptr, ep,
-                    s);
+    for (int i = 0; i < iters; i++) one();
     AC3D_CUDA(cudaEventRecord(e1, s));
     AC3D_CUDA(cudaEventSynchronize(e1));
     float t = 0;
@@ -1533,8 +1599,9 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms = t / iters;
-    const long long es = vec64 ? 16 : 8;
-    *bytes = (c->m->P.near_total + H.lr_entries) * es + 2LL * c->m->Ne * es;
+    // stored entries once; x (FP64) read and y (FP64) written once; the FP32 shadow read once
+    const long long es = H.prec == PREC_FP64 ? 16 : 8;
+    *bytes = (c->m->P.near_total + H.lr_entries) * es + c->m->Ne * (32LL + (vec64 == 2 ? 8 : 0));
   });
 }
 

@@ -33,6 +33,7 @@ struct ac3d_ctx {
   int max_outer = 10;
   int chunk = 8;           // BiCGSTAB iterations per captured graph launch
   int maxk = 100;          // APPROX_ACA_MAX_K (constants.h:16)
+  bool actual = false;     // use_actual: the coefficient / gradient calls run on the exact operator
 
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;                 // concurrent assembly work
@@ -43,6 +44,11 @@ struct ac3d_ctx {
   // mesh (shared with a server's other slots when the context serves requests)
   bool mesh_set = false, diff_set = false;
   std::shared_ptr<ac3d::MeshState> m = std::make_shared<ac3d::MeshState>();
+  // use_actual: the same tree with every leaf pair a dense block (built on first use from the
+  // set_mesh inputs, so that the element order is the H-matrix state's)
+  std::shared_ptr<ac3d::MeshState> m_dense;
+  std::vector<double> Ps_in;
+  std::vector<int32_t> Es_in;
   std::vector<double> Ls;   // receivers for value/gradient
   ac3d::DevBuf Ls_dev;
   // differentiable points

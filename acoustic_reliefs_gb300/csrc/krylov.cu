@@ -10,6 +10,7 @@
 #include "common.cuh"
 #include "internal.h"
 #include "krylov.h"
+#include "launch.cuh"
 
 namespace ac3d {
 
@@ -157,6 +158,8 @@ template <typename VT>
 __global__ void __launch_bounds__(kVecThreads) kf_p(KState* st, const double* partials, int nparts, int n,
                                                     const cplx<VT>* __restrict__ r, cplx<VT>* p, cplx<VT>* v,
                                                     cplx<VT>* rhat, cf* p32) {
+  grid_dep_wait();  // programmatic launch: the preceding kernel has completed past this point
+  grid_dep_launch();
   if (st->done) return;
   // the scalars once per CTA (FP64 division is slow): every CTA gets the same values
   __shared__ RhoStep so;
@@ -204,6 +207,8 @@ template <typename VT>
 __global__ void __launch_bounds__(kVecThreads) kf_s(KState* st, const double* red5, int n,
                                                     const cplx<VT>* __restrict__ r, const cplx<VT>* __restrict__ v,
                                                     cplx<VT>* s, cf* s32) {
+  grid_dep_wait();  // programmatic launch: the preceding kernel has completed past this point
+  grid_dep_launch();
   if (st->done) return;
   __shared__ double sa[3];
   if (threadIdx.x == 0) {
@@ -236,6 +241,8 @@ __global__ void __launch_bounds__(kVecThreads) kf_xr(KState* st, const double* r
                                                      const cplx<VT>* __restrict__ p, const cplx<VT>* __restrict__ s,
                                                      cplx<VT>* r, const cplx<VT>* __restrict__ t,
                                                      const cplx<VT>* __restrict__ rhat, double* out_partials) {
+  grid_dep_wait();  // programmatic launch: the preceding kernel has completed past this point
+  grid_dep_launch();
   if (st->done) return;
   __shared__ double sw[2];
   __shared__ bool s_last;
@@ -343,36 +350,40 @@ static int vec_grid(int n) {
 
 // vec64: 0 FP32 vectors; 1 FP64 vectors and FP64 matvec arithmetic (FP64 storage); 2 FP64 vectors,
 // FP32 storage and FP32 matvec arithmetic on FP32 shadow copies of p and s (B.p32, B.s32)
+// All launches but the first of a captured chunk are programmatic dependents of the kernel
+// before them (launch.cuh): each kernel's set-up overlaps the end of the previous one.
+#ifndef AC3D_PDL
+#define AC3D_PDL 1
+#endif
+constexpr bool kPdl = AC3D_PDL != 0;
+
+
 template <typename VT>
 static void enqueue_iteration(const KrylovBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, int vec64,
-                              cudaStream_t s) {
+                              bool first, cudaStream_t s) {
   const int n = B.n, G = vec_grid(n);
   cf* p32 = vec64 == 2 ? (cf*)B.p32 : nullptr;
   cf* s32 = vec64 == 2 ? (cf*)B.s32 : nullptr;
   KState* st = B.state;
   // partials: xr / init write slots [0, G) of rpart; the matvec gathers write the per-leaf slots
   double* rpart = B.partials + (size_t)DP.nleaf * 5;
-  note_launch();
-  kf_p<VT><<<G, kVecThreads, 0, s>>>(st, rpart, G, n, (const cplx<VT>*)B.r, (cplx<VT>*)B.p, (cplx<VT>*)B.v,
-                                     (cplx<VT>*)B.rhat, p32);
+  launch_k(kPdl && !first, kf_p<VT>, dim3(G), dim3(kVecThreads), 0, s, st, (const double*)rpart, G, n, (const cplx<VT>*)B.r,
+           (cplx<VT>*)B.p, (cplx<VT>*)B.v, (cplx<VT>*)B.rhat, p32);
   MatvecEpilogue e1;
   e1.dot_a = B.rhat;
   e1.partials = B.partials;
   e1.red5 = B.red5;
-  launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s, p32);
-  note_launch();
-  kf_s<VT><<<G, kVecThreads, 0, s>>>(st, B.red5, n, (const cplx<VT>*)B.r, (const cplx<VT>*)B.v, (cplx<VT>*)B.s,
-                                     s32);
+  launch_matvec_ex(DP, H, tr, vec64, B.p, B.v, nullptr, e1, &st->done, s, p32, kPdl);
+  launch_k(kPdl, kf_s<VT>, dim3(G), dim3(kVecThreads), 0, s, st, (const double*)B.red5, n, (const cplx<VT>*)B.r,
+           (const cplx<VT>*)B.v, (cplx<VT>*)B.s, s32);
   MatvecEpilogue e2;
   e2.dot_b = B.s;
   e2.partials = B.partials;
   e2.red5 = B.red5;
-  launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s, s32);
-  note_launch();
-  kf_xr<VT><<<G, kVecThreads, 0, s>>>(st, B.red5, n, (cplx<VT>*)B.x, (const cplx<VT>*)B.p,
-                                      (const cplx<VT>*)B.s, (cplx<VT>*)B.r, (const cplx<VT>*)B.t,
-                                      (const cplx<VT>*)B.rhat, rpart);
-  AC3D_CUDA(cudaGetLastError());
+  launch_matvec_ex(DP, H, tr, vec64, B.s, B.t, nullptr, e2, &st->done, s, s32, kPdl);
+  launch_k(kPdl, kf_xr<VT>, dim3(G), dim3(kVecThreads), 0, s, st, (const double*)B.red5, n, (cplx<VT>*)B.x,
+           (const cplx<VT>*)B.p, (const cplx<VT>*)B.s, (cplx<VT>*)B.r, (const cplx<VT>*)B.t, (const cplx<VT>*)B.rhat,
+           rpart);
 }
 
 void krylov_enqueue_init(const KrylovBufs& B, int vec64, double tol, int maxit, cudaStream_t s) {
@@ -394,9 +405,9 @@ void krylov_enqueue_iterations(const KrylovBufs& B, const DevPartition& DP, cons
                                int count, cudaStream_t s) {
   for (int i = 0; i < count; i++) {
     if (vec64)
-      enqueue_iteration<double>(B, DP, H, tr, vec64, s);
+      enqueue_iteration<double>(B, DP, H, tr, vec64, i == 0, s);
     else
-      enqueue_iteration<float>(B, DP, H, tr, 0, s);
+      enqueue_iteration<float>(B, DP, H, tr, 0, i == 0, s);
   }
 }
 

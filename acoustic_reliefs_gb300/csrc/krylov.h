@@ -43,7 +43,7 @@ int krylov_vec_grid(int n);
 
 void launch_matvec_ex(const DevPartition& DP, const DevHMat& H, bool transposed, int vec64, const void* x, void* y,
                       const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s,
-                      const void* x32 = nullptr);
+                      const void* x32 = nullptr, bool pdl = false);
 void launch_to32(int n, const void* a, void* b, cudaStream_t s);
 void launch_add32(int n, void* x, const void* d, cudaStream_t s);
 void launch_add64(int n, void* x, const void* d, cudaStream_t s);

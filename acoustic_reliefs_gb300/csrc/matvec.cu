@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "launch.cuh"
 #include "segstream.cuh"
 
 namespace ac3d {
@@ -90,6 +91,8 @@ __device__ __forceinline__ double acc_to<double, df32>(df32 v) { return (double)
 
 // x (FP64) -> double-float multipliers
 __global__ void to_df_kernel(int n, const cd* __restrict__ x, cplx<df32>* out) {
+  grid_dep_wait();
+  grid_dep_launch();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const cd v = x[i];
@@ -118,24 +121,37 @@ __global__ void __launch_bounds__(kThreads, 4) seg_dot_kernel(SegView V, const c
   extern __shared__ __align__(128) unsigned char dsmem[];
   auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(dsmem);
   __shared__ __align__(8) uint64_t full[kStages];
-  if (done && *done) return;
+  // the segments and the partition are not written by any kernel of a solve: the first stages
+  // stream in before the wait for the preceding kernel (which writes x and the done flag)
   const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
-  if (K == 0) return;
+  // a set done flag stays set for the rest of the solve, so reading it before the wait can only
+  // miss a flag that is being set (checked again after the wait)
+  if (K == 0 || (done && *(volatile const int*)done)) {
+    grid_dep_wait();
+    grid_dep_launch();
+    return;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane % G, slot = lane / G;
   AT xr[RPG], xi[RPG];
-#pragma unroll
-  for (int t = 0; t < RPG; t++) {
-    const int row = g + G * t;
-    const cplx<AT> v = row < R ? xm[ls + row] : cplx<AT>();
-    xr[t] = v.re;
-    xi[t] = v.im;
-  }
   init_ring(full);
   cplx<AT>* out = p + k0;
-  stream_leaf<MT>(stage, full, R, nullptr, 0, lrseg + V.b_seg[leaf], K, V.err,
+  auto after_prefetch = [&]() -> bool {
+    grid_dep_wait();
+    grid_dep_launch();
+    if (done && *done) return false;
+#pragma unroll
+    for (int t = 0; t < RPG; t++) {
+      const int row = g + G * t;
+      const cplx<AT> v = row < R ? xm[ls + row] : cplx<AT>();
+      xr[t] = v.re;
+      xi[t] = v.im;
+    }
+    return true;
+  };
+  stream_leaf<MT>(stage, full, R, nullptr, 0, lrseg + V.b_seg[leaf], K, V.err, after_prefetch,
                   [&](const cplx<MT>* S, int, int c0, int ncols, int, int, int) {
                     // two columns per lane in flight: j and j + STEP
                     for (int jb = warp * CPW; jb < ncols; jb += 2 * STEP) {
@@ -178,6 +194,8 @@ __global__ void __launch_bounds__(256) seg_reduce_kernel(const int* __restrict__
                                                          const int* __restrict__ kpos,
                                                          const cplx<AT>* __restrict__ p, cplx<AT>* __restrict__ t,
                                                          const int* __restrict__ done) {
+  grid_dep_wait();
+  grid_dep_launch();
   if (done && *done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ntask_cap || i >= *t_total) return;
@@ -186,6 +204,21 @@ __global__ void __launch_bounds__(256) seg_reduce_kernel(const int* __restrict__
   const int e0 = ent_ptr[b], e1 = ent_ptr[b + 1];
   AT sr = 0, si = 0;
   int e = e0;
+  // batches of 16: every load of a batch is issued before its first add (a block spans up to a
+  // few hundred leaves); the adds keep the entry order, so any batching gives the same sums
+  for (; e + 15 < e1; e += 16) {
+    int kk[16];
+#pragma unroll
+    for (int u = 0; u < 16; u++) kk[u] = kpos[e + u];
+    cplx<AT> v[16];
+#pragma unroll
+    for (int u = 0; u < 16; u++) v[u] = p[kk[u] + q];
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      sr = acc_add(sr, v[u].re);
+      si = acc_add(si, v[u].im);
+    }
+  }
   for (; e + 3 < e1; e += 4) {
     const int k0 = kpos[e], k1 = kpos[e + 1], k2 = kpos[e + 2], k3 = kpos[e + 3];
     const cplx<AT> v0 = p[k0 + q], v1 = p[k1 + q], v2 = p[k2 + q], v3 = p[k3 + q];
@@ -244,7 +277,14 @@ __global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gath
   __shared__ __align__(16) unsigned char zraw[kStages * kThreads * sizeof(cplx<AT>)];
   auto zbuf = reinterpret_cast<cplx<AT>(*)[kThreads]>(zraw);
   __shared__ double sdot[kWarps][5];
-  if (done && *done) return;
+  // Under a programmatic launch this kernel may start while the reduce pass (which writes t) runs;
+  // the kernels before that one (x, the done flag) have completed. The next kernel may be
+  // scheduled at once: it waits for this grid to complete before it reads anything.
+  grid_dep_launch();
+  if (done && *done) {
+    grid_dep_wait();
+    return;
+  }
   const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -316,6 +356,7 @@ __global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gath
     int c = 0;
     for (; c < nch; c++) {
       const int s = c % kStages;
+      if (c == na) grid_dep_wait();  // region B multipliers come from the preceding kernel
       if (c >= kStages) {
         const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], (uint32_t)(c / kStages - 1) & 1u));
         if (!got) {
@@ -338,6 +379,7 @@ __global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gath
       }
       load_idx(c + 1);
     }
+    if (c <= na) grid_dep_wait();  // no region B chunk was issued
     // every copy issued has landed before the CTA reuses or leaves the ring
     cp_async_wait_all();
     if (lane == 0)
@@ -546,7 +588,7 @@ void prepare_matvec_kernels() {
 
 template <typename MT, typename VT, typename AT, int RPL>
 static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* x, void* y, const void* bminus,
-                 const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s, const void* x32) {
+                 const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s, const void* x32, bool pdl) {
   SegView v;
   v.leaf_start = DP.leaf_start.as<int>();
   v.a_seg = DP.near_seg.as<long long>();
@@ -565,9 +607,8 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
   // vectors on FP32 arithmetic) or its double-float copy
   const cplx<AT>* xm = x32 ? (const cplx<AT>*)x32 : (const cplx<AT>*)x;
   if constexpr (std::is_same<AT, df32>::value) {
-    note_launch();
-    to_df_kernel<<<(DP.ne + 255) / 256, 256, 0, s>>>(DP.ne, (const cd*)x, H.xdf.as<cplx<df32>>());
-    AC3D_CUDA(cudaGetLastError());
+    launch_k(pdl, to_df_kernel, dim3((DP.ne + 255) / 256), dim3(256), 0, s, DP.ne, (const cd*)x,
+             H.xdf.as<cplx<df32>>());
     xm = H.xdf.as<cplx<df32>>();
   }
   if (DP.na > 0) {
@@ -576,70 +617,66 @@ static void mv_t(const DevPartition& DP, const DevHMat& H, bool tr, const void* 
     d.b_seg = tr ? H.seg_f.as<long long>() : H.seg_t.as<long long>();
     d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
     d.order = tr ? H.order_rows.as<int>() : H.order_cols.as<int>();
-    note_launch();
-    seg_dot_kernel<MT, AT, RPL><<<DP.nleaf, kThreads, kRingBytes, s>>>(d, tr ? useg : vseg, xm, p, done);
-    AC3D_CUDA(cudaGetLastError());
-    note_launch();
-    seg_reduce_kernel<AT><<<(int)((H.task_cap + 255) / 256), 256, 0, s>>>(
-        H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na,
-        tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(), p, t,
-        done);
-    AC3D_CUDA(cudaGetLastError());
+    launch_k(pdl, seg_dot_kernel<MT, AT, RPL>, dim3(DP.nleaf), dim3(kThreads), kRingBytes, s, d,
+             tr ? useg : vseg, xm, p, done);
+    launch_k(pdl, seg_reduce_kernel<AT>, dim3((int)((H.task_cap + 255) / 256)), dim3(256), 0, s,
+             H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na,
+             tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(),
+             p, t, done);
   }
   v.b_seg = tr ? H.seg_t.as<long long>() : H.seg_f.as<long long>();
   v.b_kptr = tr ? H.kseg_t.as<int>() : H.kseg_f.as<int>();
   v.b_idx = tr ? H.vidx.as<int>() : H.uidx.as<int>();
   v.order = tr ? H.order_cols.as<int>() : H.order_rows.as<int>();
-  note_launch();
-  if (tr)
-    seg_gather_kernel<MT, VT, AT, true, RPL><<<DP.nleaf, kGatherThreads, kRingBytes, s>>>(
-        v, H.near.as<cplx<MT>>(), vseg, t, (const cplx<VT>*)x, xm, (cplx<VT>*)y, (const cplx<VT>*)bminus,
-        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
-  else
-    seg_gather_kernel<MT, VT, AT, false, RPL><<<DP.nleaf, kGatherThreads, kRingBytes, s>>>(
-        v, H.near.as<cplx<MT>>(), useg, t, (const cplx<VT>*)x, xm, (cplx<VT>*)y, (const cplx<VT>*)bminus,
-        (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
-  AC3D_CUDA(cudaGetLastError());
+  const cplx<AT>* tc = t;
+  // the gather reads x and the done flag before its wait, which needs the dot and reduce passes
+  // between it and the kernel that wrote them; without low-rank blocks it is an ordinary launch
+  launch_k(pdl && DP.na > 0, tr ? seg_gather_kernel<MT, VT, AT, true, RPL> : seg_gather_kernel<MT, VT, AT, false, RPL>,
+           dim3(DP.nleaf), dim3(kGatherThreads), kRingBytes, s, v, (const cplx<MT>*)H.near.as<cplx<MT>>(),
+           tr ? vseg : useg, tc, (const cplx<VT>*)x, xm, (cplx<VT>*)y, (const cplx<VT>*)bminus,
+           (const cplx<VT>*)ep.dot_a, (const cplx<VT>*)ep.dot_b, ep.partials, ep.red5, H.ticket.as<unsigned>(), done);
 }
 
 template <typename MT, typename VT, typename AT>
 static void mv_rpl(const DevPartition& DP, const DevHMat& H, bool tr, const void* x, void* y, const void* bminus,
-                   const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s, const void* x32) {
+                   const MatvecEpilogue& ep, const int* done, void* tvec, cudaStream_t s, const void* x32,
+                   bool pdl) {
   const int rpl = (DP.max_leaf + 31) / 32;
   if (rpl <= 1)
-    mv_t<MT, VT, AT, 1>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
+    mv_t<MT, VT, AT, 1>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32, pdl);
   else if (rpl <= 2)
-    mv_t<MT, VT, AT, 2>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
+    mv_t<MT, VT, AT, 2>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32, pdl);
   else if (rpl <= 4)
-    mv_t<MT, VT, AT, 4>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
+    mv_t<MT, VT, AT, 4>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32, pdl);
   else
-    mv_t<MT, VT, AT, 8>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32);
+    mv_t<MT, VT, AT, 8>(DP, H, tr, x, y, bminus, ep, done, tvec, s, x32, pdl);
 }
 
 // vec64: 0 FP32 vectors; 1 FP64 vectors (FP64 storage: FP64 arithmetic; FP32 storage: the
 // double-float residual); 2 FP64 vectors on FP32 storage with FP32 arithmetic, the multipliers
-// taken from the FP32 shadow x32 of x
+// taken from the FP32 shadow x32 of x. pdl: launch the passes as programmatic dependents (the
+// kernel before the first pass then must follow the same protocol, see launch.cuh).
 void launch_matvec_ex(const DevPartition& DP, const DevHMat& H, bool transposed, int vec64, const void* x, void* y,
                       const void* b_minus, const MatvecEpilogue& ep, const int* done, cudaStream_t s,
-                      const void* x32) {
+                      const void* x32, bool pdl) {
   if (H.prec == PREC_FP64) {
     if (!vec64) throw Error(3, "internal: FP64 H-matrix needs FP64 vectors");
-    mv_rpl<double, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s, nullptr);
+    mv_rpl<double, double, double>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s, nullptr, pdl);
   } else if (vec64 == 2) {
     if (!x32) throw Error(3, "internal: FP32 shadow of the matvec input missing");
-    mv_rpl<float, double, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s, x32);
+    mv_rpl<float, double, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s, x32, pdl);
   } else if (vec64) {
     // FP32 H-matrix with FP64 vectors (refinement residuals): double-float arithmetic
-    mv_rpl<float, double, df32>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s, nullptr);
+    mv_rpl<float, double, df32>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec64.p, s, nullptr, pdl);
   } else {
-    mv_rpl<float, float, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s, nullptr);
+    mv_rpl<float, float, float>(DP, H, transposed, x, y, b_minus, ep, done, H.tvec.p, s, nullptr, pdl);
   }
 }
 
 void launch_matvec(const DevPartition& DP, const DevHMat& H, int ne, bool transposed, int vec64, const void* x,
                    void* y, const void* b_minus, const MatvecEpilogue& ep, cudaStream_t s) {
   (void)ne;
-  launch_matvec_ex(DP, H, transposed, vec64, x, y, b_minus, ep, nullptr, s, nullptr);
+  launch_matvec_ex(DP, H, transposed, vec64, x, y, b_minus, ep, nullptr, s, nullptr, false);
 }
 
 int matvec_grid(const DevPartition& DP, bool) { return DP.nleaf; }

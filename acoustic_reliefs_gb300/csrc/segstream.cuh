@@ -118,11 +118,13 @@ struct SegView {
 // Iterates the chunks of the (up to two) regions of one leaf through the copy ring and calls
 // fn(stage_ptr, region, first_column, columns, next_region, next_first_column, next_columns) for
 // each chunk, all threads together (next_columns = 0 after the last chunk), so that the callback
-// can prefetch what the next chunk needs while it computes this one.
-template <typename MT, typename F>
+// can prefetch what the next chunk needs while it computes this one. pre() runs on all threads
+// once the first stages are in flight and before any is consumed; it returns the same value on
+// every thread, false to stop (the copies in flight land before the return).
+template <typename MT, typename P, typename F>
 __device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes], uint64_t* full, int R,
                                             const cplx<MT>* a_ptr, int a_cols, const cplx<MT>* b_ptr, int b_cols,
-                                            int* err, F&& fn) {
+                                            int* err, P&& pre, F&& fn) {
   const int cpc = max(2, (int)(kStageBytes / sizeof(cplx<MT>)) / R & ~1);  // columns per chunk, even
   const int na = (a_cols + cpc - 1) / cpc, nb = (b_cols + cpc - 1) / cpc;
   const int nch = na + nb;
@@ -148,6 +150,12 @@ __device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes],
       mbar_expect_tx(&full[c], bytes);
       bulk_copy_g2s(stage[c], src, bytes, &full[c]);
     }
+  }
+  if (!pre()) {
+    if (threadIdx.x == 0)
+      for (int c = 0; c < min(nch, kStages); c++) mbar_wait_bounded(&full[c], 0u);
+    __syncthreads();
+    return true;
   }
   bool ok = true;
   int c = 0;
@@ -189,6 +197,13 @@ __device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes],
     __syncthreads();
   }
   return ok;
+}
+
+template <typename MT, typename F>
+__device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes], uint64_t* full, int R,
+                                            const cplx<MT>* a_ptr, int a_cols, const cplx<MT>* b_ptr, int b_cols,
+                                            int* err, F&& fn) {
+  return stream_leaf<MT>(stage, full, R, a_ptr, a_cols, b_ptr, b_cols, err, [] { return true; }, fn);
 }
 
 __device__ __forceinline__ void init_ring(uint64_t* full) {

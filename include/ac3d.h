@@ -125,17 +125,25 @@ int ac3d_gradient(ac3d_ctx* ctx, const double* x, double* c, double* grad);
 int ac3d_value_dev(ac3d_ctx* ctx, const double* x_dev, double* c_dev, void* stream);
 int ac3d_gradient_dev(ac3d_ctx* ctx, const double* x_dev, double* c_dev, double* grad_dev, void* stream);
 
-/* sphere(sphere_mesh, freq, LL, lrad, actual=false) -- sphere.h:28-85, with the mesh passed as
+/* sphere(sphere_mesh, freq, LL, lrad, actual) -- sphere.h:28-85, with the mesh passed as
  * arrays instead of an OBJ path: leaf 128, factor 1.5, ACA and solver tolerance 1e-10, plane
- * wave e^{-ikx}, LL receivers on a circle of radius lrad in the xz plane. */
+ * wave e^{-ikx}, LL receivers on a circle of radius lrad in the xz plane. actual != 0 replaces the
+ * reference's dense QR solve (sphere.h:65-69) by the exact operator (every leaf pair a dense
+ * block, FP64) solved by BiCGSTAB to 1e-12. */
 int ac3d_sphere(const double* Ps, int V, const int32_t* Es, int Ne, double freq, int LL, double lrad, int precision,
-                double* out);
+                int actual, double* out);
+/* use_actual attribute (acoustics3d.h:49; adjoint.cpp:33-83,148-170): when on, band_value,
+ * values, value and gradient (and their _dev forms) run on the exact operator -- the same tree
+ * with every leaf pair a dense block, FP64, exact receiver product, BiCGSTAB to 1e-12 in place of
+ * the reference's dense QR solve. pvals and surface_vals keep the H-matrix, as in the reference. */
+int ac3d_set_actual(ac3d_ctx* ctx, int on);
 
 int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
 /* Times `iters` back-to-back H-matrix matvecs (y = op(A) x, inner-solve precision) on the
  * H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, with CUDA events on the
  * context stream. Outputs the mean milliseconds per matvec and the algorithmic bytes per matvec:
- * stored matrix entries x entry size + 16 Ne (read x, write y). No reference counterpart. */
+ * stored matrix entries x entry size + 32 Ne (read x and write y, FP64 complex), + 8 Ne for the
+ * FP32 shadow of x the mixed inner solve reads. No reference counterpart. */
 int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_matvec, long long* bytes);
 
 /* Receiver far field y_l = sum_j M(receiver l, element j) x_j (FP64), with every argument in
