@@ -11,13 +11,14 @@ The work runs on the GPU through ``libac3d.so`` (include/ac3d.h); there is no CP
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
 from . import _lib as _L
 from ._lib import AC3DError
 
-__all__ = ["DiffBEM", "sphere", "AC3DError"]
+__all__ = ["DiffBEM", "sphere", "read_obj", "write_obj", "AC3DError"]
 
 _PREC = {"mixed": _L.PREC_MIXED, "fp32": _L.PREC_MIXED, "fp64": _L.PREC_FP64}
 
@@ -289,6 +290,33 @@ class DiffBEM:
         self._bands = list(b)
 
 
+def read_obj(path: str):
+    """read_obj (read_obj.cpp:8-50) in the C++ library: (Ps (V, 3) float64, Es (Ne, 3) int32,
+    0-based). Reads "v" and triangle "f" records, including "f a/b/c" forms and negative indices;
+    skips "vn", "vt" and other records."""
+    L = _L.lib()
+    V, Ne = ctypes.c_int(), ctypes.c_int()
+    p = os.fsencode(path)
+    rc = L.ac3d_read_obj(p, None, 0, None, 0, ctypes.byref(V), ctypes.byref(Ne))
+    if rc == _L.OK:
+        Ps = np.zeros((V.value, 3))
+        Es = np.zeros((Ne.value, 3), np.int32)
+        rc = L.ac3d_read_obj(p, _L.ptr(Ps), V.value, _L.ptr(Es), Ne.value, ctypes.byref(V), ctypes.byref(Ne))
+    if rc != _L.OK:
+        raise AC3DError(rc, L.ac3d_obj_last_error().decode())
+    return Ps, Es
+
+
+def write_obj(path: str, Ps, Es) -> None:
+    """write_obj (read_obj.cpp:52-63) in the C++ library: full-precision vertices, 1-based faces."""
+    P = _f64(Ps).reshape(-1, 3)
+    E = _i32(Es).reshape(-1, 3)
+    L = _L.lib()
+    rc = L.ac3d_write_obj(os.fsencode(path), _L.ptr(P), len(P), _L.ptr(E), len(E))
+    if rc != _L.OK:
+        raise AC3DError(rc, L.ac3d_obj_last_error().decode())
+
+
 def sphere(sphere_mesh, freq, LL=100, lrad=10, actual=False, *, precision: str = "fp64") -> np.ndarray:
     """sphere.h:28-85: scattered pressure of a plane wave e^{-ikx} on a mesh read from an OBJ path
     (or given as an (Ps, Es) tuple), at LL receivers on a circle of radius lrad in the xz plane.
@@ -297,8 +325,7 @@ def sphere(sphere_mesh, freq, LL=100, lrad=10, actual=False, *, precision: str =
     if isinstance(sphere_mesh, (tuple, list)):
         Ps, Es = sphere_mesh
     else:
-        from .meshes import read_obj
-        Ps, Es = read_obj(sphere_mesh)
+        Ps, Es = read_obj(sphere_mesh)  # sphere.h:30
     Ps = _f64(Ps).reshape(-1, 3)
     Es = _i32(Es).reshape(-1, 3)
     out = np.zeros(2 * int(LL))

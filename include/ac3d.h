@@ -138,6 +138,18 @@ int ac3d_sphere(const double* Ps, int V, const int32_t* Es, int Ne, double freq,
  * the reference's dense QR solve. pvals and surface_vals keep the H-matrix, as in the reference. */
 int ac3d_set_actual(ac3d_ctx* ctx, int on);
 
+/* read_obj / write_obj -- read_obj.cpp:8-63. ac3d_read_obj reads "v" and triangle "f" records
+ * (vertex index of "a", "a/b", "a//c", "a/b/c"; negative indices relative to the vertices read so
+ * far) and skips "vn", "vt", "vp", comments and grouping / material records, where the reference
+ * rejects files that have them. With Ps and Es NULL it only sets *V and *Ne; otherwise it fills
+ * Ps (V x 3) and Es (Ne x 3, 0-based) when V_cap and Ne_cap hold the mesh (else
+ * AC3D_ERR_RESOURCE). Faces that are not triangles and indices out of range are AC3D_ERR_ARG.
+ * ac3d_write_obj writes full-precision vertices (a write / read round trip is exact) and 1-based
+ * faces. No context: ac3d_obj_last_error() gives the calling thread's last message. */
+int ac3d_read_obj(const char* path, double* Ps, int V_cap, int32_t* Es, int Ne_cap, int* V, int* Ne);
+int ac3d_write_obj(const char* path, const double* Ps, int V, const int32_t* Es, int Ne);
+const char* ac3d_obj_last_error(void);
+
 int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
 /* Times `iters` back-to-back H-matrix matvecs (y = op(A) x, inner-solve precision) on the
  * H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, with CUDA events on the
