@@ -16,17 +16,23 @@ Two modes, mirroring the store-or-recompute choice of ``recompute_matrices``:
 ``DiffBEM.value`` does (acoustics3d.cpp:128 vs :224-233). The gradient is always that of the value
 returned.
 
-``eval_uv`` / ``heights_from_texture`` restate the reference's bilinear texture sampling
-(acoustics_opt.py:24-34) in torch, so that autograd carries the gradient from vertex heights back to
-a texture (the scatter of acoustics_opt.py:43-56).
+``TexMap`` / ``eval_uv`` / ``heights_from_texture`` run the reference's bilinear texture sampling
+(acoustics_opt.py:23-33) and its transpose, the texture gradient of acoustic_gradient
+(acoustics_opt.py:44-57), as CUDA kernels of the library (``ac3d_texmap_*``), so that autograd
+carries the gradient from vertex heights back to a texture on the device; both directions are
+bitwise the reference's NumPy results.
 """
 from __future__ import annotations
 
+import ctypes
+
+import numpy as np
 import torch
 
-from .acoustics3d import DiffBEM
+from . import _lib as _L
+from .acoustics3d import AC3DError, DiffBEM
 
-__all__ = ["DiffusionCoefficient", "diffusion_coefficient", "eval_uv", "heights_from_texture"]
+__all__ = ["DiffusionCoefficient", "diffusion_coefficient", "TexMap", "eval_uv", "heights_from_texture"]
 
 
 def _run(bem: DiffBEM, h: torch.Tensor, want_grad: bool):
@@ -72,25 +78,83 @@ def diffusion_coefficient(heights: torch.Tensor, bem: DiffBEM, mode: str = "stor
     return DiffusionCoefficient.apply(heights, bem, mode, reduction)
 
 
-def eval_uv(tex: torch.Tensor, uvs: torch.Tensor) -> torch.Tensor:
-    """Bilinear sample of an (h, w) texture at (n, 2) uv coordinates, (0, 0) at the top-left texel's
-    corner, indices clamped at the far edges (acoustics_opt.py:24-34)."""
-    h, w = tex.shape
-    u = uvs[:, 0].to(tex.dtype) * w - 0.5
-    v = uvs[:, 1].to(tex.dtype) * h - 0.5
-    # numpy.modf splits toward zero; negative fractions are wrapped to 1 + f as the reference does
-    ui_t, vi_t = torch.trunc(u), torch.trunc(v)
-    uf, vf = u - ui_t, v - vi_t
-    uf = torch.where(uf < 0, 1 + uf, uf)
-    vf = torch.where(vf < 0, 1 + vf, vf)
-    ui = ui_t.to(torch.int64).clamp_min(0)
-    vi = vi_t.to(torch.int64).clamp_min(0)
-    ui1 = (ui + 1).clamp_max(w - 1)
-    vi1 = (vi + 1).clamp_max(h - 1)
-    return ((1 - vf) * (1 - uf) * tex[vi, ui] + (1 - vf) * uf * tex[vi, ui1] + vf * (1 - uf) * tex[vi1, ui] +
-            vf * uf * tex[vi1, ui1])
+class TexMap:
+    """Bilinear lookup of an (H, W) heightmap texture at fixed uv points, (0, 0) at the top-left
+    texel's corner, indices clamped at the far edges (eval_uv, acoustics_opt.py:23-33), and its
+    transpose. The texel indices and weights are built once for the uv set; ``tm(tex)`` is
+    differentiable with respect to ``tex`` (a CUDA tensor)."""
+
+    def __init__(self, uvs, shape):
+        uv = uvs.detach().cpu().numpy() if isinstance(uvs, torch.Tensor) else uvs
+        uv = np.ascontiguousarray(np.asarray(uv, dtype=np.float64).reshape(-1, 2))
+        self.H, self.W = int(shape[0]), int(shape[1])
+        self.n = len(uv)
+        h = ctypes.c_void_p()
+        rc = _L.lib().ac3d_texmap_create(ctypes.byref(h), _L.ptr(uv), self.n, self.H, self.W)
+        if rc != _L.OK:
+            raise AC3DError(rc, "invalid uvs or texture size, or no CUDA device")
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _L.lib().ac3d_texmap_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def _stream(self, t: torch.Tensor) -> int:
+        if not t.is_cuda:
+            raise ValueError("the texture must be a CUDA tensor")
+        return torch.cuda.current_stream(t.device).cuda_stream
+
+    def sample(self, tex: torch.Tensor) -> torch.Tensor:
+        """Heights (n,) FP64 from an (H, W) texture (no autograd)."""
+        t = tex.detach().to(torch.float64).contiguous()
+        if tuple(t.shape) != (self.H, self.W):
+            raise ValueError(f"texture shape {tuple(t.shape)} != {(self.H, self.W)}")
+        out = torch.empty(self.n, dtype=torch.float64, device=t.device)
+        rc = _L.lib().ac3d_texmap_sample_dev(self._h, ctypes.c_void_p(t.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                             ctypes.c_void_p(self._stream(t)))
+        if rc != _L.OK:
+            raise AC3DError(rc, "texture lookup failed")
+        return out
+
+    def scatter(self, grad: torch.Tensor) -> torch.Tensor:
+        """Texture gradient (H, W) FP64 from per-point gradients (n,)."""
+        g = grad.detach().to(torch.float64).contiguous()
+        if g.numel() != self.n:
+            raise ValueError(f"gradient length {g.numel()} != {self.n}")
+        out = torch.empty((self.H, self.W), dtype=torch.float64, device=g.device)
+        rc = _L.lib().ac3d_texmap_scatter_dev(self._h, ctypes.c_void_p(g.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                              ctypes.c_void_p(self._stream(g)))
+        if rc != _L.OK:
+            raise AC3DError(rc, "texture scatter failed")
+        return out
+
+    def __call__(self, tex: torch.Tensor) -> torch.Tensor:
+        return _TexSample.apply(tex, self)
 
 
-def heights_from_texture(tex: torch.Tensor, diff_uvs: torch.Tensor) -> torch.Tensor:
+class _TexSample(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, tex: torch.Tensor, tm: TexMap):
+        ctx.tm, ctx.dtype = tm, tex.dtype
+        return tm.sample(tex).to(tex.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        return ctx.tm.scatter(grad_out).to(ctx.dtype), None
+
+
+def eval_uv(tex: torch.Tensor, uvs) -> torch.Tensor:
+    """Bilinear sample of an (h, w) CUDA texture at (n, 2) uv coordinates (acoustics_opt.py:23-33),
+    differentiable with respect to ``tex``. Builds the lookup for ``uvs`` on each call; hold a
+    ``TexMap`` to reuse it."""
+    return TexMap(uvs, tex.shape)(tex)
+
+
+def heights_from_texture(tex: torch.Tensor, diff_uvs) -> torch.Tensor:
     """Heights of the differentiable vertices sampled from a heightmap texture (differentiable)."""
     return eval_uv(tex, diff_uvs)

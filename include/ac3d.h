@@ -150,6 +150,19 @@ int ac3d_read_obj(const char* path, double* Ps, int V_cap, int32_t* Es, int Ne_c
 int ac3d_write_obj(const char* path, const double* Ps, int V, const int32_t* Es, int Ne);
 const char* ac3d_obj_last_error(void);
 
+/* Heightmap texture -> differentiable-vertex heights and back (eval_uv, acoustics_opt.py:23-33,
+ * and the texture gradient of acoustic_gradient, acoustics_opt.py:44-57). A texmap holds, on the
+ * current device, the bilinear texel indices and weights of n uv points (n x 2, (0, 0) at the
+ * top-left texel's corner) on an H x W texture, and the transposed (texel-major) lists.
+ * ac3d_texmap_sample_dev: heights (n) from the texture (H x W row-major), both FP64 device arrays;
+ * ac3d_texmap_scatter_dev: texture gradient (H x W) from per-point gradients (n). Both are
+ * ordered on `stream` (a cudaStream_t) and give the reference's NumPy results bitwise. */
+typedef struct ac3d_texmap ac3d_texmap;
+int ac3d_texmap_create(ac3d_texmap** out, const double* uvs, int n, int H, int W);
+void ac3d_texmap_destroy(ac3d_texmap* map);
+int ac3d_texmap_sample_dev(const ac3d_texmap* map, const double* tex_dev, double* heights_dev, void* stream);
+int ac3d_texmap_scatter_dev(const ac3d_texmap* map, const double* grad_dev, double* tex_grad_dev, void* stream);
+
 int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
 /* Times `iters` back-to-back H-matrix matvecs (y = op(A) x, inner-solve precision) on the
  * H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, with CUDA events on the

@@ -1,36 +1,69 @@
-"""torch.autograd binding: texture sampling on CPU, the GPU coefficient/gradient through autograd.
+"""torch.autograd binding: the device texture lookup and its transpose, and the GPU
+coefficient / gradient through autograd.
 
-The texture lookup and its transpose are checked against the NumPy restatement of
-acoustics_opt.py:24-56 in ``meshes``; the autograd function against ``DiffBEM.gradient`` (itself
-checked against the oracle's adjoint in test_gpu_parity)."""
+The texture lookup and its transpose (ac3d_texmap_*) are checked bitwise against the NumPy
+restatement of acoustics_opt.py:23-57 in ``meshes``; the autograd function against
+``DiffBEM.gradient`` (itself checked against the oracle's adjoint in test_gpu_parity)."""
 import numpy as np
 import pytest
 import torch
 
 from acoustic_reliefs_gb300 import meshes
-from acoustic_reliefs_gb300.autograd import diffusion_coefficient, eval_uv, heights_from_texture
+from acoustic_reliefs_gb300.autograd import TexMap, diffusion_coefficient, eval_uv, heights_from_texture
 
 
 def _uvs(n, seed):
     rng = np.random.default_rng(seed)
     uv = rng.uniform(0.0001, 0.9999, size=(n, 2))
-    uv[:4] = [[0.0001, 0.0001], [0.9999, 0.9999], [0.0001, 0.9999], [0.5, 0.5]]  # corners, centre
+    # corners, centre, the texture's edges and texel centres
+    uv[:8] = [[0.0001, 0.0001], [0.9999, 0.9999], [0.0001, 0.9999], [0.5, 0.5], [0.0, 0.0], [1.0, 1.0],
+              [0.0, 1.0], [1.0 / 64, 3.0 / 64]]
     return uv
 
 
-def test_eval_uv_matches_numpy_lookup():
+@pytest.mark.gpu
+def test_eval_uv_matches_numpy_lookup(gpu_lib):
     tex = np.random.default_rng(1).uniform(0, 0.1, size=(24, 32))
     uv = _uvs(500, 2)
-    got = eval_uv(torch.from_numpy(tex), torch.from_numpy(uv)).numpy()
-    np.testing.assert_allclose(got, meshes.sample_heightmap(tex, uv), rtol=0, atol=1e-15)
+    got = eval_uv(torch.tensor(tex, device="cuda"), torch.from_numpy(uv)).cpu().numpy()
+    assert np.array_equal(got, meshes.sample_heightmap(tex, uv))
 
 
-def test_eval_uv_backward_is_reference_scatter():
-    tex = torch.from_numpy(np.random.default_rng(3).uniform(0, 0.1, size=(16, 16))).requires_grad_(True)
+@pytest.mark.gpu
+def test_eval_uv_backward_is_reference_scatter(gpu_lib):
+    tex = torch.tensor(np.random.default_rng(3).uniform(0, 0.1, size=(16, 16)), device="cuda", requires_grad=True)
     uv = _uvs(300, 4)
     w = np.random.default_rng(5).normal(size=len(uv))
-    (heights_from_texture(tex, torch.from_numpy(uv)) * torch.from_numpy(w)).sum().backward()
-    np.testing.assert_allclose(tex.grad.numpy(), meshes.scatter_to_heightmap((16, 16), uv, w), rtol=0, atol=1e-12)
+    (heights_from_texture(tex, uv) * torch.tensor(w, device="cuda")).sum().backward()
+    assert np.array_equal(tex.grad.cpu().numpy(), meshes.scatter_to_heightmap((16, 16), uv, w))
+
+
+@pytest.mark.gpu
+def test_texmap_reuse_on_the_relief(gpu_lib):
+    """A TexMap built once serves every step: the 64 x 64 relief's 4225 top vertices."""
+    R = meshes.relief_20k(0)
+    tm = TexMap(R.uvs, (64, 64))
+    for seed in range(3):
+        tex = np.random.default_rng(seed).uniform(0, 0.1, size=(64, 64))
+        h = tm.sample(torch.tensor(tex, device="cuda")).cpu().numpy()
+        assert np.array_equal(h, meshes.sample_heightmap(tex, R.uvs))
+    g = np.random.default_rng(9).normal(size=len(R.uvs))
+    assert np.array_equal(tm.scatter(torch.tensor(g, device="cuda")).cpu().numpy(),
+                          meshes.scatter_to_heightmap((64, 64), R.uvs, g))
+
+
+def test_texmap_needs_cuda_tensors():
+    """No CPU fallback: a CPU texture is rejected before any work (the library must be built)."""
+    pytest.importorskip("ctypes")
+    from acoustic_reliefs_gb300 import _lib
+    try:
+        _lib.lib()
+    except RuntimeError:
+        pytest.skip("library not built")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(Exception):
+        eval_uv(torch.zeros(4, 4, dtype=torch.float64), np.full((2, 2), 0.5))
 
 
 def _bem():
