@@ -53,6 +53,7 @@ SIGNATURES = {
     "ac3d_read_obj": (_I, [ctypes.c_char_p, _P, _I, _P, _I, _P, _P]),
     "ac3d_write_obj": (_I, [ctypes.c_char_p, _P, _I, _P, _I]),
     "ac3d_obj_last_error": (ctypes.c_char_p, []),
+    "ac3d_kernel_launches": (ctypes.c_longlong, []),
     "ac3d_texmap_create": (_I, [_P, _P, _I, _I, _I]),
     "ac3d_texmap_destroy": (None, [_P]),
     "ac3d_texmap_sample_dev": (_I, [_P, _P, _P, _P]),

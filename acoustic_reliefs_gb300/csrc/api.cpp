@@ -26,6 +26,7 @@
 namespace ac3d {
 
 std::atomic<long long> g_kernel_launches{0};
+thread_local long long t_kernel_launches = 0;
 
 void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
   if (e != cudaSuccess) {
@@ -346,12 +347,12 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   krylov_enqueue_init(B, vec64, tol, maxit, s);
   // capture one chunk of iterations as a graph and replay it until the state reports completion
   cudaGraph_t graph;
-  const long long before = g_kernel_launches.load();
+  const long long before = t_kernel_launches;
   AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   krylov_enqueue_iterations(B, c->m->DP, H, tr, vec64, c->chunk, s);
   AC3D_CUDA(cudaStreamEndCapture(s, &graph));
-  const long long nodes = g_kernel_launches.load() - before;
-  g_kernel_launches.fetch_sub(nodes);  // captured, not launched
+  const long long nodes = t_kernel_launches - before;
+  unnote_launches(nodes);  // captured, not launched
   cudaGraphExec_t exec;
   AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   AC3D_CUDA(cudaGraphDestroy(graph));
@@ -489,12 +490,12 @@ int run_block_krylov(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vec
   const int maxit = c->maxit > 0 ? c->maxit : 2 * B.n;
   mkrylov_enqueue_init(B, maxit, s);
   cudaGraph_t graph;
-  const long long before = g_kernel_launches.load();
+  const long long before = t_kernel_launches;
   AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   mkrylov_enqueue_iterations(B, c->m->DP, H, c->chunk, s);
   AC3D_CUDA(cudaStreamEndCapture(s, &graph));
-  const long long nodes = g_kernel_launches.load() - before;
-  g_kernel_launches.fetch_sub(nodes);
+  const long long nodes = t_kernel_launches - before;
+  unnote_launches(nodes);
   cudaGraphExec_t exec;
   AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   AC3D_CUDA(cudaGraphDestroy(graph));
@@ -817,10 +818,10 @@ int guard(ac3d_ctx* c, F&& f) {
   try {
     c->err.clear();
     auto t0 = std::chrono::steady_clock::now();
-    const long long l0 = g_kernel_launches.load();
+    const long long l0 = t_kernel_launches;
     f();
     c->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    c->stats.kernel_launches = g_kernel_launches.load() - l0;
+    c->stats.kernel_launches = t_kernel_launches - l0;
     return AC3D_OK;
   } catch (const Error& e) {
     c->err = e.what();
@@ -1604,6 +1605,8 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     *bytes = (c->m->P.near_total + H.lr_entries) * es + c->m->Ne * (32LL + (vec64 == 2 ? 8 : 0));
   });
 }
+
+long long ac3d_kernel_launches(void) { return g_kernel_launches.load(); }
 
 int ac3d_get_stats(const ac3d_ctx* c, ac3d_stats* out) {
   if (!c || !out) return AC3D_ERR_ARG;

@@ -14,9 +14,20 @@ namespace ac3d {
 
 constexpr double kPiHost = 3.14159265358979323846;
 
-// Kernels launched by this library (process-wide); graph replays add their captured node count.
+// Kernels launched by this library: process-wide, and by the calling thread (so that a context's
+// counts and the captured-node accounting of its graphs are not mixed with other threads');
+// graph replays add their captured node count.
 extern std::atomic<long long> g_kernel_launches;
-inline void note_launch(long long n = 1) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
+extern thread_local long long t_kernel_launches;
+inline void note_launch(long long n = 1) {
+  g_kernel_launches.fetch_add(n, std::memory_order_relaxed);
+  t_kernel_launches += n;
+}
+// A stream capture's launches were counted by note_launch but are graph nodes, not launches.
+inline void unnote_launches(long long n) {
+  g_kernel_launches.fetch_sub(n, std::memory_order_relaxed);
+  t_kernel_launches -= n;
+}
 
 // ------------------------------------------------------------------------------------------
 // Errors: host code throws; the C-ABI converts to status codes + a per-context message.

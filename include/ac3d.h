@@ -163,6 +163,10 @@ void ac3d_texmap_destroy(ac3d_texmap* map);
 int ac3d_texmap_sample_dev(const ac3d_texmap* map, const double* tex_dev, double* heights_dev, void* stream);
 int ac3d_texmap_scatter_dev(const ac3d_texmap* map, const double* grad_dev, double* tex_grad_dev, void* stream);
 
+/* Kernels this library has launched in the process so far, from every context, server slot and
+ * thread (a graph replay counts its kernel nodes). No reference counterpart. */
+long long ac3d_kernel_launches(void);
+
 int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
 /* Times `iters` back-to-back H-matrix matvecs (y = op(A) x, inner-solve precision) on the
  * H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, with CUDA events on the
