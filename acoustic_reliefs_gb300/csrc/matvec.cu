@@ -334,6 +334,7 @@ __global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gath
   }
   __syncthreads();
 
+  static_assert(32 * RPL <= kThreads, "one epilogue row per thread");
   AT ar[RPG], ai[RPG];
 #pragma unroll
   for (int q = 0; q < RPG; q++) ar[q] = ai[q] = 0;
@@ -352,18 +353,30 @@ __global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gath
         }
       }
     };
+    // the matrix chunk of a stage goes out as soon as the stage is free, ahead of its multiplier
+    // gathers (which wait for their indices): the first stages before any index load
+    auto issue_copy = [&](int cc) {
+      const Chunk k = chunk(cc);
+      const uint32_t bytes = (uint32_t)(k.ncols * R * sizeof(cplx<MT>));
+      fence_proxy_async();
+      mbar_expect_tx(&full[cc % kStages], bytes);
+      bulk_copy_g2s(stage[cc % kStages], k.src, bytes, &full[cc % kStages]);
+    };
+    if (lane == 0)
+      for (int cc = 0; cc < min(nch, kStages); cc++) issue_copy(cc);
     load_idx(0);
     int c = 0;
     for (; c < nch; c++) {
       const int s = c % kStages;
-      if (c == na) grid_dep_wait();  // region B multipliers come from the preceding kernel
       if (c >= kStages) {
         const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], (uint32_t)(c / kStages - 1) & 1u));
         if (!got) {
           if (lane == 0) atomicExch(&s_fail, 1);
           break;
         }
+        if (lane == 0) issue_copy(c);
       }
+      if (c == na) grid_dep_wait();  // region B multipliers come from the preceding kernel
       const Chunk k = chunk(c);
 #pragma unroll
       for (int u = 0; u < kProdCols; u++) {
@@ -371,12 +384,6 @@ __global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gath
         if (col < k.ncols) cp_async_elem<sizeof(cplx<AT>)>(&zbuf[s][col], k.z + max(nidx[u], 0));
       }
       cp_async_arrive_noinc(&full[s]);
-      if (lane == 0) {
-        fence_proxy_async();
-        const uint32_t bytes = (uint32_t)(k.ncols * R * sizeof(cplx<MT>));
-        mbar_expect_tx(&full[s], bytes);
-        bulk_copy_g2s(stage[s], k.src, bytes, &full[s]);
-      }
       load_idx(c + 1);
     }
     if (c <= na) grid_dep_wait();  // no region B chunk was issued
@@ -469,7 +476,8 @@ __global__ void __launch_bounds__(kGatherThreads, AC3D_GATHER_MIN_CTAS) seg_gath
   }
   __syncthreads();
   double d[5] = {0, 0, 0, 0, 0};
-  for (int r = tid; r < R; r += kThreads) {
+  if (tid < R) {
+    const int r = tid;
     AT sr = 0, si = 0;
     for (int w = 0; w < kWarps; w++) {
       sr = acc_add(sr, part[w * R + r].re);
