@@ -333,8 +333,11 @@ __device__ __forceinline__ void sub_terms(cplx<R>& acc, const cplx<R>* coef, con
   for (; p < nst; p++) cfms(acc, coef[p], pool[toff[p] + off]);
 }
 
+// Blocks of 129-256 rows (8 rows per lane) are few (less than one wave at 4 CTAs per SM), so
+// that variant takes the registers of 2 CTAs per SM and keeps its u / v rows unspilled.
 template <typename R, typename P4, int LPL>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) aca_warp_kernel(AcaArgs<R, P4> A, int nblocks) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? (LPL == 8 ? 2 : 4) : 1)
+    aca_warp_kernel(AcaArgs<R, P4> A, int nblocks) {
   __shared__ __align__(16) unsigned char s_raw[8 * kWarpAcaTerms * (2 * sizeof(cplx<R>) + sizeof(long long))];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int bi = blockIdx.x * 8 + warp;
