@@ -1584,15 +1584,17 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     launch_copy64(c->m->Ne, c->x64.p, B.p, s);
     if (vec64 == 2) launch_to32(c->m->Ne, c->x64.p, B.p32, s);
     MatvecEpilogue ep;
-    auto one = [&] {
-      launch_matvec_ex(c->m->DP, H, transposed != 0, vec64, B.p, B.v, nullptr, ep, nullptr, s, B.p32);
+    // back-to-back matvecs launched as the solve launches them: every pass after the first a
+    // programmatic dependent of the one before (x is not written, so each pass may start early)
+    auto one = [&](bool pdl) {
+      launch_matvec_ex(c->m->DP, H, transposed != 0, vec64, B.p, B.v, nullptr, ep, nullptr, s, B.p32, pdl);
     };
-    one();  // warm-up
+    one(false);  // warm-up
     cudaEvent_t e0, e1;
     AC3D_CUDA(cudaEventCreate(&e0));
     AC3D_CUDA(cudaEventCreate(&e1));
     AC3D_CUDA(cudaEventRecord(e0, s));
-    for (int i = 0; i < iters; i++) one();
+    for (int i = 0; i < iters; i++) one(i > 0);
     AC3D_CUDA(cudaEventRecord(e1, s));
     AC3D_CUDA(cudaEventSynchronize(e1));
     float t = 0;

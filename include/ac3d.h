@@ -170,7 +170,7 @@ long long ac3d_kernel_launches(void);
 int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
 /* Times `iters` back-to-back H-matrix matvecs (y = op(A) x, inner-solve precision) on the
  * H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, with CUDA events on the
- * context stream. Outputs the mean milliseconds per matvec and the algorithmic bytes per matvec:
+ * context stream; the passes are launched as in the solve (programmatic dependent launches). Outputs the mean milliseconds per matvec and the algorithmic bytes per matvec:
  * stored matrix entries x entry size + 32 Ne (read x and write y, FP64 complex), + 8 Ne for the
  * FP32 shadow of x the mixed inner solve reads. No reference counterpart. */
 int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_matvec, long long* bytes);
