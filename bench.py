@@ -363,6 +363,44 @@ class _NullCtx:
         return False
 
 
+def run_single(args):
+    """One context on one stream, one solve after another, no request-server threads: the command
+    line for kernel captures under a profiler. Prints the single-context rate, the solver
+    statistics and the matvec timing of the last solve's H-matrix."""
+    import torch
+    torch.cuda.set_device(0)
+    from acoustic_reliefs_gb300.acoustics3d import DiffBEM
+    R, Ls = workload(0)
+    bem = DiffBEM(LEAF, FACTOR, [FREQ], 1, ACA_TOL, ACA_TOL, SOLVER_TOL, precision="mixed",
+                  incident=("plane", DIRECTION), device=0)
+    bem.silent = True
+    bem.set_solver(0, args.inner_tol, 10)
+    bem.set_mesh(R.Ps, R.Es)
+    dev = torch.device("cuda", 0)
+    L = len(Ls)
+    Ls_dev = torch.tensor(Ls, dtype=torch.float64, device=dev)
+    out = torch.zeros(2 * L, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        bem.pvals_dev(FREQ, out.data_ptr(), Ls_dev.data_ptr(), L, stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        bem.pvals_dev(FREQ, out.data_ptr(), Ls_dev.data_ptr(), L, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = bem.stats()
+    mv_ms, mv_bytes = bem.matvec_timing(20)
+    print(json.dumps({"mode": "single context (kernel captures)", "workload": WORKLOAD,
+                      "solves_per_s": args.steps / (ms / 1e3), "ms_per_solve": ms / args.steps,
+                      "iterations": st["iterations"], "refinement_steps": st["outer_steps"],
+                      "rel_residual": st["rel_residual"], "ms_assemble": st["ms_assemble"],
+                      "ms_solve": st["ms_solve"], "matvec_ms": mv_ms, "matvec_bytes": int(mv_bytes)}), flush=True)
+    return 0
+
+
 def run_gpu(args):
     import torch
     world, rank, local = dist_init()
@@ -546,9 +584,13 @@ def main():
     ap.add_argument("--slots", type=int, default=4, help="server slots (concurrent requests)")
     ap.add_argument("--no-fp64-sweep", action="store_true")
     ap.add_argument("--multi-rhs", type=int, default=16, help="directions of the block-solve leg (0 to skip)")
+    ap.add_argument("--single-context", action="store_true",
+                    help="only one context on one stream (no request server): the command for kernel captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.single_context:
+        return run_single(args)
     return run_gpu(args)
 
 
