@@ -30,6 +30,7 @@ SIGNATURES = {
     "ac3d_set_incident": (_I, [_P, _I, _P]),
     "ac3d_set_listener_mode": (_I, [_P, _I]),
     "ac3d_set_solver": (_I, [_P, _I, _D, _I]),
+    "ac3d_set_krylov": (_I, [_P, _I, _I]),
     "ac3d_set_listeners": (_I, [_P, _P, _I]),
     "ac3d_set_mesh": (_I, [_P, _P, _I, _P, _I, _P]),
     "ac3d_set_diff_points": (_I, [_P, _P, _I]),
@@ -67,6 +68,7 @@ SIGNATURES = {
     "ac3d_partition_free": (None, [_P]),
     "ac3d_server_create": (_I, [ctypes.POINTER(_P), _I, _I, ctypes.c_longlong]),
     "ac3d_server_destroy": (None, [_P]),
+    "ac3d_server_set_krylov": (_I, [_P, _I, _I]),
     "ac3d_server_last_error": (ctypes.c_char_p, [_P]),
     "ac3d_server_add_mesh": (_I, [_P, _P, _I, _P, _I, _I, _D, _D, _D, _P, ctypes.POINTER(_I)]),
     "ac3d_server_submit": (_I, [_P, _I, _D, _I, _P, _P, _I, ctypes.POINTER(ctypes.c_longlong)]),

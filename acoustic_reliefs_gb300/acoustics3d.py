@@ -21,6 +21,7 @@ from ._lib import AC3DError
 __all__ = ["DiffBEM", "sphere", "read_obj", "write_obj", "AC3DError"]
 
 _PREC = {"mixed": _L.PREC_MIXED, "fp32": _L.PREC_MIXED, "fp64": _L.PREC_FP64}
+_KRYLOV = {"bicgstab": 0, "gmres": 1}
 
 
 def _f64(a, shape=None) -> np.ndarray:
@@ -112,6 +113,12 @@ class DiffBEM:
 
     def set_solver(self, max_iterations: int = 0, inner_tol: float = 1e-6, max_outer: int = 10) -> None:
         self._check(_L.lib().ac3d_set_solver(self._h, int(max_iterations), float(inner_tol), int(max_outer)))
+
+    def set_krylov(self, method: str = "gmres", restart: int = 300) -> None:
+        """Krylov method of the single right-hand-side solves: "bicgstab" (the reference's solver,
+        the default) or "gmres" (one matvec per iteration; cycles of at most `restart` iterations
+        inside the refinement loop, which checks the same relative residual)."""
+        self._check(_L.lib().ac3d_set_krylov(self._h, _KRYLOV[method], int(restart)))
 
     def set_listeners(self, listeners) -> None:
         Ls = _f64(listeners).reshape(-1, 3)

@@ -19,6 +19,7 @@
 #include "../../include/ac3d.h"
 #include "context.h"
 #include "internal.h"
+#include "gmres.h"
 #include "krylov.h"
 #include "listener.h"
 #include "multi.h"
@@ -395,6 +396,89 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   return st.iter;
 }
 
+#ifndef AC3D_GMRES_REORTH32
+#define AC3D_GMRES_REORTH32 1
+#endif
+
+// GMRES buffers of this context for the H-matrix's precision, carved from one allocation.
+GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const cd* b) {
+  GmresBufs G;
+  G.n = c->m->Ne;
+  G.m = std::max(1, std::min(c->gm_restart, G.n));
+  G.vec64 = H.prec == PREC_FP64 ? 1 : 0;
+  const size_t es = G.vec64 ? sizeof(cd) : sizeof(cf);
+  auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const size_t vb = up(((size_t)G.m + 1) * G.n * es), nb = up((size_t)G.n * es);
+  const size_t gb = up(gmres_scalar_doubles(G.m, G.n) * sizeof(double));
+  c->gm.ensure(vb + 3 * nb + gb + up(sizeof(GState)), c->stream);
+  char* p = (char*)c->gm.p;
+  G.V = p;
+  G.q = p + vb;
+  G.W = p + vb + nb;
+  G.W2 = p + vb + 2 * nb;
+  G.gd = (double*)(p + vb + 3 * nb);
+  G.state = (GState*)(p + vb + 3 * nb + gb);
+  // FP32 classical Gram-Schmidt loses orthogonality over long cycles: two passes keep the FP32
+  // cycle converging like the FP64 one
+  G.reorth = G.vec64 ? 0 : AC3D_GMRES_REORTH32;
+  G.b = (void*)b;
+  if (!c->h_gstate) AC3D_CUDA(cudaMallocHost(&c->h_gstate, 2 * sizeof(GState)));
+  return G;
+}
+
+// One GMRES cycle on op(A) d = b (complex FP64 device vectors): at most gm_restart iterations, in
+// the H-matrix's precision. Returns the iterations; the state's done code in *done.
+int run_gmres(ac3d_ctx* c, const DevHMat& H, const cd* b, cd* d, bool tr, double tol, int* done) {
+  cudaStream_t s = c->stream;
+  GmresBufs G = gmres_bufs(c, H, b);
+  // the scalars' ticket starts at zero; each reducing pass leaves it at zero
+  AC3D_CUDA(cudaMemsetAsync(G.state, 0, sizeof(GState), s));
+  gmres_enqueue_init(G, tol, s);
+  cudaGraph_t graph;
+  const long long before = t_kernel_launches;
+  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  gmres_enqueue_iterations(G, c->m->DP, H, tr, c->gm_chunk, s);
+  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
+  const long long nodes = t_kernel_launches - before;
+  unnote_launches(nodes);  // captured, not launched
+  cudaGraphExec_t exec;
+  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  AC3D_CUDA(cudaGraphDestroy(graph));
+  // keep one chunk in flight while the host reads the state after the previous one
+  const int max_launch = (G.m + c->gm_chunk - 1) / c->gm_chunk + 1;
+  int launched = 0;
+  AC3D_CUDA(cudaGraphLaunch(exec, s));
+  note_launch(nodes);
+  AC3D_CUDA(cudaMemcpyAsync(&c->h_gstate[0], G.state, sizeof(GState), cudaMemcpyDeviceToHost, s));
+  launched++;
+  cudaEvent_t ev;
+  AC3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  AC3D_CUDA(cudaEventRecord(ev, s));
+  while (true) {
+    const bool more = launched < max_launch;
+    if (more) {
+      AC3D_CUDA(cudaGraphLaunch(exec, s));
+      note_launch(nodes);
+      AC3D_CUDA(cudaMemcpyAsync(&c->h_gstate[launched & 1], G.state, sizeof(GState), cudaMemcpyDeviceToHost, s));
+    }
+    AC3D_CUDA(cudaEventSynchronize(ev));
+    const GState st = c->h_gstate[(launched - 1) & 1];
+    if (st.done || !more) break;
+    launched++;
+    AC3D_CUDA(cudaEventRecord(ev, s));
+  }
+  gmres_enqueue_finish(G, d, s);
+  GState st{};
+  AC3D_CUDA(cudaMemcpyAsync(&c->h_gstate[0], G.state, sizeof(GState), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  st = c->h_gstate[0];
+  AC3D_CUDA(cudaEventDestroy(ev));
+  AC3D_CUDA(cudaGraphExecDestroy(exec));
+  *done = st.done;
+  c->stats.matvecs += st.j;
+  return st.j;
+}
+
 double reduce_norm2_residual(ac3d_ctx* c, const DevHMat& H, bool tr, const cd* b, const cd* x, cd* r) {
   cudaStream_t s = c->stream;
   MatvecEpilogue ep;
@@ -422,12 +506,50 @@ void solve(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   check_pipeline(c, H);
 }
 
+// GMRES cycles inside the refinement loop: x = 0, then d = op(A)^{-1} r by one cycle, x += d and
+// r = b - op(A) x in FP64 (double-float arithmetic on an FP32 H-matrix) until |r| <= tol |b|. A
+// cycle runs in the H-matrix's precision; an FP32 cycle stops at inner_tol (or 0.3 of what is
+// still needed), an FP64 one at half of what is needed.
+void solve_gmres(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
+  cudaStream_t s = c->stream;
+  const int n = c->m->Ne;
+  const double tol = c->solver_tol;
+  const bool fp64 = H.prec == PREC_FP64;
+  KrylovBufs B = bufs(c, 1);  // B.x holds each cycle's correction
+  launch_zero64(n, x, s);
+  launch_copy64(n, b, c->r64.p, s);
+  const int nb = launch_norm2_64(n, b, c->partials.as<double>(), s);
+  launch_reduce5(c->partials.as<double>(), nb, c->red.as<double>(), s);
+  AC3D_CUDA(cudaMemcpyAsync(&c->h_red[5], c->red.as<double>() + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
+  double bn2 = 0.0, rn2 = 0.0;
+  int outer = 0, done = 0;
+  while (outer < c->max_outer) {
+    const double need = outer == 0 ? tol : tol * std::sqrt(bn2 / rn2);
+    const double tin = fp64 ? 0.5 * need : std::max(c->inner_tol, 0.3 * need);
+    const int it = run_gmres(c, H, c->r64.as<cd>(), (cd*)B.x, tr, tin, &done);  // ends synchronised
+    if (outer == 0) bn2 = c->h_red[5];
+    c->stats.iterations += it;
+    launch_add64(n, x, B.x, s);
+    rn2 = reduce_norm2_residual(c, H, tr, b, x, c->r64.as<cd>());
+    outer++;
+    if (rn2 <= tol * tol * bn2) break;
+    if (done == 3) break;  // non-finite values: no further cycle can help
+  }
+  c->stats.outer_steps += outer;
+  c->stats.rel_residual = bn2 > 0 ? std::sqrt(rn2 / bn2) : 0.0;
+  if (rn2 > tol * tol * bn2) c->stats.converged = 0;
+}
+
 void solve_impl(ac3d_ctx* c, DevHMat& H, const cd* b, cd* x, bool tr) {
   cudaStream_t s = c->stream;
   ensure_work(c);
   const int n = c->m->Ne;
   const double tol = c->solver_tol;
   int done = 0;
+  if (c->krylov == AC3D_KRYLOV_GMRES) {
+    solve_gmres(c, H, b, x, tr);
+    return;
+  }
   if (H.prec == PREC_FP64) {
     KrylovBufs B = bufs(c, 1);
     launch_copy64(n, b, B.b, s);
@@ -1001,7 +1123,7 @@ void ac3d_destroy(ac3d_ctx* c) {
   c->last_H.reset();
   DevBuf* bufs[] = {&c->kv, &c->kv32, &c->partials, &c->kstate, &c->red, &c->b64, &c->x64, &c->r64, &c->ff_scratch,
                     &c->adj_scratch, &c->tmp_recv, &c->Ls_dev, &c->d_h_off, &c->d_pair_elem, &c->d_pair_corner,
-                    &c->d_pair_touch, &c->d_touch};
+                    &c->d_pair_touch, &c->d_touch, &c->gm};
   for (DevBuf* b : bufs) b->release();
   c->m.reset();  // a mesh shared with other contexts stays alive until its last user goes
   c->m_dense.reset();
@@ -1055,6 +1177,14 @@ int ac3d_set_solver(ac3d_ctx* c, int max_iterations, double inner_tol, int max_o
   c->maxit = max_iterations;
   c->inner_tol = inner_tol;
   c->max_outer = max_outer;
+  return AC3D_OK;
+}
+
+int ac3d_set_krylov(ac3d_ctx* c, int method, int restart) {
+  if (!c || (method != AC3D_KRYLOV_BICGSTAB && method != AC3D_KRYLOV_GMRES) || restart < 0 || restart > 600)
+    return AC3D_ERR_ARG;
+  c->krylov = method;
+  c->gm_restart = restart > 0 ? restart : 300;
   return AC3D_OK;
 }
 
@@ -1576,12 +1706,15 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     cudaStream_t s = c->stream;
     const DevHMat& H = *c->last_H;
     ensure_work(c);
-    // the variant the solve runs: FP64 vectors on the FP64 H-matrix; FP64 vectors with their FP32
-    // shadows (FP32 arithmetic) on the FP32 H-matrix
-    const int vec64 = H.prec == PREC_FP64 ? 1 : 2;
+    // the variant the solve runs: FP64 vectors on the FP64 H-matrix; on the FP32 H-matrix FP32
+    // vectors (GMRES) or FP64 vectors with their FP32 shadows (BiCGSTAB), FP32 arithmetic
+    const int vec64 = H.prec == PREC_FP64 ? 1 : (c->krylov == AC3D_KRYLOV_GMRES ? 0 : 2);
     KrylovBufs B = bufs(c, vec64);
     // x = the last solution, y = scratch
-    launch_copy64(c->m->Ne, c->x64.p, B.p, s);
+    if (vec64 == 0)
+      launch_to32(c->m->Ne, c->x64.p, B.p, s);
+    else
+      launch_copy64(c->m->Ne, c->x64.p, B.p, s);
     if (vec64 == 2) launch_to32(c->m->Ne, c->x64.p, B.p32, s);
     MatvecEpilogue ep;
     // back-to-back matvecs launched as the solve launches them: every pass after the first a
@@ -1602,9 +1735,9 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms = t / iters;
-    // stored entries once; x (FP64) read and y (FP64) written once; the FP32 shadow read once
+    // stored entries once; x read and y written once (FP32 or FP64); the FP32 shadow read once
     const long long es = H.prec == PREC_FP64 ? 16 : 8;
-    *bytes = (c->m->P.near_total + H.lr_entries) * es + c->m->Ne * (32LL + (vec64 == 2 ? 8 : 0));
+    *bytes = (c->m->P.near_total + H.lr_entries) * es + c->m->Ne * (vec64 == 0 ? 16LL : 32LL + (vec64 == 2 ? 8 : 0));
   });
 }
 

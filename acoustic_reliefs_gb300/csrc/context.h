@@ -12,6 +12,7 @@
 #include "../../include/ac3d.h"
 #include "common.cuh"
 #include "internal.h"
+#include "gmres.h"
 #include "krylov.h"
 
 struct ac3d_ctx {
@@ -32,6 +33,9 @@ struct ac3d_ctx {
   double inner_tol = 1e-6; // floor of the relative tolerance of each FP32 inner solve
   int max_outer = 10;
   int chunk = 8;           // BiCGSTAB iterations per captured graph launch
+  int krylov = AC3D_KRYLOV_BICGSTAB;  // inner solver of the single right-hand-side solves
+  int gm_restart = 300;    // GMRES basis size: iterations per cycle before a restart
+  int gm_chunk = 16;       // GMRES iterations per captured graph launch
   int maxk = 100;          // APPROX_ACA_MAX_K (constants.h:16)
   bool actual = false;     // use_actual: the coefficient / gradient calls run on the exact operator
 
@@ -60,12 +64,15 @@ struct ac3d_ctx {
   // work buffers
   ac3d::DevBuf kv, partials, kstate, red, b64, x64, r64, ff_scratch, adj_scratch, tmp_recv;
   ac3d::DevBuf kv32;  // FP32 shadows of the Krylov p and s of the mixed-precision inner solve
+  ac3d::DevBuf gm;    // GMRES basis, matvec input / output, scalars and state
   std::unique_ptr<ac3d::DevHMat> last_H;  // H-matrix of the latest forward solve (matvec timing)
   ac3d::KState* h_state = nullptr;  // pinned
+  ac3d::GState* h_gstate = nullptr;  // pinned, two slots
   double* h_red = nullptr;    // pinned
 
   ~ac3d_ctx() {
     if (h_state) cudaFreeHost(h_state);
+    if (h_gstate) cudaFreeHost(h_gstate);
     if (h_red) cudaFreeHost(h_red);
   }
 };

@@ -1,0 +1,495 @@
+// Device-resident GMRES (Saad and Schultz 1986): Arnoldi with classical Gram-Schmidt and Givens
+// rotations, one cycle of at most m iterations per call. An option beside the reference's
+// BiCGSTAB (Eigen::BiCGSTAB at adjoint.cpp:92-95 and acoustics3d.cpp:266-269): it solves the same
+// system to the same relative residual with one matvec per iteration instead of two. Restarts are
+// the caller's refinement loop: when the basis fills before the tolerance is met, the caller forms
+// the true residual and runs another cycle on it.
+//
+// Storage: the basis vectors are kept unnormalised, V_k stored with its scale s_k = 1 / |V_k|, so
+// that the vector the update pass writes is the next matvec's input without a normalisation pass:
+//   W = A V_j;  h_kj = s_k s_j (V_k^H W);  V_{j+1} = s_j W - sum_k (h_kj s_k) V_k;
+//   h_{j+1,j} = |V_{j+1}|,  s_{j+1} = 1 / h_{j+1,j}.
+// Per iteration: the matvec (into W), a dot pass (the j + 1 dots, per-CTA partials reduced by the
+// last CTA in fixed order) and an update pass (V_{j+1}, its norm, and in the last CTA the Givens
+// rotation of the new Hessenberg column and the residual estimate |g_{j+1}|). Vectors and their
+// arithmetic, the dots and the norms are in the solve's vector type (FP32 for the mixed-precision
+// inner solve, FP64 for the FP64 solve); the Hessenberg matrix, the rotations and the scalars are
+// FP64. No atomics touch floating-point sums, so a solve is bit-reproducible.
+#include <algorithm>
+
+#include "common.cuh"
+#include "gmres.h"
+#include "internal.h"
+#include "krylov.h"
+#include "launch.cuh"
+
+namespace ac3d {
+
+namespace {
+constexpr int kGmThreads = 256;
+constexpr int kGmWarps = kGmThreads / 32;
+constexpr int kSliceMax = 1024;  // elements per CTA of the dot and update passes
+
+struct Dc {  // complex FP64 scalar arithmetic of the small dense part
+  double re, im;
+};
+__device__ __forceinline__ Dc dc(double r, double i) { return Dc{r, i}; }
+__device__ __forceinline__ Dc operator*(Dc a, Dc b) { return Dc{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ Dc operator+(Dc a, Dc b) { return Dc{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ Dc operator-(Dc a, Dc b) { return Dc{a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ Dc conjd(Dc a) { return Dc{a.re, -a.im}; }
+__device__ __forceinline__ double abs2(Dc a) { return a.re * a.re + a.im * a.im; }
+}  // namespace
+
+// FP64 arrays of a cycle, after the state struct (offsets in doubles).
+struct GmLayout {
+  int m, G;
+  __host__ __device__ size_t s() const { return 0; }                                     // m + 1
+  __host__ __device__ size_t hcol() const { return (size_t)m + 1; }                      // 2 (m + 1)
+  __host__ __device__ size_t coef() const { return hcol() + 2 * ((size_t)m + 1); }       // 2 (m + 1)
+  __host__ __device__ size_t g() const { return coef() + 2 * ((size_t)m + 1); }          // 2 (m + 1)
+  __host__ __device__ size_t cs() const { return g() + 2 * ((size_t)m + 1); }            // 2 m
+  __host__ __device__ size_t sn() const { return cs() + 2 * (size_t)m; }                 // 2 m
+  __host__ __device__ size_t R() const { return sn() + 2 * (size_t)m; }                  // 2 m m
+  __host__ __device__ size_t part() const { return R() + 2 * (size_t)m * m; }            // 2 (m + 1) G
+  __host__ __device__ size_t npart() const { return part() + 2 * ((size_t)m + 1) * G; }  // G
+  __host__ __device__ size_t total() const { return npart() + (size_t)G; }
+};
+
+// Contiguous element range of this CTA.
+__device__ __forceinline__ void gm_range(int n, int& lo, int& hi) {
+  const int per = (n + (int)gridDim.x - 1) / (int)gridDim.x;
+  lo = min(n, (int)blockIdx.x * per);
+  hi = min(n, lo + per);
+}
+
+// Last-CTA election after this CTA's partial results are written.
+__device__ __forceinline__ bool gm_last_cta(unsigned* ticket) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
+// Fixed-order sum of a run of G per-CTA partials by one warp: lanes take every 32nd partial, then
+// a fixed xor tree. The sums are in the vector type: GB300's FP64 pipe is a small fraction of its
+// FP32 rate, so bulk FP64 arithmetic would dominate these latency-bound passes.
+template <typename VT>
+__device__ __forceinline__ double warp_sum_run(const double* p, int G, int lane, int stride = 1) {
+  VT a = 0;
+  for (int c = lane; c < G; c += 32) a += (VT)__ldcg(&p[(size_t)c * stride]);
+  return (double)warp_sum(a);
+}
+
+// V_0 = b (rounded to VT), q = V_0, s_0 = 1 / |V_0|, g = (|V_0|, 0, ...).
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_init(GState* st, double* gd, int m, int n, const cd* __restrict__ b,
+                                                        cplx<VT>* V, cplx<VT>* q, double tol) {
+  const GmLayout L{m, (int)gridDim.x};
+  int lo, hi;
+  gm_range(n, lo, hi);
+  VT a = 0;
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const cd bi = b[i];
+    const cplx<VT> v((VT)bi.re, (VT)bi.im);
+    V[i] = v;
+    q[i] = v;
+    a = fma(v.re, v.re, fma(v.im, v.im, a));
+  }
+  __shared__ VT sw[kGmWarps];
+  a = warp_sum(a);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    VT t = 0;
+    for (int w = 0; w < kGmWarps; w++) t += sw[w];
+    gd[L.npart() + blockIdx.x] = (double)t;
+  }
+  if (!gm_last_cta(&st->ticket)) return;
+  if (threadIdx.x < 32) {
+    const double b2 = warp_sum_run<VT>(gd + L.npart(), L.G, threadIdx.x);
+    if (threadIdx.x == 0) {
+      const double beta = sqrt(b2);
+      st->j = 0;
+      st->m = m;
+      st->beta = beta;
+      st->tol_abs = tol * beta;
+      st->resid = beta;
+      // a zero right-hand side has the zero solution; a non-finite one cannot be solved
+      st->done = beta > 0.0 && isfinite(beta) ? 0 : (beta == 0.0 ? 1 : 3);
+      gd[L.s()] = beta > 0.0 ? 1.0 / beta : 0.0;
+      gd[L.g()] = beta;
+      gd[L.g() + 1] = 0.0;
+      st->ticket = 0u;
+    }
+  }
+}
+
+// One Gram-Schmidt pass, dots: h_k = s_k sx V_k^H X for k = 0..j, X the matvec output (sx = s_j,
+// first pass) or the first pass's result (sx = 1, second pass). Per-CTA partials over the CTA's
+// elements, each warp four vectors at a time (twenty loads in flight per lane); the last CTA sums
+// them in CTA order, sets (first pass) or adds to (second pass) the Hessenberg column and writes
+// the update coefficients h_k s_k.
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_dots(GState* st, double* gd, int m, int n,
+                                                        const cplx<VT>* __restrict__ V,
+                                                        const cplx<VT>* __restrict__ X, int second) {
+  grid_dep_wait();  // X comes from the kernel just before
+  grid_dep_launch();
+  if (st->done) return;
+  const GmLayout L{m, (int)gridDim.x};
+  const int j = st->j;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int lo, hi;
+  gm_range(n, lo, hi);
+  __shared__ cplx<VT> xs[kSliceMax];
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) xs[i - lo] = X[i];
+  __syncthreads();
+  const int len = hi - lo;
+  for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
+    VT ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
+    for (int t = lane; t < len; t += 32) {
+      const cplx<VT> x = xs[t];
+      cplx<VT> v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) v[u] = kb + u <= j ? V[(size_t)(kb + u) * n + lo + t] : cplx<VT>();
+#pragma unroll
+      for (int u = 0; u < 4; u++) {  // conj(v) x
+        ar[u] = fma(v[u].re, x.re, ar[u]);
+        ar[u] = fma(v[u].im, x.im, ar[u]);
+        ai[u] = fma(v[u].re, x.im, ai[u]);
+        ai[u] = fma(-v[u].im, x.re, ai[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      ar[u] = warp_sum(ar[u]);
+      ai[u] = warp_sum(ai[u]);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (kb + u <= j) {
+          gd[L.part() + ((size_t)(kb + u) * L.G + blockIdx.x) * 2] = (double)ar[u];
+          gd[L.part() + ((size_t)(kb + u) * L.G + blockIdx.x) * 2 + 1] = (double)ai[u];
+        }
+  }
+  if (!gm_last_cta(&st->ticket)) return;
+  const double sx = second ? 1.0 : gd[L.s() + j];
+  for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
+    VT a[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) a[u] = 0;
+    for (int c = lane; c < L.G; c += 32)
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (kb + u <= j) {
+          a[2 * u] += (VT)__ldcg(&gd[L.part() + ((size_t)(kb + u) * L.G + c) * 2]);
+          a[2 * u + 1] += (VT)__ldcg(&gd[L.part() + ((size_t)(kb + u) * L.G + c) * 2 + 1]);
+        }
+#pragma unroll
+    for (int u = 0; u < 8; u++) a[u] = warp_sum(a[u]);
+    if (lane < 4 && kb + lane <= j) {
+      const int k = kb + lane;
+      double hr = 0, hi2 = 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (u == lane) {
+          hr = (double)a[2 * u];
+          hi2 = (double)a[2 * u + 1];
+        }
+      const double sk = gd[L.s() + k];
+      hr *= sk * sx;
+      hi2 *= sk * sx;
+      if (second) {
+        gd[L.hcol() + 2 * k] += hr;
+        gd[L.hcol() + 2 * k + 1] += hi2;
+      } else {
+        gd[L.hcol() + 2 * k] = hr;
+        gd[L.hcol() + 2 * k + 1] = hi2;
+      }
+      gd[L.coef() + 2 * k] = hr * sk;
+      gd[L.coef() + 2 * k + 1] = hi2 * sk;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) st->ticket = 0u;
+}
+
+// One Gram-Schmidt pass, update: U = sx X - sum_k coef_k V_k (sx = s_j on the first pass, 1 on
+// the second). Not final: U goes to Y (the second pass's input). Final: U is V_{j+1} (also into q,
+// the next matvec's input), with |U|^2 partials; the last CTA rotates the new Hessenberg column,
+// updates the residual estimate and decides whether the cycle goes on.
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_update(GState* st, double* gd, int m, int n, cplx<VT>* V,
+                                                          const cplx<VT>* __restrict__ X, cplx<VT>* Y, cplx<VT>* q,
+                                                          int second, int final_pass) {
+  grid_dep_wait();  // the coefficients come from the dot pass just before
+  grid_dep_launch();
+  if (st->done) return;
+  const GmLayout L{m, (int)gridDim.x};
+  const int j = st->j;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  cplx<VT>* coef = reinterpret_cast<cplx<VT>*>(gsm);  // j + 1 coefficients
+  for (int k = threadIdx.x; k <= j; k += blockDim.x)
+    coef[k] = cplx<VT>((VT)gd[L.coef() + 2 * k], (VT)gd[L.coef() + 2 * k + 1]);
+  __syncthreads();
+  const VT sx = second ? VT(1) : (VT)gd[L.s() + j];
+  int lo, hi;
+  gm_range(n, lo, hi);
+  cplx<VT>* out = final_pass ? V + (size_t)(j + 1) * n : Y;
+  VT a = 0;
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const cplx<VT> x = X[i];
+    VT ur = sx * x.re, ui = sx * x.im;
+    const cplx<VT>* Vi = V + i;
+    int k = 0;
+    // sixteen loads in flight before their products; the products keep the order k = 0, 1, ...
+    for (; k + 16 <= j + 1; k += 16) {
+      cplx<VT> v[16];
+#pragma unroll
+      for (int u = 0; u < 16; u++) v[u] = Vi[(size_t)(k + u) * n];
+#pragma unroll
+      for (int u = 0; u < 16; u++) {
+        const cplx<VT> c = coef[k + u];
+        ur = fma(-c.re, v[u].re, ur);
+        ur = fma(c.im, v[u].im, ur);
+        ui = fma(-c.re, v[u].im, ui);
+        ui = fma(-c.im, v[u].re, ui);
+      }
+    }
+    for (; k <= j; k++) {
+      const cplx<VT> v = Vi[(size_t)k * n];
+      const cplx<VT> c = coef[k];
+      ur = fma(-c.re, v.re, ur);
+      ur = fma(c.im, v.im, ur);
+      ui = fma(-c.re, v.im, ui);
+      ui = fma(-c.im, v.re, ui);
+    }
+    const cplx<VT> u(ur, ui);
+    out[i] = u;
+    if (final_pass) {
+      q[i] = u;
+      a = fma(ur, ur, fma(ui, ui, a));
+    }
+  }
+  if (!final_pass) return;
+  __shared__ VT sw[kGmWarps];
+  a = warp_sum(a);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    VT t = 0;
+    for (int w = 0; w < kGmWarps; w++) t += sw[w];
+    gd[L.npart() + blockIdx.x] = (double)t;
+  }
+  if (!gm_last_cta(&st->ticket)) return;
+  // Rotate the new column h (j + 2 entries) by the earlier rotations: with x_0 = h_0,
+  //   r_i = c_i x_i + s_i h_{i+1},  x_{i+1} = conj(c_i) h_{i+1} - conj(s_i) x_i  (i < j),
+  // so the terms conj(c_i) h_{i+1} are formed in parallel and one thread runs the short chain.
+  __shared__ double nrm_s;
+  Dc* hs = reinterpret_cast<Dc*>(gsm);      // h: j + 2 entries (the coefficients are no longer needed)
+  Dc* tc = hs + (j + 2);                    // conj(c_i) h_{i+1}: j entries
+  Dc* xs = tc + j;                          // chain values x_i: j + 1 entries
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const double u2 = warp_sum_run<VT>(gd + L.npart(), L.G, threadIdx.x);
+    if (threadIdx.x == 0) nrm_s = sqrt(u2);
+  }
+  // CTA 0 of this pass completed the column before its ticket (read past L1)
+  for (int k = threadIdx.x; k <= j; k += blockDim.x)
+    hs[k] = dc(__ldcg(&gd[L.hcol() + 2 * k]), __ldcg(&gd[L.hcol() + 2 * k + 1]));
+  __syncthreads();
+  const double nrm = nrm_s;
+  if (threadIdx.x == 0) hs[j + 1] = dc(nrm, 0.0);
+  for (int i = threadIdx.x; i < j; i += blockDim.x) {
+    const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
+    tc[i] = conjd(c) * hs[i + 1];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double* snp = gd + L.sn();
+    Dc x = hs[0];
+    xs[0] = x;
+    for (int i = 0; i < j; i++) {
+      const Dc s = dc(snp[2 * i], -snp[2 * i + 1]);  // conj(s_i)
+      x = tc[i] - s * x;
+      xs[i + 1] = x;
+    }
+  }
+  __syncthreads();
+  double* R = gd + L.R() + 2 * (size_t)j * m;  // column j: rows 0..j
+  for (int i = threadIdx.x; i < j; i += blockDim.x) {
+    const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
+    const Dc s = dc(gd[L.sn() + 2 * i], gd[L.sn() + 2 * i + 1]);
+    const Dc r = c * xs[i] + s * hs[i + 1];
+    R[2 * i] = r.re;
+    R[2 * i + 1] = r.im;
+  }
+  if (threadIdx.x == 0) {
+    const Dc a0 = xs[j], b0 = hs[j + 1];
+    const double d = sqrt(abs2(a0) + abs2(b0));
+    Dc c = dc(1.0, 0.0), s = dc(0.0, 0.0);
+    if (d > 0.0) {
+      c = dc(a0.re / d, -a0.im / d);  // conj(a) / d
+      s = dc(b0.re / d, -b0.im / d);  // conj(b) / d
+    }
+    R[2 * j] = d;
+    R[2 * j + 1] = 0.0;
+    gd[L.cs() + 2 * j] = c.re;
+    gd[L.cs() + 2 * j + 1] = c.im;
+    gd[L.sn() + 2 * j] = s.re;
+    gd[L.sn() + 2 * j + 1] = s.im;
+    const Dc gj = dc(gd[L.g() + 2 * j], gd[L.g() + 2 * j + 1]);
+    const Dc g1 = dc(0.0, 0.0) - conjd(s) * gj;
+    const Dc g0 = c * gj;
+    gd[L.g() + 2 * j] = g0.re;
+    gd[L.g() + 2 * j + 1] = g0.im;
+    gd[L.g() + 2 * (j + 1)] = g1.re;
+    gd[L.g() + 2 * (j + 1) + 1] = g1.im;
+    const double res = sqrt(abs2(g1));
+    gd[L.s() + j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    st->resid = res;
+    st->j = j + 1;
+    if (!isfinite(res) || !isfinite(d) || d == 0.0)
+      st->done = (d == 0.0 && isfinite(res) && res <= st->tol_abs) ? 1 : 3;
+    else if (res <= st->tol_abs || nrm == 0.0)
+      st->done = 1;
+    else if (j + 1 >= m)
+      st->done = 2;
+    st->ticket = 0u;
+  }
+}
+
+// y = R^{-1} g over the completed columns, then coef_k = y_k s_k (one CTA).
+__global__ void __launch_bounds__(kGmThreads) k_gm_solve(const GState* st, double* gd, int m, int G) {
+  const GmLayout L{m, G};
+  const int jj = st->done == 3 ? 0 : st->j;  // a failed cycle adds nothing
+  extern __shared__ __align__(16) unsigned char gsm[];
+  Dc* gs = reinterpret_cast<Dc*>(gsm);  // jj entries
+  for (int k = threadIdx.x; k < jj; k += blockDim.x) gs[k] = dc(gd[L.g() + 2 * k], gd[L.g() + 2 * k + 1]);
+  __shared__ Dc yk;
+  __syncthreads();
+  for (int k = jj - 1; k >= 0; k--) {
+    const double* Rk = gd + L.R() + 2 * (size_t)k * m;  // column k
+    if (threadIdx.x == 0) {
+      const double d = Rk[2 * k];  // real and positive
+      yk = dc(gs[k].re / d, gs[k].im / d);
+      const double sk = gd[L.s() + k];
+      gd[L.coef() + 2 * k] = yk.re * sk;
+      gd[L.coef() + 2 * k + 1] = yk.im * sk;
+    }
+    __syncthreads();
+    const Dc y = yk;
+    for (int l = threadIdx.x; l < k; l += blockDim.x) gs[l] = gs[l] - dc(Rk[2 * l], Rk[2 * l + 1]) * y;
+    __syncthreads();
+  }
+}
+
+// x = sum_k coef_k V_k over the completed columns (FP64 output).
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_x(const GState* st, const double* gd, int m, int n,
+                                                     const cplx<VT>* __restrict__ V, cd* x) {
+  const GmLayout L{m, 1};
+  const int jj = st->done == 3 ? 0 : st->j;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  cplx<VT>* coef = reinterpret_cast<cplx<VT>*>(gsm);
+  for (int k = threadIdx.x; k < jj; k += blockDim.x)
+    coef[k] = cplx<VT>((VT)gd[L.coef() + 2 * k], (VT)gd[L.coef() + 2 * k + 1]);
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    VT ar = 0, ai = 0;
+    const cplx<VT>* Vi = V + i;
+#pragma unroll 4
+    for (int k = 0; k < jj; k++) {
+      const cplx<VT> v = Vi[(size_t)k * n];
+      const cplx<VT> c = coef[k];
+      ar = fma(c.re, v.re, ar);
+      ar = fma(-c.im, v.im, ar);
+      ai = fma(c.re, v.im, ai);
+      ai = fma(c.im, v.re, ai);
+    }
+    x[i] = cd((double)ar, (double)ai);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------
+int gmres_grid(int n) {
+  return std::max(device_sm_count(), (n + kSliceMax - 1) / kSliceMax);
+}
+
+size_t gmres_scalar_doubles(int m, int n) {
+  return GmLayout{m, gmres_grid(n)}.total();
+}
+
+void gmres_enqueue_init(const GmresBufs& B, double tol, cudaStream_t s) {
+  const int G = gmres_grid(B.n);
+  note_launch();
+  if (B.vec64)
+    k_gm_init<double><<<G, kGmThreads, 0, s>>>(B.state, B.gd, B.m, B.n, (const cd*)B.b, (cplx<double>*)B.V,
+                                                (cplx<double>*)B.q, tol);
+  else
+    k_gm_init<float><<<G, kGmThreads, 0, s>>>(B.state, B.gd, B.m, B.n, (const cd*)B.b, (cplx<float>*)B.V,
+                                               (cplx<float>*)B.q, tol);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+size_t gmres_update_smem(int m) {
+  // the update pass keeps j + 1 coefficients, then 3 j + 3 complex FP64 values of the rotation
+  return std::max(sizeof(cplx<double>) * ((size_t)m + 1), sizeof(double) * 2 * (3 * (size_t)m + 3));
+}
+
+template <typename VT>
+static void enqueue_one(const GmresBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, bool first,
+                        cudaStream_t s) {
+  const int G = gmres_grid(B.n);
+  const size_t smem = gmres_update_smem(B.m);
+  MatvecEpilogue ep;  // no fused dots
+  launch_matvec_ex(DP, H, tr, B.vec64, B.q, B.W, nullptr, ep, &B.state->done, s, nullptr, !first);
+  launch_k(true, k_gm_dots<VT>, dim3(G), dim3(kGmThreads), 0, s, B.state, B.gd, B.m, B.n,
+           (const cplx<VT>*)B.V, (const cplx<VT>*)B.W, 0);
+  if (B.reorth) {
+    launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
+             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 0);
+    launch_k(true, k_gm_dots<VT>, dim3(G), dim3(kGmThreads), 0, s, B.state, B.gd, B.m, B.n,
+             (const cplx<VT>*)B.V, (const cplx<VT>*)B.W2, 1);
+    launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
+             (cplx<VT>*)B.V, (const cplx<VT>*)B.W2, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 1, 1);
+  } else {
+    launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
+             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 1);
+  }
+}
+
+void gmres_enqueue_iterations(const GmresBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, int count,
+                              cudaStream_t s) {
+  for (int i = 0; i < count; i++) {
+    if (B.vec64)
+      enqueue_one<double>(B, DP, H, tr, i == 0, s);
+    else
+      enqueue_one<float>(B, DP, H, tr, i == 0, s);
+  }
+}
+
+void gmres_enqueue_finish(const GmresBufs& B, void* x, cudaStream_t s) {
+  const int G = gmres_grid(B.n);
+  note_launch();
+  k_gm_solve<<<1, kGmThreads, sizeof(double) * 2 * (size_t)B.m, s>>>(B.state, B.gd, B.m, G);
+  AC3D_CUDA(cudaGetLastError());
+  const int gx = std::max(1, std::min((B.n + kGmThreads - 1) / kGmThreads, 4 * device_sm_count()));
+  note_launch();
+  if (B.vec64)
+    k_gm_x<double><<<gx, kGmThreads, sizeof(cplx<double>) * (size_t)B.m, s>>>(B.state, B.gd, B.m, B.n,
+                                                                              (const cplx<double>*)B.V, (cd*)x);
+  else
+    k_gm_x<float><<<gx, kGmThreads, sizeof(cplx<float>) * (size_t)B.m, s>>>(B.state, B.gd, B.m, B.n,
+                                                                            (const cplx<float>*)B.V, (cd*)x);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+}  // namespace ac3d

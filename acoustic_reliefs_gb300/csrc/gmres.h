@@ -1,0 +1,44 @@
+// Device-resident GMRES interface (internal).
+#pragma once
+
+#include "internal.h"
+
+namespace ac3d {
+
+// Scalars of one GMRES cycle, kept on the device.
+struct GState {
+  int j;       // basis vectors 0..j exist; iterations done in this cycle
+  int m;       // basis capacity: at most m iterations per cycle
+  int done;    // 0 running, 1 converged, 2 basis full, 3 breakdown (non-finite values)
+  int pad;
+  double tol_abs;   // stop when the least-squares residual estimate falls to this
+  double beta;      // norm of the right-hand side of the cycle
+  double resid;     // latest least-squares residual estimate |g_j|
+  unsigned ticket;  // last-CTA ticket of the reducing passes (zero between launches)
+  int pad2;
+};
+
+// Device buffers of one cycle. vec64: 0 complex FP32 vectors (FP32 H-matrix and arithmetic),
+// 1 complex FP64 vectors (FP64 H-matrix).
+struct GmresBufs {
+  int n = 0, m = 0, vec64 = 0;
+  void* b = nullptr;   // right-hand side, complex FP64 (n)
+  void* V = nullptr;   // basis, (m + 1) x n vectors of the vector type
+  void* q = nullptr;   // the next matvec's input (n)
+  void* W = nullptr;   // the matvec's output (n)
+  void* W2 = nullptr;  // the first Gram-Schmidt pass's result (n), when there are two
+  int reorth = 0;      // 1: two classical Gram-Schmidt passes per iteration (FP32 vectors)
+  double* gd = nullptr;  // gmres_scalar_doubles(m, n) doubles
+  GState* state = nullptr;
+};
+
+int gmres_grid(int n);
+size_t gmres_scalar_doubles(int m, int n);
+size_t gmres_update_smem(int m);
+void gmres_enqueue_init(const GmresBufs& B, double tol, cudaStream_t s);
+void gmres_enqueue_iterations(const GmresBufs& B, const DevPartition& DP, const DevHMat& H, bool transposed,
+                              int count, cudaStream_t s);
+// x (complex FP64, n) = the cycle's solution: the least-squares coefficients applied to the basis
+void gmres_enqueue_finish(const GmresBufs& B, void* x, cudaStream_t s);
+
+}  // namespace ac3d

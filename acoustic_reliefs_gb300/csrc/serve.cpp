@@ -68,6 +68,7 @@ using namespace ac3d;
 struct ac3d_server {
   int device = 0;
   int prec = AC3D_PREC_MIXED;
+  int krylov = AC3D_KRYLOV_BICGSTAB, gm_restart = 300;
   int64_t budget = 0, in_use = 0;
   int running = 0;
   cudaStream_t stream = nullptr;  // mesh uploads
@@ -96,7 +97,12 @@ int64_t footprint(const ac3d_server* S, const MeshEntry& me, double f, int L) {
   lr = std::min<int64_t>(std::max<int64_t>(lr, 1), std::max<int64_t>(m.worst_pool, 1));
   const int64_t pool = std::max<int64_t>(m.pool_hint[S->prec == AC3D_PREC_FP64 ? 1 : 0].load(), lr);
   const int64_t H = (m.P.near_total + pool + lr) * es + (int64_t)m.P.aca_term_cap * 48;
-  const int64_t work = (int64_t)m.Ne * 176 + (int64_t)(m.DP.nleaf + 64) * 40 + (int64_t)L * 64 * 16 + (1 << 20);
+  int64_t work = (int64_t)m.Ne * 176 + (int64_t)(m.DP.nleaf + 64) * 40 + (int64_t)L * 64 * 16 + (1 << 20);
+  if (S->krylov == AC3D_KRYLOV_GMRES) {
+    const int mm = std::min(S->gm_restart, m.Ne);
+    work += ((int64_t)mm + 4) * m.Ne * (es == 16 ? 16 : 8) +
+            (int64_t)gmres_scalar_doubles(mm, m.Ne) * 8 + 4096;
+  }
   return H + work;
 }
 
@@ -168,6 +174,8 @@ void worker(ac3d_server* S, int slot) {
     r->info.slot = slot;
     S->in_use += r->info.footprint_bytes;
     S->running++;
+    c->krylov = S->krylov;
+    c->gm_restart = S->gm_restart;
     lk.unlock();
 
     int rc = AC3D_OK;
@@ -286,6 +294,15 @@ void ac3d_server_destroy(ac3d_server* S) {
 }
 
 const char* ac3d_server_last_error(const ac3d_server* S) { return S ? S->err.c_str() : "null server"; }
+
+int ac3d_server_set_krylov(ac3d_server* S, int method, int restart) {
+  if (!S || (method != AC3D_KRYLOV_BICGSTAB && method != AC3D_KRYLOV_GMRES) || restart < 0 || restart > 600)
+    return AC3D_ERR_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->krylov = method;
+  S->gm_restart = restart > 0 ? restart : 300;
+  return AC3D_OK;
+}
 
 int ac3d_server_add_mesh(ac3d_server* S, const double* Ps, int V, const int32_t* Es, int Ne, int cluster_size,
                          double radius_factor, double aca_tol, double solver_tol, int32_t* Es_out, int* mesh_id) {

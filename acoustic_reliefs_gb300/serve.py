@@ -31,7 +31,8 @@ def admit_next(footprints, bypassed, budget: int, in_use: int, n_running: int) -
 
 
 class Server:
-    def __init__(self, slots: int = 4, precision: str = "mixed", hbm_budget: int = 0, device: int | None = None):
+    def __init__(self, slots: int = 4, precision: str = "mixed", hbm_budget: int = 0, device: int | None = None,
+                 krylov: str = "bicgstab", restart: int = 300):
         L = _L.lib()
         if device is not None:
             rc = L.ac3d_select_device(int(device))
@@ -42,6 +43,7 @@ class Server:
         if rc != _L.OK:
             raise AC3DError(rc, "cannot create the server (no CUDA device or invalid arguments)")
         self._h = h
+        self._check(L.ac3d_server_set_krylov(h, {"bicgstab": 0, "gmres": 1}[krylov], int(restart)))
         self.precision = precision
         self.slots = slots
         self._nL: dict[int, int] = {}

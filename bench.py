@@ -42,6 +42,7 @@ UNIT = "solves/s"
 FREQ = 2000.0
 LEAF, FACTOR, ACA_TOL, SOLVER_TOL = 32, 2.0, 1e-4, 1e-6
 DIRECTION = (0.0, -1.0, 0.0)
+RESTART = 300  # GMRES basis: iterations per cycle
 WORKLOAD = ("0.6 m relief, 64x64 smoothed seeded heightmap, 20480 triangles, 2 kHz, normal plane wave, "
             "181 receivers on a 5 m semicircle, leaf 32, eta 2, ACA 1e-4, BiCGSTAB 1e-6")
 
@@ -69,12 +70,12 @@ def sweep_workload(seed: int, subdivs):
     return reliefs, [reqs[i] for i in order]
 
 
-def run_served(precision, reliefs, reqs, Ls, slots, rate, seed):
+def run_served(precision, reliefs, reqs, Ls, slots, rate, seed, krylov="gmres"):
     """Submits the requests with Poisson arrivals at `rate` per second (all at once if rate is None)
     to a server with `slots` slots; returns (solves/s over the makespan, latencies ms, results)."""
     import threading
     from acoustic_reliefs_gb300.serve import Server
-    with Server(slots=slots, precision=precision) as srv:
+    with Server(slots=slots, precision=precision, krylov=krylov, restart=RESTART) as srv:
         ids = [srv.add_mesh(R.Ps, R.Es, LEAF, FACTOR, ACA_TOL, SOLVER_TOL)[0] for R in reliefs]
         # one untimed request per mesh (kernel set-up, allocator warm-up, footprint estimates)
         for mid in ids:
@@ -110,16 +111,16 @@ def served_sweep(args, Ls):
     out = {"workload": SWEEP_WORKLOAD.format(subdivs="/".join(map(str, subdivs)),
                                              sizes="/".join(str(len(R.Es)) for R in reliefs)),
            "requests": len(reqs), "slots": args.slots}
-    thr, lat_sat, res_m = run_served("mixed", reliefs, reqs, Ls, args.slots, None, 0)
+    thr, lat_sat, res_m = run_served("mixed", reliefs, reqs, Ls, args.slots, None, 0, args.krylov)
     out["mixed"] = {"solves_per_s": thr, "offered": "all requests at t=0 (saturated)",
                     "p50_ms_saturated": float(np.percentile(lat_sat, 50)),
                     "p99_ms_saturated": float(np.percentile(lat_sat, 99))}
     rate = 0.5 * thr
-    thr_l, lat_l, _ = run_served("mixed", reliefs, reqs, Ls, args.slots, rate, 0)
+    thr_l, lat_l, _ = run_served("mixed", reliefs, reqs, Ls, args.slots, rate, 0, args.krylov)
     out["mixed"].update({"poisson_rate_per_s": rate, "solves_per_s_at_rate": thr_l,
                          "p50_ms": float(np.percentile(lat_l, 50)), "p99_ms": float(np.percentile(lat_l, 99))})
     if not args.no_fp64_sweep:
-        thr64, lat64, res_d = run_served("fp64", reliefs, reqs, Ls, args.slots, None, 0)
+        thr64, lat64, res_d = run_served("fp64", reliefs, reqs, Ls, args.slots, None, 0, args.krylov)
         err = max(float(np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0])) for a, b in zip(res_m, res_d))
         out["fp64"] = {"solves_per_s": thr64, "offered": "all requests at t=0 (saturated)",
                        "p50_ms_saturated": float(np.percentile(lat64, 50)),
@@ -307,7 +308,7 @@ def run_reference(args):
     return 0
 
 
-def served_c2(args, R, Ls, precision, n_req, n_warm, rate=None, seed=0, clocks=None):
+def served_c2(args, R, Ls, precision, n_req, n_warm, rate=None, seed=0, clocks=None, krylov=None):
     """Requests of this workload (one mesh, 2 kHz) through the request server with args.slots slots.
     rate None: all n_req requests submitted at once, timed with CUDA events bracketing a device-wide
     synchronisation on both sides (the server's slots run on their own streams); else Poisson
@@ -318,7 +319,7 @@ def served_c2(args, R, Ls, precision, n_req, n_warm, rate=None, seed=0, clocks=N
     from acoustic_reliefs_gb300.serve import Server
     lib = _L.lib()
     inc = ("plane", DIRECTION)
-    with Server(slots=args.slots, precision=precision) as srv:
+    with Server(slots=args.slots, precision=precision, krylov=krylov or args.krylov, restart=RESTART) as srv:
         mid = srv.add_mesh(R.Ps, R.Es, LEAF, FACTOR, ACA_TOL, SOLVER_TOL)[0]
         for _ in range(n_warm):  # one at a time, then a full round of slots
             srv.wait(srv.submit(mid, FREQ, Ls, inc))
@@ -375,6 +376,7 @@ def run_single(args):
                   incident=("plane", DIRECTION), device=0)
     bem.silent = True
     bem.set_solver(0, args.inner_tol, 10)
+    bem.set_krylov(args.krylov, RESTART)
     bem.set_mesh(R.Ps, R.Es)
     dev = torch.device("cuda", 0)
     L = len(Ls)
@@ -393,7 +395,7 @@ def run_single(args):
     ms = e0.elapsed_time(e1)
     st = bem.stats()
     mv_ms, mv_bytes = bem.matvec_timing(20)
-    print(json.dumps({"mode": "single context (kernel captures)", "workload": WORKLOAD,
+    print(json.dumps({"mode": "single context (kernel captures)", "workload": WORKLOAD, "krylov": args.krylov,
                       "solves_per_s": args.steps / (ms / 1e3), "ms_per_solve": ms / args.steps,
                       "iterations": st["iterations"], "refinement_steps": st["outer_steps"],
                       "rel_residual": st["rel_residual"], "ms_assemble": st["ms_assemble"],
@@ -414,6 +416,7 @@ def run_gpu(args):
                     incident=("plane", DIRECTION), device=local)
         b.silent = True
         b.set_solver(0, args.inner_tol, 10)
+        b.set_krylov(args.krylov, RESTART)
         b.set_mesh(R.Ps, R.Es)
         return b
 
@@ -492,6 +495,18 @@ def run_gpu(args):
     err64 = float(np.linalg.norm(y_mixed - y64) / np.linalg.norm(y64))
     it64 = res_d[0][1]["iterations"]
 
+    # the reference's solver (BiCGSTAB) served the same way, for comparison with the headline
+    bicg = None
+    if args.krylov != "bicgstab":
+        bicg = {"note": "BiCGSTAB (the reference's solver) inner solves, request server with the same slots"}
+        for prec, nreq in (("mixed", args.steps), ("fp64", n64)):
+            _, bms, _, _, res_b = served_c2(args, R, Ls, prec, nreq, 1, krylov="bicgstab")
+            bms = max_over_ranks(world, bms)
+            bicg[prec] = {"solves_per_s": world * nreq / (bms / 1e3), "ms_per_step": bms / nreq,
+                          "iterations": res_b[0][1]["iterations"],
+                          "pressure_rel_err_vs_headline": float(np.linalg.norm(res_b[0][0] - y_mixed) /
+                                                                np.linalg.norm(y_mixed))}
+
     # block solve: 16 incidence directions of the same frequency against one H-matrix
     multi = None
     if args.multi_rhs > 0:
@@ -529,6 +544,8 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 storage/products, f64 dots+refinement",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "precision": "mixed (FP32 + FP64 refinement)",
+                   "krylov": (f"GMRES({RESTART}) cycles, two classical Gram-Schmidt passes in FP32, inside the FP64 "
+                              "refinement loop" if args.krylov == "gmres" else "BiCGSTAB (as the reference)"),
                    "serving": f"request server, {args.slots} slots, {args.steps} requests submitted at once; "
                               "mesh registered (resident) before the timed region",
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (H-matrix ~550 MB per solve)"},
@@ -540,6 +557,7 @@ def run_gpu(args):
                     "note": "p50/p99 at the top level are request latencies (submit to result on the host) under "
                             "Poisson arrivals at half the saturated rate; saturated = all requests at once"},
         "single_context": single,
+        "bicgstab": bicg,
         "served_results_bitwise_equal_to_single_context": bool(served_equal),
         "fp64_gpu": {"value": f64_value, "unit": UNIT, "ms_per_step": f64_ms / n64, "requests": n64,
                      "serving": f"request server, {args.slots} slots, all requests at once",
@@ -584,6 +602,9 @@ def main():
     ap.add_argument("--slots", type=int, default=4, help="server slots (concurrent requests)")
     ap.add_argument("--no-fp64-sweep", action="store_true")
     ap.add_argument("--multi-rhs", type=int, default=16, help="directions of the block-solve leg (0 to skip)")
+    ap.add_argument("--krylov", default="gmres", choices=["gmres", "bicgstab"],
+                    help="inner solver of every GPU leg (BiCGSTAB is the reference's; a served BiCGSTAB leg is "
+                         "reported beside a GMRES headline)")
     ap.add_argument("--single-context", action="store_true",
                     help="only one context on one stream (no request server): the command for kernel captures")
     args = ap.parse_args()

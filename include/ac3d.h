@@ -34,6 +34,9 @@ extern "C" {
 #define AC3D_INCIDENT_POINT 0 /* point source e^{-ikr}/(4 pi r) at the given point */
 #define AC3D_INCIDENT_PLANE 1 /* plane wave e^{-ik d.x} along the given unit vector */
 
+#define AC3D_KRYLOV_BICGSTAB 0 /* the reference's solver (Eigen::BiCGSTAB, adjoint.cpp:92-95) */
+#define AC3D_KRYLOV_GMRES 1    /* GMRES: one matvec per iteration, restarted by the refinement loop */
+
 #define AC3D_LISTENER_DENSE 0 /* receiver matrix evaluated exactly on the fly */
 #define AC3D_LISTENER_ACA 1   /* receiver matrix by ACA with Q_ACA_tol, as the reference */
 
@@ -74,6 +77,13 @@ int ac3d_set_precision(ac3d_ctx* ctx, int precision);
 int ac3d_set_incident(ac3d_ctx* ctx, int kind, const double* v3);
 int ac3d_set_listener_mode(ac3d_ctx* ctx, int mode);
 int ac3d_set_solver(ac3d_ctx* ctx, int max_iterations, double inner_tol, int max_outer);
+/* Krylov method of the single right-hand-side solves (forward, adjoint, exact operator):
+ * AC3D_KRYLOV_BICGSTAB (default, as the reference) or AC3D_KRYLOV_GMRES with a basis of `restart`
+ * vectors (1..600; 0: 300). GMRES stops on the same relative residual; each cycle of at most
+ * `restart` iterations is followed by a true-residual check of the refinement loop, which starts
+ * the next cycle if needed (at most max_outer cycles; max_iterations applies to BiCGSTAB only).
+ * Block solves (ac3d_solve_multi) always use block BiCGSTAB. No reference counterpart. */
+int ac3d_set_krylov(ac3d_ctx* ctx, int method, int restart);
 /* Replace the receivers used by value / values / band_value / gradient (default: the
  * hemisphere of compute_listener_pts, helpers.cpp:52-65). */
 int ac3d_set_listeners(ac3d_ctx* ctx, const double* Ls, int L);
@@ -170,9 +180,11 @@ long long ac3d_kernel_launches(void);
 int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
 /* Times `iters` back-to-back H-matrix matvecs (y = op(A) x, inner-solve precision) on the
  * H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, with CUDA events on the
- * context stream; the passes are launched as in the solve (programmatic dependent launches). Outputs the mean milliseconds per matvec and the algorithmic bytes per matvec:
- * stored matrix entries x entry size + 32 Ne (read x and write y, FP64 complex), + 8 Ne for the
- * FP32 shadow of x the mixed inner solve reads. No reference counterpart. */
+ * context stream, in the variant the context's solver runs, launched as in the solve (programmatic
+ * dependent launches). Outputs the mean milliseconds per matvec and the algorithmic bytes per
+ * matvec: stored matrix entries x entry size + reading x and writing y (32 Ne for FP64 vectors,
+ * + 8 Ne for the FP32 shadow of x the mixed BiCGSTAB reads; 16 Ne for the FP32 vectors of the
+ * mixed GMRES). No reference counterpart. */
 int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_matvec, long long* bytes);
 
 /* Receiver far field y_l = sum_j M(receiver l, element j) x_j (FP64), with every argument in
@@ -236,7 +248,7 @@ typedef struct ac3d_request_info {
   long long footprint_bytes;   /* admission estimate */
   long long hmat_bytes;        /* device bytes of the assembled H-matrix */
   long long lr_entries, near_entries;
-  int iterations, outer_steps; /* BiCGSTAB iterations; refinement steps */
+  int iterations, outer_steps; /* Krylov iterations; refinement steps */
   double rel_residual;         /* final FP64 |b - A x| / |b| */
   double ms_assemble, ms_solve, ms_listener; /* device time of the phases */
 } ac3d_request_info;
@@ -245,6 +257,9 @@ typedef struct ac3d_request_info {
 int ac3d_server_create(ac3d_server** out, int slots, int precision, long long hbm_budget_bytes);
 /* Waits for every submitted request, then releases the slots, meshes and streams. */
 void ac3d_server_destroy(ac3d_server* srv);
+/* Krylov method of the requests that start after the call (ac3d_set_krylov semantics). No
+ * reference counterpart. */
+int ac3d_server_set_krylov(ac3d_server* srv, int method, int restart);
 const char* ac3d_server_last_error(const ac3d_server* srv);
 /* Registers a mesh (set_mesh semantics: Es_out, if given, receives the tree-ordered connectivity
  * the results refer to) with its H-matrix and solver parameters. */

@@ -1,0 +1,94 @@
+"""GPU parity of the GMRES inner solver (ac3d_set_krylov / ac3d_server_set_krylov) through the C-ABI:
+the same golden oracle pressures as the BiCGSTAB path (1e-4 relative L2), the same relative
+residual (1e-6), restarted cycles, the adjoint (transposed) solve, bitwise repeatability and the
+request server. The reference solves with BiCGSTAB; no reference test pins a solver's
+iterations, so the contract is the solution: both solvers must meet the residual and agree with
+the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from acoustic_reliefs_gb300.acoustics3d import DiffBEM
+from acoustic_reliefs_gb300.serve import Server
+from tests import cases
+from tests.test_gpu_parity import small_diffbem
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+P_TOL = 1e-4
+
+
+def pressures(c, precision, krylov="gmres", restart=300, max_outer=10):
+    bem = DiffBEM(c["leaf"], c["factor"], [c["freq"]], 1, c["aca_tol"], c["aca_tol"], c["tol"],
+                  precision=precision, incident=("plane", c["vec"]))
+    bem.silent = True
+    bem.set_solver(0, 1e-6, max_outer)
+    bem.set_krylov(krylov, restart)
+    _, Es = bem.set_mesh(c["Ps"], c["Es"])
+    y = bem.pvals(c["freq"], c["Ls"])
+    return y, bem.stats(), Es
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gmres_sphere_vs_oracle_and_mie(gpu_lib, precision):
+    g = np.load(os.path.join(GOLDEN, "sphere_c1.npz"))
+    c = cases.sphere_c1()
+    y, st, Es = pressures(c, precision)
+    assert np.array_equal(Es, g["Es_tree"])
+    assert cases.rel_l2(y, g["y_oracle_dense"]) < P_TOL
+    assert cases.rel_l2(y, g["y_mie"]) < 2e-2
+    assert st["converged"] == 1 and st["rel_residual"] <= c["tol"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gmres_relief_vs_oracle(gpu_lib, precision):
+    g = np.load(os.path.join(GOLDEN, "relief_small.npz"))
+    c = cases.relief_small()
+    y, st, _ = pressures(c, precision)
+    assert cases.rel_l2(y, g["y_oracle"]) < P_TOL
+    assert st["converged"] == 1 and st["rel_residual"] <= c["tol"]
+    # one matvec per iteration: fewer matvecs than BiCGSTAB's two per iteration on this system
+    yb, sb, _ = pressures(c, precision, "bicgstab")
+    assert st["iterations"] < 2 * sb["iterations"]
+    assert cases.rel_l2(y, yb) < P_TOL / 2
+
+
+def test_gmres_restarted_cycles(gpu_lib):
+    """A basis of 24 vectors: the refinement loop restarts the cycle until the residual is met."""
+    c = cases.relief_small()
+    y, st, _ = pressures(c, "fp64", restart=24, max_outer=40)
+    assert st["outer_steps"] > 1
+    assert st["converged"] == 1 and st["rel_residual"] <= c["tol"]
+    yb, _, _ = pressures(c, "fp64", "bicgstab")
+    assert cases.rel_l2(y, yb) < P_TOL / 2
+
+
+def test_gmres_repeatable_bitwise(gpu_lib):
+    c = cases.relief_small()
+    y1, _, _ = pressures(c, "mixed")
+    y2, _, _ = pressures(c, "mixed")
+    assert np.array_equal(y1, y2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gmres_gradient_vs_oracle(oracle_lib, gpu_lib, precision):
+    """The adjoint solves the transposed system through the same GMRES path."""
+    gpu, orc, R = small_diffbem(oracle_lib, precision)
+    gpu.set_krylov("gmres")
+    x = np.random.default_rng(6).uniform(0, 0.02, size=len(R.diff_pts))
+    cg, gg = gpu.gradient(x)
+    co, go = orc.gradient(x)
+    assert abs(cg - co) < 1e-3
+    assert np.linalg.norm(gg - go) / np.linalg.norm(go) < 1e-3
+
+
+def test_gmres_served_equals_single_context(gpu_lib):
+    c = cases.relief_small()
+    y1, st, _ = pressures(c, "mixed")
+    with Server(slots=2, krylov="gmres") as srv:
+        mid, _ = srv.add_mesh(c["Ps"], c["Es"], 32, 2.0, 1e-4, 1e-6)
+        res = [srv.wait(h) for h in [srv.submit(mid, c["freq"], c["Ls"], ("plane", c["vec"])) for _ in range(3)]]
+    for y, info in res:
+        assert np.array_equal(y, y1)
+        assert info["iterations"] == st["iterations"]
