@@ -226,11 +226,16 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def measured_traffic():
+def traffic_profile(krylov):
+    """The committed ncu capture of the matvec variant the solver runs."""
+    return os.path.join("profiles", "gmres_solve_relief20k.md" if krylov == "gmres" else "hmatvec_relief20k_ncu.md")
+
+
+def measured_traffic(krylov):
     """DRAM bytes of one matvec of this workload from the committed ncu capture (one pass of
     dram__bytes_read.sum + dram__bytes_write.sum over the dot, reduce and gather kernels)."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", "hmatvec_relief20k_ncu.md")):
+        for line in open(os.path.join(ROOT, traffic_profile(krylov))):
             if line.startswith("traffic_bytes_per_matvec:"):
                 return int(line.split(":")[1])
     except OSError:
@@ -573,8 +578,8 @@ def run_gpu(args):
                 "path": "DiffBEM C-ABI (ac3d_set_points + ac3d_pressures), one request after another"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": measured_traffic(),
-                     "traffic_source": "profiles/hmatvec_relief20k_ncu.md (ncu, one matvec of this workload)",
+                     "frac": achieved / peak, "traffic": measured_traffic(args.krylov),
+                     "traffic_source": traffic_profile(args.krylov) + " (ncu, one matvec of this workload)",
                      "kernel": "H-matrix matvec (dot + reduce + gather passes)",
                      "bytes_per_launch": int(mv_bytes), "ms_per_launch": mv_ms, "peak_kind": peak_kind},
         "clocks": clk.summary(),
