@@ -504,8 +504,8 @@ def run_gpu(args):
     bicg = None
     if args.krylov != "bicgstab":
         bicg = {"note": "BiCGSTAB (the reference's solver) inner solves, request server with the same slots"}
-        for prec, nreq in (("mixed", args.steps), ("fp64", n64)):
-            _, bms, _, _, res_b = served_c2(args, R, Ls, prec, nreq, 1, krylov="bicgstab")
+        for prec, nreq, nwarm in (("mixed", args.steps, args.warmup), ("fp64", n64, 1)):
+            _, bms, _, _, res_b = served_c2(args, R, Ls, prec, nreq, nwarm, krylov="bicgstab")
             bms = max_over_ranks(world, bms)
             bicg[prec] = {"solves_per_s": world * nreq / (bms / 1e3), "ms_per_step": bms / nreq,
                           "iterations": res_b[0][1]["iterations"],
