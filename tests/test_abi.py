@@ -43,3 +43,10 @@ def test_create_rejects_bad_arguments():
     # cluster size 0 is rejected before any device work
     rc = L.lib().ac3d_create(ctypes.byref(h), 0, 1.5, L.ptr(bands), 1, 1, 1e-3, 1e-3, 1e-3, L.ptr(src), 50.0, 5.0, 0)
     assert rc == L.ERR_ARG and not h.value
+
+
+def test_krylov_option_rejects_bad_arguments():
+    """ac3d_set_krylov / ac3d_server_set_krylov validate before touching any context."""
+    lib = L.lib()
+    assert lib.ac3d_set_krylov(None, 1, 300) == L.ERR_ARG
+    assert lib.ac3d_server_set_krylov(None, 1, 300) == L.ERR_ARG
