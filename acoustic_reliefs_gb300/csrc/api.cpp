@@ -396,10 +396,6 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   return st.iter;
 }
 
-#ifndef AC3D_GMRES_REORTH32
-#define AC3D_GMRES_REORTH32 1
-#endif
-
 // GMRES buffers of this context for the H-matrix's precision, carved from one allocation.
 GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const cd* b) {
   GmresBufs G;
@@ -420,7 +416,7 @@ GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const cd* b) {
   G.state = (GState*)(p + vb + 3 * nb + gb);
   // FP32 classical Gram-Schmidt loses orthogonality over long cycles: two passes keep the FP32
   // cycle converging like the FP64 one
-  G.reorth = G.vec64 ? 0 : AC3D_GMRES_REORTH32;
+  G.reorth = G.vec64 ? 0 : 1;
   G.b = (void*)b;
   if (!c->h_gstate) AC3D_CUDA(cudaMallocHost(&c->h_gstate, 2 * sizeof(GState)));
   return G;
