@@ -417,9 +417,6 @@ GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const cd* b) {
   // FP32 classical Gram-Schmidt loses orthogonality over long cycles: two passes keep the FP32
   // cycle converging like the FP64 one
   G.reorth = G.vec64 ? 0 : 1;
-  // the first 64 iterations of a cycle take one pass: 15.2 instead of 16.1 ms of solve on the 20k
-  // relief at 2 kHz, with the same iteration counts there and on the 32k relief at 3.5 kHz
-  G.two_from = 64;
   G.b = (void*)b;
   if (!c->h_gstate) AC3D_CUDA(cudaMallocHost(&c->h_gstate, 2 * sizeof(GState)));
   return G;

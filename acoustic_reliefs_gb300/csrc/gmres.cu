@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_dots(GState* st, double* gd, 
                                                         const cplx<VT>* __restrict__ X, int second) {
   grid_dep_wait();  // X comes from the kernel just before
   grid_dep_launch();
-  if (st->done || (second && st->one_pass)) return;
+  if (st->done) return;
   const GmLayout L{m, (int)gridDim.x};
   const int j = st->j;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -226,16 +226,12 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_dots(GState* st, double* gd, 
 template <typename VT>
 __global__ void __launch_bounds__(kGmThreads) k_gm_update(GState* st, double* gd, int m, int n, cplx<VT>* V,
                                                           const cplx<VT>* __restrict__ X, cplx<VT>* Y, cplx<VT>* q,
-                                                          int second, int final_pass, int two_from) {
+                                                          int second, int final_pass) {
   grid_dep_wait();  // the coefficients come from the dot pass just before
   grid_dep_launch();
-  if (st->done || (second && st->one_pass)) return;
+  if (st->done) return;
   const GmLayout L{m, (int)gridDim.x};
   const int j = st->j;
-  // the first pass is the final one while j < two_from: early in a cycle the basis is still
-  // orthogonal to working accuracy, and one pass costs half as much
-  if (!final_pass && j < two_from) final_pass = 1;
-  if (!second && blockIdx.x == 0 && threadIdx.x == 0) st->one_pass = final_pass;
   extern __shared__ __align__(16) unsigned char gsm[];
   cplx<VT>* coef = reinterpret_cast<cplx<VT>*>(gsm);  // j + 1 coefficients
   for (int k = threadIdx.x; k <= j; k += blockDim.x)
@@ -459,14 +455,14 @@ static void enqueue_one(const GmresBufs& B, const DevPartition& DP, const DevHMa
            (const cplx<VT>*)B.V, (const cplx<VT>*)B.W, 0);
   if (B.reorth) {
     launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
-             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 0, B.two_from);
+             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 0);
     launch_k(true, k_gm_dots<VT>, dim3(G), dim3(kGmThreads), 0, s, B.state, B.gd, B.m, B.n,
              (const cplx<VT>*)B.V, (const cplx<VT>*)B.W2, 1);
     launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
-             (cplx<VT>*)B.V, (const cplx<VT>*)B.W2, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 1, 1, 0);
+             (cplx<VT>*)B.V, (const cplx<VT>*)B.W2, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 1, 1);
   } else {
     launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
-             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 1, 0);
+             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 1);
   }
 }
 

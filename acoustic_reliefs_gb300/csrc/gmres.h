@@ -10,7 +10,7 @@ struct GState {
   int j;       // basis vectors 0..j exist; iterations done in this cycle
   int m;       // basis capacity: at most m iterations per cycle
   int done;    // 0 running, 1 converged, 2 basis full, 3 breakdown (non-finite values)
-  int one_pass;  // the running iteration's first Gram-Schmidt pass was its final one
+  int pad;
   double tol_abs;   // stop when the least-squares residual estimate falls to this
   double beta;      // norm of the right-hand side of the cycle
   double resid;     // latest least-squares residual estimate |g_j|
@@ -28,7 +28,6 @@ struct GmresBufs {
   void* W = nullptr;   // the matvec's output (n)
   void* W2 = nullptr;  // the first Gram-Schmidt pass's result (n), when there are two
   int reorth = 0;      // 1: two classical Gram-Schmidt passes per iteration (FP32 vectors)
-  int two_from = 0;    // with reorth: iterations j < two_from take one pass
   double* gd = nullptr;  // gmres_scalar_doubles(m, n) doubles
   GState* state = nullptr;
 };
