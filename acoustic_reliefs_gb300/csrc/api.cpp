@@ -396,30 +396,46 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   return st.iter;
 }
 
-// GMRES buffers of this context for the H-matrix's precision, carved from one allocation.
-GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const cd* b) {
+// GMRES buffers of this context, carved from one allocation: nrb cycles (a batch shares its
+// matvecs; the block vectors q, W and b belong to the caller then) in the H-matrix's precision.
+GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const void* b, int nrb = 1) {
   GmresBufs G;
   G.n = c->m->Ne;
   G.m = std::max(1, std::min(c->gm_restart, G.n));
   G.vec64 = H.prec == PREC_FP64 ? 1 : 0;
+  G.nrb = nrb;
+  G.vs = nrb;
   const size_t es = G.vec64 ? sizeof(cd) : sizeof(cf);
   auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
-  const size_t vb = up(((size_t)G.m + 1) * G.n * es), nb = up((size_t)G.n * es);
-  const size_t gb = up(gmres_scalar_doubles(G.m, G.n) * sizeof(double));
-  c->gm.ensure(vb + 3 * nb + gb + up(sizeof(GState)), c->stream);
+  G.Vs = ((size_t)G.m + 1) * G.n;
+  G.gds = (gmres_scalar_doubles(G.m, G.n) + 1) & ~(size_t)1;
+  const size_t vb = up(G.Vs * es * nrb), nb = up((size_t)G.n * es);
+  const size_t gb = up(G.gds * nrb * sizeof(double)), sb = up(nrb * sizeof(GState) + sizeof(GMulti));
+  const size_t vecs = nrb == 1 ? 3 * nb : 0;  // single: q, W, W2 here; a batch uses the caller's
+  c->gm.ensure(vb + vecs + gb + sb, c->stream);
   char* p = (char*)c->gm.p;
   G.V = p;
-  G.q = p + vb;
-  G.W = p + vb + nb;
-  G.W2 = p + vb + 2 * nb;
-  G.gd = (double*)(p + vb + 3 * nb);
-  G.state = (GState*)(p + vb + 3 * nb + gb);
+  if (nrb == 1) {
+    G.q = p + vb;
+    G.W = p + vb + nb;
+    G.W2 = p + vb + 2 * nb;
+  }
+  G.gd = (double*)(p + vb + vecs);
+  G.state = (GState*)(p + vb + vecs + gb);
+  G.gm = (GMulti*)(G.state + nrb);
+  G.b = (void*)b;
   // FP32 classical Gram-Schmidt loses orthogonality over long cycles: two passes keep the FP32
   // cycle converging like the FP64 one
   G.reorth = G.vec64 ? 0 : 1;
-  G.b = (void*)b;
   if (!c->h_gstate) AC3D_CUDA(cudaMallocHost(&c->h_gstate, 2 * sizeof(GState)));
   return G;
+}
+
+// Zero states (their tickets start at zero; each reducing pass leaves them at zero) and batch
+// completion count; no host wait, so the host captures the cycle's graph while the device runs
+// the assembly.
+void gmres_reset(const GmresBufs& G, cudaStream_t s) {
+  AC3D_CUDA(cudaMemsetAsync(G.state, 0, G.nrb * sizeof(GState) + sizeof(GMulti), s));
 }
 
 // One GMRES cycle on op(A) d = b (complex FP64 device vectors): at most gm_restart iterations, in
@@ -427,8 +443,7 @@ GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const cd* b) {
 int run_gmres(ac3d_ctx* c, const DevHMat& H, const cd* b, cd* d, bool tr, double tol, int* done) {
   cudaStream_t s = c->stream;
   GmresBufs G = gmres_bufs(c, H, b);
-  // the scalars' ticket starts at zero; each reducing pass leaves it at zero
-  AC3D_CUDA(cudaMemsetAsync(G.state, 0, sizeof(GState), s));
+  gmres_reset(G, s);
   gmres_enqueue_init(G, tol, s);
   cudaGraph_t graph;
   const long long before = t_kernel_launches;
@@ -635,6 +650,54 @@ int run_block_krylov(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vec
   return st.iter;
 }
 
+// One batch of GMRES cycles, one per column of the FP32 block right-hand side B.b (element-major,
+// tolerances B.tol): every iteration is one block matvec of all the columns' inputs, then each
+// column's Gram-Schmidt passes. Writes the FP32 block solution B.x; per-column done codes in
+// `done`. Returns the iterations of the longest cycle.
+int run_block_gmres(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vector<int>& done) {
+  cudaStream_t s = c->stream;
+  GmresBufs G = gmres_bufs(c, H, B.b, B.nrb);
+  G.b32 = 1;
+  G.tolv = B.tol;
+  G.q = B.p;   // block vectors of the block solver, free during a GMRES batch
+  G.W = B.v;
+  G.W2 = B.s;  // nrb columns of n
+  gmres_reset(G, s);
+  gmres_enqueue_init(G, 1.0, s);
+  cudaGraph_t graph;
+  const long long before = t_kernel_launches;
+  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  gmres_enqueue_iterations_block(G, B, c->m->DP, H, c->gm_chunk, s);
+  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
+  const long long nodes = t_kernel_launches - before;
+  unnote_launches(nodes);
+  cudaGraphExec_t exec;
+  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  AC3D_CUDA(cudaGraphDestroy(graph));
+  const int max_launch = (G.m + c->gm_chunk - 1) / c->gm_chunk + 1;
+  GMulti gm{};
+  for (int launched = 0; launched < max_launch; launched++) {
+    AC3D_CUDA(cudaGraphLaunch(exec, s));
+    note_launch(nodes);
+    AC3D_CUDA(cudaMemcpyAsync(&gm, G.gm, sizeof(GMulti), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    if (gm.done_all) break;
+  }
+  AC3D_CUDA(cudaGraphExecDestroy(exec));
+  gmres_enqueue_finish(G, B.x, s);
+  std::vector<GState> st(G.nrb);
+  AC3D_CUDA(cudaMemcpyAsync(st.data(), G.state, G.nrb * sizeof(GState), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  done.assign(G.nrb, 0);
+  int iters = 0;
+  for (int j = 0; j < G.nrb; j++) {
+    done[j] = st[j].done;
+    iters = std::max(iters, st[j].j);
+  }
+  c->stats.matvecs += iters;
+  return iters;
+}
+
 // |b - A x|^2 of one column (contiguous FP64 vectors) with the double-float residual matvec
 double column_residual2(ac3d_ctx* c, const DevHMat& H, const cd* b, const cd* x, cd* r) {
   return reduce_norm2_residual(c, H, false, b, x, r);
@@ -710,7 +773,7 @@ void solve_block(ac3d_ctx* c, DevHMat& H, int nrb, int nr, const cd* b64, cd* x6
     if (!any) break;
     AC3D_CUDA(cudaMemcpyAsync(W.tolb.p, tin.data(), nrb * sizeof(double), cudaMemcpyHostToDevice, s));
     launch_to32(n * nrb, W.r64.p, B.b, s);
-    iters += run_block_krylov(c, H, B, done);
+    iters += c->krylov == AC3D_KRYLOV_GMRES ? run_block_gmres(c, H, B, done) : run_block_krylov(c, H, B, done);
     launch_add32(n * nrb, x64, B.x, s);
     for (int j = 0; j < nr; j++) {
       if (!(rn2[j] > tol * tol * bn2[j])) continue;

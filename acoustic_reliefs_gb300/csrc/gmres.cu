@@ -22,6 +22,7 @@
 #include "internal.h"
 #include "krylov.h"
 #include "launch.cuh"
+#include "multi.h"
 
 namespace ac3d {
 
@@ -56,6 +57,25 @@ struct GmLayout {
   __host__ __device__ size_t total() const { return npart() + (size_t)G; }
 };
 
+// Column r = blockIdx.y of a batch: its state, scalars and basis.
+struct GmCols {
+  GState* st;
+  GMulti* gm;
+  double* gd;
+  size_t gds;  // doubles per column
+  size_t Vs;   // basis elements per column
+  int vs;      // element stride of the block vectors
+};
+
+// Ends the cycle of this column with `code` (once) and counts it towards the batch's completion
+// (the batch is the grid's y extent).
+__device__ __forceinline__ void gm_mark_done(GState* st, GMulti* gm, int code) {
+  if (st->done || !code) return;
+  st->done = code;
+  __threadfence();
+  if (atomicAdd(&gm->ndone, 1) == (int)gridDim.y - 1) gm->done_all = 1;
+}
+
 // Contiguous element range of this CTA.
 __device__ __forceinline__ void gm_range(int n, int& lo, int& hi) {
   const int per = (n + (int)gridDim.x - 1) / (int)gridDim.x;
@@ -85,18 +105,25 @@ __device__ __forceinline__ double warp_sum_run(const double* p, int G, int lane,
 }
 
 // V_0 = b (rounded to VT), q = V_0, s_0 = 1 / |V_0|, g = (|V_0|, 0, ...).
-template <typename VT>
-__global__ void __launch_bounds__(kGmThreads) k_gm_init(GState* st, double* gd, int m, int n, const cd* __restrict__ b,
-                                                        cplx<VT>* V, cplx<VT>* q, double tol) {
+template <typename VT, typename BT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_init(GmCols C, int m, int n, const cplx<BT>* __restrict__ b,
+                                                        cplx<VT>* V, cplx<VT>* q, double tol,
+                                                        const double* __restrict__ tolv) {
+  const int r = blockIdx.y, vs = C.vs;
+  GState* st = C.st + r;
+  double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  b += r;
+  q += r;
   const GmLayout L{m, (int)gridDim.x};
   int lo, hi;
   gm_range(n, lo, hi);
   VT a = 0;
   for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    const cd bi = b[i];
+    const cplx<BT> bi = b[(size_t)i * vs];
     const cplx<VT> v((VT)bi.re, (VT)bi.im);
     V[i] = v;
-    q[i] = v;
+    q[(size_t)i * vs] = v;
     a = fma(v.re, v.re, fma(v.im, v.im, a));
   }
   __shared__ VT sw[kGmWarps];
@@ -116,14 +143,14 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_init(GState* st, double* gd, 
       st->j = 0;
       st->m = m;
       st->beta = beta;
-      st->tol_abs = tol * beta;
+      st->tol_abs = (tolv ? tolv[r] : tol) * beta;
       st->resid = beta;
-      // a zero right-hand side has the zero solution; a non-finite one cannot be solved
-      st->done = beta > 0.0 && isfinite(beta) ? 0 : (beta == 0.0 ? 1 : 3);
       gd[L.s()] = beta > 0.0 ? 1.0 / beta : 0.0;
       gd[L.g()] = beta;
       gd[L.g() + 1] = 0.0;
       st->ticket = 0u;
+      // a zero right-hand side has the zero solution; a non-finite one cannot be solved
+      gm_mark_done(st, C.gm, beta > 0.0 && isfinite(beta) ? 0 : (beta == 0.0 ? 1 : 3));
     }
   }
 }
@@ -134,25 +161,32 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_init(GState* st, double* gd, 
 // them in CTA order, sets (first pass) or adds to (second pass) the Hessenberg column and writes
 // the update coefficients h_k s_k.
 template <typename VT>
-__global__ void __launch_bounds__(kGmThreads) k_gm_dots(GState* st, double* gd, int m, int n,
-                                                        const cplx<VT>* __restrict__ V,
+__global__ void __launch_bounds__(kGmThreads) k_gm_dots(GmCols C, int m, int n, const cplx<VT>* __restrict__ V,
                                                         const cplx<VT>* __restrict__ X, int second) {
   grid_dep_wait();  // X comes from the kernel just before
   grid_dep_launch();
+  const int r = blockIdx.y;
+  GState* st = C.st + r;
   if (st->done) return;
+  double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  // X: the matvec output (block vectors) on the first pass, the first pass's result (one column
+  // of n) on the second
+  const int xstr = second ? 1 : C.vs;
+  X += second ? (size_t)r * n : (size_t)r;
   const GmLayout L{m, (int)gridDim.x};
   const int j = st->j;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int lo, hi;
   gm_range(n, lo, hi);
-  __shared__ cplx<VT> xs[kSliceMax];
-  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) xs[i - lo] = X[i];
+  __shared__ cplx<VT> xsm[kSliceMax];
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) xsm[i - lo] = X[(size_t)i * xstr];
   __syncthreads();
   const int len = hi - lo;
   for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
     VT ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
     for (int t = lane; t < len; t += 32) {
-      const cplx<VT> x = xs[t];
+      const cplx<VT> x = xsm[t];
       cplx<VT> v[4];
 #pragma unroll
       for (int u = 0; u < 4; u++) v[u] = kb + u <= j ? V[(size_t)(kb + u) * n + lo + t] : cplx<VT>();
@@ -224,12 +258,22 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_dots(GState* st, double* gd, 
 // the next matvec's input), with |U|^2 partials; the last CTA rotates the new Hessenberg column,
 // updates the residual estimate and decides whether the cycle goes on.
 template <typename VT>
-__global__ void __launch_bounds__(kGmThreads) k_gm_update(GState* st, double* gd, int m, int n, cplx<VT>* V,
+__global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n, cplx<VT>* V,
                                                           const cplx<VT>* __restrict__ X, cplx<VT>* Y, cplx<VT>* q,
                                                           int second, int final_pass) {
   grid_dep_wait();  // the coefficients come from the dot pass just before
   grid_dep_launch();
+  const int r = blockIdx.y;
+  GState* st = C.st + r;
   if (st->done) return;
+  double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  // X: the matvec output (block vectors, first pass) or this column's first-pass result; Y: this
+  // column's first-pass result; q: the next matvec's input (block vectors)
+  const int xstr = second ? 1 : C.vs;
+  X += second ? (size_t)r * n : (size_t)r;
+  Y += (size_t)r * n;
+  q += r;
   const GmLayout L{m, (int)gridDim.x};
   const int j = st->j;
   extern __shared__ __align__(16) unsigned char gsm[];
@@ -243,7 +287,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GState* st, double* gd
   cplx<VT>* out = final_pass ? V + (size_t)(j + 1) * n : Y;
   VT a = 0;
   for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    const cplx<VT> x = X[i];
+    const cplx<VT> x = X[(size_t)i * xstr];
     VT ur = sx * x.re, ui = sx * x.im;
     const cplx<VT>* Vi = V + i;
     int k = 0;
@@ -272,7 +316,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GState* st, double* gd
     const cplx<VT> u(ur, ui);
     out[i] = u;
     if (final_pass) {
-      q[i] = u;
+      q[(size_t)i * C.vs] = u;
       a = fma(ur, ur, fma(ui, ui, a));
     }
   }
@@ -325,9 +369,9 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GState* st, double* gd
   for (int i = threadIdx.x; i < j; i += blockDim.x) {
     const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
     const Dc s = dc(gd[L.sn() + 2 * i], gd[L.sn() + 2 * i + 1]);
-    const Dc r = c * xs[i] + s * hs[i + 1];
-    R[2 * i] = r.re;
-    R[2 * i + 1] = r.im;
+    const Dc rv = c * xs[i] + s * hs[i + 1];
+    R[2 * i] = rv.re;
+    R[2 * i + 1] = rv.im;
   }
   if (threadIdx.x == 0) {
     const Dc a0 = xs[j], b0 = hs[j + 1];
@@ -354,19 +398,23 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GState* st, double* gd
     gd[L.s() + j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
     st->resid = res;
     st->j = j + 1;
-    if (!isfinite(res) || !isfinite(d) || d == 0.0)
-      st->done = (d == 0.0 && isfinite(res) && res <= st->tol_abs) ? 1 : 3;
-    else if (res <= st->tol_abs || nrm == 0.0)
-      st->done = 1;
-    else if (j + 1 >= m)
-      st->done = 2;
     st->ticket = 0u;
+    int code = 0;
+    if (!isfinite(res) || !isfinite(d) || d == 0.0)
+      code = (d == 0.0 && isfinite(res) && res <= st->tol_abs) ? 1 : 3;
+    else if (res <= st->tol_abs || nrm == 0.0)
+      code = 1;
+    else if (j + 1 >= m)
+      code = 2;
+    gm_mark_done(st, C.gm, code);
   }
 }
 
 // y = R^{-1} g over the completed columns, then coef_k = y_k s_k (one CTA).
-__global__ void __launch_bounds__(kGmThreads) k_gm_solve(const GState* st, double* gd, int m, int G) {
+__global__ void __launch_bounds__(kGmThreads) k_gm_solve(GmCols C, int m, int G) {
   const GmLayout L{m, G};
+  const GState* st = C.st + blockIdx.y;
+  double* gd = C.gd + blockIdx.y * C.gds;
   const int jj = st->done == 3 ? 0 : st->j;  // a failed cycle adds nothing
   extern __shared__ __align__(16) unsigned char gsm[];
   Dc* gs = reinterpret_cast<Dc*>(gsm);  // jj entries
@@ -389,11 +437,16 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_solve(const GState* st, doubl
   }
 }
 
-// x = sum_k coef_k V_k over the completed columns (FP64 output).
-template <typename VT>
-__global__ void __launch_bounds__(kGmThreads) k_gm_x(const GState* st, const double* gd, int m, int n,
-                                                     const cplx<VT>* __restrict__ V, cd* x) {
+// x = sum_k coef_k V_k over the completed columns (complex FP64 vector, or FP32 block vectors).
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_x(GmCols C, int m, int n, const cplx<VT>* __restrict__ V,
+                                                     cplx<XT>* x) {
   const GmLayout L{m, 1};
+  const int r = blockIdx.y;
+  const GState* st = C.st + r;
+  const double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  x += r;
   const int jj = st->done == 3 ? 0 : st->j;
   extern __shared__ __align__(16) unsigned char gsm[];
   cplx<VT>* coef = reinterpret_cast<cplx<VT>*>(gsm);
@@ -412,7 +465,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_x(const GState* st, const dou
       ai = fma(c.re, v.im, ai);
       ai = fma(c.im, v.re, ai);
     }
-    x[i] = cd((double)ar, (double)ai);
+    x[(size_t)i * C.vs] = cplx<XT>((XT)ar, (XT)ai);
   }
 }
 
@@ -427,15 +480,23 @@ size_t gmres_scalar_doubles(int m, int n) {
   return GmLayout{m, gmres_grid(n)}.total();
 }
 
+static GmCols cols(const GmresBufs& B) {
+  return GmCols{B.state, B.gm, B.gd, B.gds, B.Vs, B.vs};
+}
+
 void gmres_enqueue_init(const GmresBufs& B, double tol, cudaStream_t s) {
-  const int G = gmres_grid(B.n);
+  const dim3 grid(gmres_grid(B.n), B.nrb);
+  const GmCols C = cols(B);
   note_launch();
   if (B.vec64)
-    k_gm_init<double><<<G, kGmThreads, 0, s>>>(B.state, B.gd, B.m, B.n, (const cd*)B.b, (cplx<double>*)B.V,
-                                                (cplx<double>*)B.q, tol);
+    k_gm_init<double, double><<<grid, kGmThreads, 0, s>>>(C, B.m, B.n, (const cd*)B.b, (cplx<double>*)B.V,
+                                                          (cplx<double>*)B.q, tol, B.tolv);
+  else if (B.b32)
+    k_gm_init<float, float><<<grid, kGmThreads, 0, s>>>(C, B.m, B.n, (const cf*)B.b, (cplx<float>*)B.V,
+                                                        (cplx<float>*)B.q, tol, B.tolv);
   else
-    k_gm_init<float><<<G, kGmThreads, 0, s>>>(B.state, B.gd, B.m, B.n, (const cd*)B.b, (cplx<float>*)B.V,
-                                               (cplx<float>*)B.q, tol);
+    k_gm_init<float, double><<<grid, kGmThreads, 0, s>>>(C, B.m, B.n, (const cd*)B.b, (cplx<float>*)B.V,
+                                                         (cplx<float>*)B.q, tol, B.tolv);
   AC3D_CUDA(cudaGetLastError());
 }
 
@@ -444,51 +505,64 @@ size_t gmres_update_smem(int m) {
   return std::max(sizeof(cplx<double>) * ((size_t)m + 1), sizeof(double) * 2 * (3 * (size_t)m + 3));
 }
 
+// The Gram-Schmidt passes of one iteration, after the matvec into B.W.
 template <typename VT>
-static void enqueue_one(const GmresBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, bool first,
-                        cudaStream_t s) {
-  const int G = gmres_grid(B.n);
+static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
+  const dim3 grid(gmres_grid(B.n), B.nrb);
   const size_t smem = gmres_update_smem(B.m);
-  MatvecEpilogue ep;  // no fused dots
-  launch_matvec_ex(DP, H, tr, B.vec64, B.q, B.W, nullptr, ep, &B.state->done, s, nullptr, !first);
-  launch_k(true, k_gm_dots<VT>, dim3(G), dim3(kGmThreads), 0, s, B.state, B.gd, B.m, B.n,
-           (const cplx<VT>*)B.V, (const cplx<VT>*)B.W, 0);
+  const GmCols C = cols(B);
+  launch_k(true, k_gm_dots<VT>, grid, dim3(kGmThreads), 0, s, C, B.m, B.n, (const cplx<VT>*)B.V,
+           (const cplx<VT>*)B.W, 0);
   if (B.reorth) {
-    launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
-             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 0);
-    launch_k(true, k_gm_dots<VT>, dim3(G), dim3(kGmThreads), 0, s, B.state, B.gd, B.m, B.n,
-             (const cplx<VT>*)B.V, (const cplx<VT>*)B.W2, 1);
-    launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
-             (cplx<VT>*)B.V, (const cplx<VT>*)B.W2, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 1, 1);
+    launch_k(true, k_gm_update<VT>, grid, dim3(kGmThreads), smem, s, C, B.m, B.n, (cplx<VT>*)B.V,
+             (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 0);
+    launch_k(true, k_gm_dots<VT>, grid, dim3(kGmThreads), 0, s, C, B.m, B.n, (const cplx<VT>*)B.V,
+             (const cplx<VT>*)B.W2, 1);
+    launch_k(true, k_gm_update<VT>, grid, dim3(kGmThreads), smem, s, C, B.m, B.n, (cplx<VT>*)B.V,
+             (const cplx<VT>*)B.W2, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 1, 1);
   } else {
-    launch_k(true, k_gm_update<VT>, dim3(G), dim3(kGmThreads), smem, s, B.state, B.gd, B.m, B.n,
-             (cplx<VT>*)B.V, (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 1);
+    launch_k(true, k_gm_update<VT>, grid, dim3(kGmThreads), smem, s, C, B.m, B.n, (cplx<VT>*)B.V,
+             (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 1);
   }
 }
 
 void gmres_enqueue_iterations(const GmresBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, int count,
                               cudaStream_t s) {
   for (int i = 0; i < count; i++) {
+    MatvecEpilogue ep;  // no fused dots
+    launch_matvec_ex(DP, H, tr, B.vec64, B.q, B.W, nullptr, ep, &B.gm->done_all, s, nullptr, i > 0);
     if (B.vec64)
-      enqueue_one<double>(B, DP, H, tr, i == 0, s);
+      enqueue_gs<double>(B, s);
     else
-      enqueue_one<float>(B, DP, H, tr, i == 0, s);
+      enqueue_gs<float>(B, s);
+  }
+}
+
+void gmres_enqueue_iterations_block(const GmresBufs& B, const MultiBufs& MB, const DevPartition& DP,
+                                    const DevHMat& H, int count, cudaStream_t s) {
+  for (int i = 0; i < count; i++) {
+    launch_mmatvec(DP, H, MB, B.q, B.W, nullptr, nullptr, &B.gm->done_all, s);
+    enqueue_gs<float>(B, s);
   }
 }
 
 void gmres_enqueue_finish(const GmresBufs& B, void* x, cudaStream_t s) {
   const int G = gmres_grid(B.n);
+  const GmCols C = cols(B);
   note_launch();
-  k_gm_solve<<<1, kGmThreads, sizeof(double) * 2 * (size_t)B.m, s>>>(B.state, B.gd, B.m, G);
+  k_gm_solve<<<dim3(1, B.nrb), kGmThreads, sizeof(double) * 2 * (size_t)B.m, s>>>(C, B.m, G);
   AC3D_CUDA(cudaGetLastError());
-  const int gx = std::max(1, std::min((B.n + kGmThreads - 1) / kGmThreads, 4 * device_sm_count()));
+  const dim3 gx(std::max(1, std::min((B.n + kGmThreads - 1) / kGmThreads, 4 * device_sm_count())), B.nrb);
   note_launch();
   if (B.vec64)
-    k_gm_x<double><<<gx, kGmThreads, sizeof(cplx<double>) * (size_t)B.m, s>>>(B.state, B.gd, B.m, B.n,
-                                                                              (const cplx<double>*)B.V, (cd*)x);
+    k_gm_x<double, double><<<gx, kGmThreads, sizeof(cplx<double>) * (size_t)B.m, s>>>(
+        C, B.m, B.n, (const cplx<double>*)B.V, (cplx<double>*)x);
+  else if (B.b32)
+    k_gm_x<float, float><<<gx, kGmThreads, sizeof(cplx<float>) * (size_t)B.m, s>>>(
+        C, B.m, B.n, (const cplx<float>*)B.V, (cplx<float>*)x);
   else
-    k_gm_x<float><<<gx, kGmThreads, sizeof(cplx<float>) * (size_t)B.m, s>>>(B.state, B.gd, B.m, B.n,
-                                                                            (const cplx<float>*)B.V, (cd*)x);
+    k_gm_x<float, double><<<gx, kGmThreads, sizeof(cplx<float>) * (size_t)B.m, s>>>(
+        C, B.m, B.n, (const cplx<float>*)B.V, (cplx<double>*)x);
   AC3D_CUDA(cudaGetLastError());
 }
 

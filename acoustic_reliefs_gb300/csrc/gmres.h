@@ -18,15 +18,30 @@ struct GState {
   int pad2;
 };
 
-// Device buffers of one cycle. vec64: 0 complex FP32 vectors (FP32 H-matrix and arithmetic),
+// Completion of a batch of cycles (one per right-hand side): done_all becomes 1 when every cycle
+// of the batch has ended. The matvec passes read it to skip their work after the last one.
+struct GMulti {
+  int ndone;     // cycles that have ended
+  int done_all;
+  int pad[2];
+};
+
+// Device buffers of one cycle, or of a batch of nrb independent cycles that share their matvecs
+// (column r: state st + r, scalars gd + r gds, basis V + r Vs elements; the matvec input q and
+// output W, the right-hand side b and the solution are block vectors with element stride vs). vec64: 0 complex FP32 vectors (FP32 H-matrix and arithmetic),
 // 1 complex FP64 vectors (FP64 H-matrix).
 struct GmresBufs {
   int n = 0, m = 0, vec64 = 0;
-  void* b = nullptr;   // right-hand side, complex FP64 (n)
+  int nrb = 1, vs = 1;   // cycles in the batch; element stride of the block vectors
+  size_t gds = 0, Vs = 0;
+  GMulti* gm = nullptr;
+  const double* tolv = nullptr;  // per-cycle relative tolerances (batch), else the scalar one
+  int b32 = 0;           // 1: the right-hand side and the solution are complex FP32 (batch)
+  void* b = nullptr;   // right-hand side, complex FP64 (n), or FP32 block vectors (b32)
   void* V = nullptr;   // basis, (m + 1) x n vectors of the vector type
   void* q = nullptr;   // the next matvec's input (n)
   void* W = nullptr;   // the matvec's output (n)
-  void* W2 = nullptr;  // the first Gram-Schmidt pass's result (n), when there are two
+  void* W2 = nullptr;  // the first Gram-Schmidt pass's result (n per cycle), when there are two
   int reorth = 0;      // 1: two classical Gram-Schmidt passes per iteration (FP32 vectors)
   double* gd = nullptr;  // gmres_scalar_doubles(m, n) doubles
   GState* state = nullptr;
@@ -38,7 +53,13 @@ size_t gmres_update_smem(int m);
 void gmres_enqueue_init(const GmresBufs& B, double tol, cudaStream_t s);
 void gmres_enqueue_iterations(const GmresBufs& B, const DevPartition& DP, const DevHMat& H, bool transposed,
                               int count, cudaStream_t s);
-// x (complex FP64, n) = the cycle's solution: the least-squares coefficients applied to the basis
+// x = the cycle's solution: the least-squares coefficients applied to the basis (complex FP64,
+// n; or the FP32 block vectors of a batch)
 void gmres_enqueue_finish(const GmresBufs& B, void* x, cudaStream_t s);
+struct MultiBufs;
+// A batch's iterations: one block matvec of all the cycles' inputs (the block solver's passes and
+// buffers in MB), then every cycle's Gram-Schmidt passes.
+void gmres_enqueue_iterations_block(const GmresBufs& B, const MultiBufs& MB, const DevPartition& DP,
+                                    const DevHMat& H, int count, cudaStream_t s);
 
 }  // namespace ac3d

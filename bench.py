@@ -531,7 +531,9 @@ def run_gpu(args):
                  "block_iterations": stm["iterations"], "refinement_steps": stm["outer_steps"],
                  "max_rel_residual": stm["rel_residual"],
                  "pressure_rel_err_vs_single_solve": float(np.linalg.norm(P[0] - y_mixed) / np.linalg.norm(y_mixed)),
-                 "note": "host API call (ac3d_solve_multi), assembly + block BiCGSTAB + receivers per block"}
+                 "note": "host API call (ac3d_solve_multi), assembly + block solve + receivers per block; "
+                         + ("one GMRES cycle per direction sharing each block matvec" if args.krylov == "gmres"
+                            else "block BiCGSTAB")}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

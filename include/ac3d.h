@@ -82,7 +82,8 @@ int ac3d_set_solver(ac3d_ctx* ctx, int max_iterations, double inner_tol, int max
  * vectors (1..600; 0: 300). GMRES stops on the same relative residual; each cycle of at most
  * `restart` iterations is followed by a true-residual check of the refinement loop, which starts
  * the next cycle if needed (at most max_outer cycles; max_iterations applies to BiCGSTAB only).
- * Block solves (ac3d_solve_multi) always use block BiCGSTAB. No reference counterpart. */
+ * Block solves (ac3d_solve_multi) then run one GMRES cycle per direction, the cycles sharing each
+ * block matvec, instead of block BiCGSTAB. No reference counterpart. */
 int ac3d_set_krylov(ac3d_ctx* ctx, int method, int restart);
 /* Replace the receivers used by value / values / band_value / gradient (default: the
  * hemisphere of compute_listener_pts, helpers.cpp:52-65). */
