@@ -9,12 +9,18 @@
 // that the vector the update pass writes is the next matvec's input without a normalisation pass:
 //   W = A V_j;  h_kj = s_k s_j (V_k^H W);  V_{j+1} = s_j W - sum_k (h_kj s_k) V_k;
 //   h_{j+1,j} = |V_{j+1}|,  s_{j+1} = 1 / h_{j+1,j}.
-// Per iteration: the matvec (into W), a dot pass (the j + 1 dots, per-CTA partials reduced by the
-// last CTA in fixed order) and an update pass (V_{j+1}, its norm, and in the last CTA the Givens
-// rotation of the new Hessenberg column and the residual estimate |g_{j+1}|). Vectors and their
-// arithmetic, the dots and the norms are in the solve's vector type (FP32 for the mixed-precision
-// inner solve, FP64 for the FP64 solve); the Hessenberg matrix, the rotations and the scalars are
-// FP64. No atomics touch floating-point sums, so a solve is bit-reproducible.
+// Per iteration: the matvec (into W), then per Gram-Schmidt pass a dot pass (the j + 1 dots,
+// per-CTA partials reduced by the last CTA in fixed order) and an update pass; the final update
+// writes V_{j+1} and its norm, and its last CTA rotates the new Hessenberg column and updates the
+// residual estimate |g_{j+1}|. FP32 cycles take two passes (one loses orthogonality over long
+// cycles), FP64 cycles one. Vectors and their arithmetic, the dots and the norms are in the
+// solve's vector type (FP32 for the mixed-precision inner solve, FP64 for the FP64 solve); the
+// Hessenberg matrix, the rotations and the scalars are FP64. No atomics touch floating-point sums,
+// so a solve is bit-reproducible.
+//
+// Batches: the kernels take the cycle as the grid's y index, so nrb independent cycles (one per
+// right-hand side of a block solve) run together and share each block matvec; their inputs and
+// outputs are element-major block vectors (stride nrb).
 #include <algorithm>
 
 #include "common.cuh"
@@ -157,9 +163,8 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_init(GmCols C, int m, int n, 
 
 // One Gram-Schmidt pass, dots: h_k = s_k sx V_k^H X for k = 0..j, X the matvec output (sx = s_j,
 // first pass) or the first pass's result (sx = 1, second pass). Per-CTA partials over the CTA's
-// elements, each warp four vectors at a time (twenty loads in flight per lane); the last CTA sums
-// them in CTA order, sets (first pass) or adds to (second pass) the Hessenberg column and writes
-// the update coefficients h_k s_k.
+// elements, each warp four vectors at a time; the last CTA sums them in CTA order, sets (first
+// pass) or adds to (second pass) the Hessenberg column and writes the update coefficients h_k s_k.
 template <typename VT>
 __global__ void __launch_bounds__(kGmThreads) k_gm_dots(GmCols C, int m, int n, const cplx<VT>* __restrict__ V,
                                                         const cplx<VT>* __restrict__ X, int second) {
