@@ -10,9 +10,10 @@
 //   W = A V_j;  h_kj = s_k s_j (V_k^H W);  V_{j+1} = s_j W - sum_k (h_kj s_k) V_k;
 //   h_{j+1,j} = |V_{j+1}|,  s_{j+1} = 1 / h_{j+1,j}.
 // Per iteration: the matvec (into W), then per Gram-Schmidt pass a dot pass (the j + 1 dots,
-// per-CTA partials reduced by the last CTA in fixed order) and an update pass; the final update
-// writes V_{j+1} and its norm, and its last CTA rotates the new Hessenberg column and updates the
-// residual estimate |g_{j+1}|. FP32 cycles take two passes (one loses orthogonality over long
+// per-CTA partials reduced by the last CTA in fixed order) and an update pass; with two passes the
+// first update also computes the second pass's dots. The final update writes V_{j+1} and its
+// norm, and its last CTA rotates the new Hessenberg column and updates the residual estimate
+// |g_{j+1}|. FP32 cycles take two passes (one loses orthogonality over long
 // cycles), FP64 cycles one. Vectors and their arithmetic, the dots and the norms are in the
 // solve's vector type (FP32 for the mixed-precision inner solve, FP64 for the FP64 solve); the
 // Hessenberg matrix, the rotations and the scalars are FP64. No atomics touch floating-point sums,
@@ -161,33 +162,12 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_init(GmCols C, int m, int n, 
   }
 }
 
-// One Gram-Schmidt pass, dots: h_k = s_k sx V_k^H X for k = 0..j, X the matvec output (sx = s_j,
-// first pass) or the first pass's result (sx = 1, second pass). Per-CTA partials over the CTA's
-// elements, each warp four vectors at a time; the last CTA sums them in CTA order, sets (first
-// pass) or adds to (second pass) the Hessenberg column and writes the update coefficients h_k s_k.
+// Per-CTA partial dots conj(V_k) . X over the CTA's elements (X staged in shared memory as xsm,
+// len elements from lo) for k = 0..j, each warp four vectors at a time.
 template <typename VT>
-__global__ void __launch_bounds__(kGmThreads) k_gm_dots(GmCols C, int m, int n, const cplx<VT>* __restrict__ V,
-                                                        const cplx<VT>* __restrict__ X, int second) {
-  grid_dep_wait();  // X comes from the kernel just before
-  grid_dep_launch();
-  const int r = blockIdx.y;
-  GState* st = C.st + r;
-  if (st->done) return;
-  double* gd = C.gd + r * C.gds;
-  V += r * C.Vs;
-  // X: the matvec output (block vectors) on the first pass, the first pass's result (one column
-  // of n) on the second
-  const int xstr = second ? 1 : C.vs;
-  X += second ? (size_t)r * n : (size_t)r;
-  const GmLayout L{m, (int)gridDim.x};
-  const int j = st->j;
+__device__ __forceinline__ void gs_dot_partials(const cplx<VT>* __restrict__ V, const cplx<VT>* xsm, int len,
+                                                int lo, int n, int j, const GmLayout& L, double* gd) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int lo, hi;
-  gm_range(n, lo, hi);
-  __shared__ cplx<VT> xsm[kSliceMax];
-  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) xsm[i - lo] = X[(size_t)i * xstr];
-  __syncthreads();
-  const int len = hi - lo;
   for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
     VT ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
     for (int t = lane; t < len; t += 32) {
@@ -216,7 +196,14 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_dots(GmCols C, int m, int n, 
           gd[L.part() + ((size_t)(kb + u) * L.G + blockIdx.x) * 2 + 1] = (double)ai[u];
         }
   }
-  if (!gm_last_cta(&st->ticket)) return;
+}
+
+// The last CTA's part of a dot pass: sums the partials in CTA order into h_k = s_k sx V_k^H X
+// (sx = s_j on the first pass, 1 on the second), sets (first pass) or adds to (second pass) the
+// Hessenberg column, writes the update coefficients h_k s_k and resets the ticket.
+template <typename VT>
+__device__ __forceinline__ void gs_dot_tail(GState* st, double* gd, const GmLayout& L, int j, int second) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double sx = second ? 1.0 : gd[L.s() + j];
   for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
     VT a[8];
@@ -258,6 +245,36 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_dots(GmCols C, int m, int n, 
   if (threadIdx.x == 0) st->ticket = 0u;
 }
 
+// One Gram-Schmidt pass, dots: h_k = s_k sx V_k^H X for k = 0..j, X the matvec output (sx = s_j,
+// first pass) or the first pass's result (sx = 1, second pass). Per-CTA partials over the CTA's
+// elements; the last CTA sums them in CTA order, sets (first pass) or adds to (second pass) the
+// Hessenberg column and writes the update coefficients h_k s_k.
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_dots(GmCols C, int m, int n, const cplx<VT>* __restrict__ V,
+                                                        const cplx<VT>* __restrict__ X, int second) {
+  grid_dep_wait();  // X comes from the kernel just before
+  grid_dep_launch();
+  const int r = blockIdx.y;
+  GState* st = C.st + r;
+  if (st->done) return;
+  double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  // X: the matvec output (block vectors) on the first pass, the first pass's result (one column
+  // of n) on the second
+  const int xstr = second ? 1 : C.vs;
+  X += second ? (size_t)r * n : (size_t)r;
+  const GmLayout L{m, (int)gridDim.x};
+  const int j = st->j;
+  int lo, hi;
+  gm_range(n, lo, hi);
+  __shared__ cplx<VT> xsm[kSliceMax];
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) xsm[i - lo] = X[(size_t)i * xstr];
+  __syncthreads();
+  gs_dot_partials<VT>(V, xsm, hi - lo, lo, n, j, L, gd);
+  if (!gm_last_cta(&st->ticket)) return;
+  gs_dot_tail<VT>(st, gd, L, j, second);
+}
+
 // One Gram-Schmidt pass, update: U = sx X - sum_k coef_k V_k (sx = s_j on the first pass, 1 on
 // the second). Not final: U goes to Y (the second pass's input). Final: U is V_{j+1} (also into q,
 // the next matvec's input), with |U|^2 partials; the last CTA rotates the new Hessenberg column,
@@ -290,6 +307,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n
   int lo, hi;
   gm_range(n, lo, hi);
   cplx<VT>* out = final_pass ? V + (size_t)(j + 1) * n : Y;
+  __shared__ cplx<VT> us[kSliceMax];  // U of this CTA's elements (not final: the second pass's dots)
   VT a = 0;
   for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const cplx<VT> x = X[(size_t)i * xstr];
@@ -323,9 +341,18 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n
     if (final_pass) {
       q[(size_t)i * C.vs] = u;
       a = fma(ur, ur, fma(ui, ui, a));
+    } else {
+      us[i - lo] = u;
     }
   }
-  if (!final_pass) return;
+  if (!final_pass) {
+    // the second pass's dots of U, from shared memory, with the same partials and tail as a dot
+    // pass (one kernel boundary fewer per iteration)
+    __syncthreads();
+    gs_dot_partials<VT>(V, us, hi - lo, lo, n, j, L, gd);
+    if (gm_last_cta(&st->ticket)) gs_dot_tail<VT>(st, gd, L, j, 1);
+    return;
+  }
   __shared__ VT sw[kGmWarps];
   a = warp_sum(a);
   if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = a;
@@ -519,10 +546,9 @@ static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
   launch_k(true, k_gm_dots<VT>, grid, dim3(kGmThreads), 0, s, C, B.m, B.n, (const cplx<VT>*)B.V,
            (const cplx<VT>*)B.W, 0);
   if (B.reorth) {
+    // first pass into W2, with the second pass's dots of W2
     launch_k(true, k_gm_update<VT>, grid, dim3(kGmThreads), smem, s, C, B.m, B.n, (cplx<VT>*)B.V,
              (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 0);
-    launch_k(true, k_gm_dots<VT>, grid, dim3(kGmThreads), 0, s, C, B.m, B.n, (const cplx<VT>*)B.V,
-             (const cplx<VT>*)B.W2, 1);
     launch_k(true, k_gm_update<VT>, grid, dim3(kGmThreads), smem, s, C, B.m, B.n, (cplx<VT>*)B.V,
              (const cplx<VT>*)B.W2, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 1, 1);
   } else {
