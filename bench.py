@@ -137,15 +137,21 @@ def workload(seed: int = 0):
     return R, meshes.semicircle(5.0, 181)
 
 
-def dist_init():
+def dist_init(backend=None):
+    """Replica ranks from the torchrun environment: NCCL on GPU machines (one GPU per rank), gloo
+    otherwise. Replicas exchange only the timing maximum, never data."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -160,9 +166,15 @@ def max_over_ranks(world, v: float) -> float:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_rank: int, ms_max: float) -> float:
+    """Units all replicas processed per second of the slowest replica's time."""
+    return world * units_per_rank / (ms_max / 1e3)
 
 
 class ClockSampler:
@@ -279,8 +291,9 @@ def reference_sample(R, Ls, full_iters):
 
 
 def run_reference(args):
-    world, rank, local = dist_init()
-    if rank != 0:
+    # rank 0 alone times the CPU reference on the host cores; the other ranks exit without work
+    # (no process group: the ranks exchange nothing)
+    if int(os.environ.get("RANK", "0")) != 0:
         return 0
     R, Ls = workload(0)
     # one untimed full solve fixes the iteration count the samples are scaled to
@@ -430,7 +443,7 @@ def run_gpu(args):
     clk = ClockSampler(local)
     value, total_ms, lat_sat, launches, res_m = served_c2(args, R, Ls, "mixed", args.steps, args.warmup, clocks=clk)
     total_ms = max_over_ranks(world, total_ms)
-    value = world * args.steps / (total_ms / 1e3)
+    value = whole_job_rate(world, args.steps, total_ms)
     barrier(world)
     # latency under a sustainable load: Poisson arrivals at half the saturated rate
     rate = 0.5 * value / world
