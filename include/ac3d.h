@@ -50,7 +50,7 @@ typedef struct ac3d_stats {
   int max_rank;
   long long hmat_bytes;     /* device bytes of the last H-matrix */
   int solves;               /* linear solves in the call */
-  int iterations;           /* BiCGSTAB iterations, summed over solves and refinement steps */
+  int iterations;           /* Krylov iterations, summed over solves and refinement steps */
   int outer_steps;          /* refinement steps (mixed precision) summed over solves */
   int matvecs;
   double rel_residual;      /* final |b - A x| / |b| of the last solve (FP64) */
@@ -113,6 +113,7 @@ int ac3d_pressures(ac3d_ctx* ctx, double frequency, const double* Ls, int L, dou
  * (context receivers). No host copies of inputs or outputs. */
 int ac3d_pressures_dev(ac3d_ctx* ctx, double frequency, const double* Ls_dev, int L, double* out_dev, void* stream);
 /* Forward solves of nrhs incident fields at one frequency against one H-matrix: block BiCGSTAB
+ * (or, with ac3d_set_krylov GMRES, one GMRES cycle per right-hand side sharing each block matvec)
  * over up to 16 right-hand sides at a time (more run in batches of 16), each matrix byte read once
  * per matvec for the whole block. kind: AC3D_INCIDENT_*; vecs: nrhs x 3 (plane-wave directions or
  * point-source positions). p_out (nrhs x L complex) receives the pressures at the receivers Ls
@@ -140,13 +141,13 @@ int ac3d_gradient_dev(ac3d_ctx* ctx, const double* x_dev, double* c_dev, double*
  * arrays instead of an OBJ path: leaf 128, factor 1.5, ACA and solver tolerance 1e-10, plane
  * wave e^{-ikx}, LL receivers on a circle of radius lrad in the xz plane. actual != 0 replaces the
  * reference's dense QR solve (sphere.h:65-69) by the exact operator (every leaf pair a dense
- * block, FP64) solved by BiCGSTAB to 1e-12. */
+ * block, FP64) solved to 1e-12 by the context's Krylov method (BiCGSTAB by default). */
 int ac3d_sphere(const double* Ps, int V, const int32_t* Es, int Ne, double freq, int LL, double lrad, int precision,
                 int actual, double* out);
 /* use_actual attribute (acoustics3d.h:49; adjoint.cpp:33-83,148-170): when on, band_value,
  * values, value and gradient (and their _dev forms) run on the exact operator -- the same tree
- * with every leaf pair a dense block, FP64, exact receiver product, BiCGSTAB to 1e-12 in place of
- * the reference's dense QR solve. pvals and surface_vals keep the H-matrix, as in the reference. */
+ * with every leaf pair a dense block, FP64, exact receiver product, solved to 1e-12 (BiCGSTAB by
+ * default) in place of the reference's dense QR solve. pvals and surface_vals keep the H-matrix, as in the reference. */
 int ac3d_set_actual(ac3d_ctx* ctx, int on);
 
 /* read_obj / write_obj -- read_obj.cpp:8-63. ac3d_read_obj reads "v" and triangle "f" records
