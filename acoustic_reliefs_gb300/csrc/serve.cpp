@@ -117,8 +117,9 @@ int admit_index(const ac3d_server* S) {
   return ac3d_admit_next(fp.data(), by.data(), n, S->budget, S->in_use, S->running);
 }
 
-void run_request(ac3d_server* S, ac3d_ctx* c, Request* r) {
-  MeshEntry& me = *S->meshes[r->mesh];
+// `me` was looked up under the server lock: add_mesh may grow the mesh list meanwhile, but an
+// entry itself never moves.
+void run_request(ac3d_server* S, ac3d_ctx* c, Request* r, MeshEntry& me) {
   c->m = me.m;
   c->mesh_set = true;
   c->prec = S->prec;
@@ -176,12 +177,13 @@ void worker(ac3d_server* S, int slot) {
     S->running++;
     c->krylov = S->krylov;
     c->gm_restart = S->gm_restart;
+    MeshEntry* me = S->meshes[r->mesh].get();
     lk.unlock();
 
     int rc = AC3D_OK;
     std::string msg;
     try {
-      run_request(S, c, r);
+      run_request(S, c, r, *me);
     } catch (const Error& e) {
       rc = e.code;
       msg = e.what();
@@ -198,8 +200,7 @@ void worker(ac3d_server* S, int slot) {
     S->in_use -= r->info.footprint_bytes;
     S->running--;
     if (rc == AC3D_OK) {
-      MeshEntry& me = *S->meshes[r->mesh];
-      me.lr_per_k = std::max(me.lr_per_k, (double)r->info.lr_entries / std::max(wavenumber(r->f), kFloorK));
+      me->lr_per_k = std::max(me->lr_per_k, (double)r->info.lr_entries / std::max(wavenumber(r->f), kFloorK));
     } else {
       S->err = msg;
     }
