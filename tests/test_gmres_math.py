@@ -2,8 +2,8 @@
 a test, not the product): unnormalised basis vectors V_k with scales s_k = 1 / |V_k|, two
 classical Gram-Schmidt passes with FP32 vectors and FP64 Hessenberg scalars, Givens rotations
 applied as the split chain x_{i+1} = conj(c_i) h_{i+1} - conj(s_i) x_i, back substitution and
-x = sum_k (y_k s_k) V_k. It must meet the residual of a direct solve and take the iterations of
-textbook GMRES."""
+x = sum_k (y_k s_k) V_k. It must agree with a direct solve and take the iterations of textbook
+GMRES."""
 import numpy as np
 
 
