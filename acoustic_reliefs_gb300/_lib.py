@@ -15,6 +15,7 @@ OK, ERR_ARG, ERR_STATE, ERR_INTERNAL, ERR_RESOURCE, ERR_CUDA, ERR_NOT_CONVERGED 
 PREC_MIXED, PREC_FP64 = 0, 1
 INCIDENT_POINT, INCIDENT_PLANE = 0, 1
 LISTENER_DENSE, LISTENER_ACA = 0, 1
+ASSEMBLY_DF, ASSEMBLY_FP32 = 0, 1
 
 # Exported symbols and their signatures (restype, argtypes); kept in step with include/ac3d.h.
 _P = ctypes.c_void_p
@@ -31,6 +32,8 @@ SIGNATURES = {
     "ac3d_set_listener_mode": (_I, [_P, _I]),
     "ac3d_set_solver": (_I, [_P, _I, _D, _I]),
     "ac3d_set_krylov": (_I, [_P, _I, _I]),
+    "ac3d_set_assembly": (_I, [_P, _I]),
+    "ac3d_get_ranks": (_I, [_P, _P, _I]),
     "ac3d_set_listeners": (_I, [_P, _P, _I]),
     "ac3d_set_mesh": (_I, [_P, _P, _I, _P, _I, _P]),
     "ac3d_set_diff_points": (_I, [_P, _P, _I]),
@@ -69,6 +72,7 @@ SIGNATURES = {
     "ac3d_server_create": (_I, [ctypes.POINTER(_P), _I, _I, ctypes.c_longlong]),
     "ac3d_server_destroy": (None, [_P]),
     "ac3d_server_set_krylov": (_I, [_P, _I, _I]),
+    "ac3d_server_set_assembly": (_I, [_P, _I]),
     "ac3d_server_last_error": (ctypes.c_char_p, [_P]),
     "ac3d_server_add_mesh": (_I, [_P, _P, _I, _P, _I, _I, _D, _D, _D, _P, ctypes.POINTER(_I)]),
     "ac3d_server_submit": (_I, [_P, _I, _D, _I, _P, _P, _I, ctypes.POINTER(ctypes.c_longlong)]),
@@ -87,7 +91,8 @@ class Stats(ctypes.Structure):
                 ("solves", _I), ("iterations", _I), ("outer_steps", _I), ("matvecs", _I),
                 ("rel_residual", _D), ("converged", _I),
                 ("ms_assemble", _D), ("ms_solve", _D), ("ms_listener", _D), ("ms_adjoint", _D),
-                ("ms_total", _D), ("kernel_launches", ctypes.c_longlong)]
+                ("ms_total", _D), ("kernel_launches", ctypes.c_longlong),
+                ("aca_entries_evaluated", ctypes.c_longlong), ("ms_graph", _D)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -99,7 +104,8 @@ class RequestInfo(ctypes.Structure):
                 ("footprint_bytes", ctypes.c_longlong), ("hmat_bytes", ctypes.c_longlong),
                 ("lr_entries", ctypes.c_longlong), ("near_entries", ctypes.c_longlong),
                 ("iterations", _I), ("outer_steps", _I), ("rel_residual", _D),
-                ("ms_assemble", _D), ("ms_solve", _D), ("ms_listener", _D)]
+                ("ms_assemble", _D), ("ms_solve", _D), ("ms_listener", _D), ("ms_graph", _D),
+                ("aca_entries_evaluated", ctypes.c_longlong)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

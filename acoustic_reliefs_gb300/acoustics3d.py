@@ -100,6 +100,13 @@ class DiffBEM:
         self._check(_L.lib().ac3d_set_precision(self._h, _PREC[precision]))
         self.precision = precision
 
+    def set_assembly(self, mode: str = "df") -> None:
+        """Arithmetic of the mixed-precision assembly: "df" (default) evaluates the near field and
+        runs ACA in double-float arithmetic, so the low-rank blocks have the FP64 path's pivots and
+        ranks and differ from its factors only by their FP32 rounding; "fp32" runs them in FP32."""
+        self._check(_L.lib().ac3d_set_assembly(self._h, {"df": _L.ASSEMBLY_DF, "fp32": _L.ASSEMBLY_FP32}[mode]))
+        self.assembly = mode
+
     def set_listener_mode(self, mode: str) -> None:
         """"dense": receiver matrix evaluated exactly on the fly (default); "aca": partially pivoted
         ACA with Q_ACA_tol, as the reference (aca.cpp:84-134)."""
@@ -131,6 +138,13 @@ class DiffBEM:
         self._check(_L.lib().ac3d_matvec_timing(self._h, int(iters), int(transposed), ctypes.byref(ms),
                                                 ctypes.byref(nb)))
         return ms.value, nb.value
+
+    def ranks(self) -> np.ndarray:
+        """ACA ranks of the admissible blocks (partition order) of the last solve's H-matrix."""
+        n = self.stats()["n_approx"]
+        r = np.zeros(max(n, 1), dtype=np.int32)
+        self._check(_L.lib().ac3d_get_ranks(self._h, _L.ptr(r), int(n)))
+        return r[:n]
 
     def stats(self) -> dict:
         s = _L.Stats()

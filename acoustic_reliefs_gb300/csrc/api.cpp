@@ -113,6 +113,69 @@ struct GpuTimer {
   }
 };
 
+// A captured chunk of solver iterations as an executable graph. If enqueueing throws during the
+// capture, the capture is ended and its graph discarded, so the stream is usable again; the
+// executable graph is destroyed on every exit path after the stream has drained (an error may be
+// thrown while a launch is in flight).
+struct CapturedGraph {
+  cudaStream_t s;
+  cudaGraphExec_t exec = nullptr;
+  long long nodes = 0;  // kernels per launch
+  // host milliseconds spent capturing and instantiating are added to *ms_host
+  template <typename F>
+  CapturedGraph(cudaStream_t st, double* ms_host, F&& enqueue) : s(st) {
+    const auto t0 = std::chrono::steady_clock::now();
+    struct Add {
+      double* acc;
+      std::chrono::steady_clock::time_point t0;
+      ~Add() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+    } add{ms_host, t0};
+    const long long before = t_kernel_launches;
+    AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue();
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamEndCapture(s, &g) == cudaSuccess && g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      unnote_launches(t_kernel_launches - before);
+      throw;
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    nodes = t_kernel_launches - before;
+    unnote_launches(nodes);  // captured, not launched
+    AC3D_CUDA(ec);
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) exec = nullptr;
+    AC3D_CUDA(ei);
+  }
+  CapturedGraph(const CapturedGraph&) = delete;
+  CapturedGraph& operator=(const CapturedGraph&) = delete;
+  void launch() {
+    AC3D_CUDA(cudaGraphLaunch(exec, s));
+    note_launch(nodes);
+  }
+  ~CapturedGraph() {
+    if (exec) {
+      cudaStreamSynchronize(s);
+      cudaGraphExecDestroy(exec);
+    }
+  }
+};
+
+// An event destroyed on every exit path.
+struct ScopedEvent {
+  cudaEvent_t e = nullptr;
+  ScopedEvent() { AC3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming)); }
+  ScopedEvent(const ScopedEvent&) = delete;
+  ScopedEvent& operator=(const ScopedEvent&) = delete;
+  ~ScopedEvent() {
+    if (e) cudaEventDestroy(e);
+  }
+};
+
 struct GraphCache {
   cudaGraphExec_t exec = nullptr;
   const void* key_h = nullptr;
@@ -131,6 +194,11 @@ using namespace ac3d;
 
 namespace ac3d {
 
+std::string not_converged_message(const ac3d_ctx* c) {
+  return c->krylov == AC3D_KRYLOV_GMRES ? "GMRES (restarted by the refinement loop) did not reach solver_tol"
+                                        : "BiCGSTAB did not reach solver_tol";
+}
+
 void require_mesh(ac3d_ctx* c) {
   if (!c->mesh_set) throw Error(AC3D_ERR_STATE, "No mesh set. Set one using set_mesh or precompute.");
 }
@@ -142,13 +210,18 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
   cudaStream_t s = c->stream;
   auto H = std::make_unique<DevHMat>();
   H->prec = prec;
+  H->pool_df = prec != PREC_FP64 && c->assembly == AC3D_ASSEMBLY_DF;
   H->k = k;
   H->maxk = c->maxk;
   const size_t cs = prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
+  const size_t pool_es = prec == PREC_FP64 || H->pool_df ? 16 : sizeof(cf);  // cd or cdf terms
   H->near.alloc((size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s);
   if (prec != PREC_FP64) H->xdf.alloc((size_t)c->m->Ne * sizeof(cd), s);
   AC3D_CUDA(cudaMemsetAsync(H->near.p, 0, (size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s));
-  launch_near_assembly(c->m->G, c->m->DP, *H, s);
+  if (H->pool_df)
+    launch_near_assembly_df(c->m->G, c->m->DP, *H, s);
+  else
+    launch_near_assembly(c->m->G, c->m->DP, *H, s);
   H->err.alloc(16, s);
   AC3D_CUDA(cudaMemsetAsync(H->err.p, 0, 16, s));
   H->ticket.alloc(16, s);
@@ -156,6 +229,7 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
 
   const int na = c->m->DP.na;
   H->rank.alloc((size_t)std::max(na, 1) * sizeof(int), s);
+  H->passes.alloc((size_t)std::max(na, 1) * sizeof(int), s);
   H->t_off.alloc((size_t)(na + 1) * sizeof(int), s);
   AC3D_CUDA(cudaMemsetAsync(H->rank.p, 0, (size_t)std::max(na, 1) * sizeof(int), s));
   if (na > 0) {
@@ -165,13 +239,16 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     if (cap <= 0) cap = std::min<int64_t>(c->m->worst_pool, 16 * c->m->sum_mn);
     cap = std::max<int64_t>(cap, 1024);
     for (int attempt = 0;; attempt++) {
-      H->pool.alloc((size_t)cap * cs, s);
+      H->pool.alloc((size_t)cap * pool_es, s);
       H->pool_cap = cap;
       AC3D_CUDA(cudaMemsetAsync(H->pool_used.p, 0, 16, s));
       // small blocks (one warp each) run on the side stream, concurrently with the large ones
       AC3D_CUDA(cudaEventRecord(c->ev_fork, s));
       AC3D_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-      launch_aca(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, s, c->side);
+      if (H->pool_df)
+        launch_aca_df(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, s, c->side);
+      else
+        launch_aca(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, s, c->side);
       AC3D_CUDA(cudaEventRecord(c->ev_join, c->side));
       AC3D_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
       unsigned long long hu[2];
@@ -194,20 +271,25 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     H->tvec.alloc(tcap * (prec == PREC_FP64 ? sizeof(cd) : sizeof(cf)), s);
     H->tvec64.alloc(tcap * sizeof(cd), s);
     H->ranks_host.resize(na);
+    std::vector<int> passes(na);
     AC3D_CUDA(cudaMemcpyAsync(H->ranks_host.data(), H->rank.p, na * sizeof(int), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaMemcpyAsync(passes.data(), H->passes.p, na * sizeof(int), cudaMemcpyDeviceToHost, s));
     AC3D_CUDA(cudaStreamSynchronize(s));
-    int64_t lr = 0;
+    int64_t lr = 0, ev = 0;
     int mx = 0;
     double sr = 0;
     for (int b = 0; b < na; b++) {
       int r = H->ranks_host[b];
       const int* q = &c->m->P.approx[4 * b];
       lr += (int64_t)r * ((q[1] - q[0]) + (q[3] - q[2]));
+      ev += (int64_t)passes[b] * ((q[1] - q[0]) + (q[3] - q[2]));
       mx = std::max(mx, r);
       sr += r;
     }
     H->lr_entries = lr;
+    H->aca_evaluated = ev;
     c->stats.lr_entries = lr;
+    c->stats.aca_entries_evaluated = ev;
     // per-leaf segments (U by row leaf, V by column leaf), then the pool is released
     int64_t sum_rn = 0, kf = 0, kt = 0;
     for (int b = 0; b < na; b++) sum_rn += (int64_t)H->ranks_host[b] * (c->m->P.approx[4 * b + 3] - c->m->P.approx[4 * b + 2]);
@@ -347,32 +429,21 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   const int maxit = c->maxit > 0 ? c->maxit : 2 * c->m->Ne;
   krylov_enqueue_init(B, vec64, tol, maxit, s);
   // capture one chunk of iterations as a graph and replay it until the state reports completion
-  cudaGraph_t graph;
-  const long long before = t_kernel_launches;
-  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  krylov_enqueue_iterations(B, c->m->DP, H, tr, vec64, c->chunk, s);
-  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
-  const long long nodes = t_kernel_launches - before;
-  unnote_launches(nodes);  // captured, not launched
-  cudaGraphExec_t exec;
-  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  AC3D_CUDA(cudaGraphDestroy(graph));
+  CapturedGraph g(s, &c->stats.ms_graph, [&] { krylov_enqueue_iterations(B, c->m->DP, H, tr, vec64, c->chunk, s); });
   int launched = 0;
   const int max_launch = maxit / c->chunk + 2;
   // keep one chunk in flight while the host reads the previous state
-  AC3D_CUDA(cudaGraphLaunch(exec, s));
-  note_launch(nodes);
+  g.launch();
   AC3D_CUDA(cudaMemcpyAsync(&c->h_state[0], B.state, sizeof(KState), cudaMemcpyDeviceToHost, s));
   launched++;
-  cudaEvent_t ev;
-  AC3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  ScopedEvent sev;
+  cudaEvent_t ev = sev.e;
   AC3D_CUDA(cudaEventRecord(ev, s));
   KState st{};
   while (true) {
     bool more = launched < max_launch;
     if (more) {
-      AC3D_CUDA(cudaGraphLaunch(exec, s));
-      note_launch(nodes);
+      g.launch();
       AC3D_CUDA(cudaMemcpyAsync(&c->h_state[launched & 1], B.state, sizeof(KState), cudaMemcpyDeviceToHost, s));
     }
     AC3D_CUDA(cudaEventSynchronize(ev));
@@ -389,8 +460,6 @@ int run_krylov(ac3d_ctx* c, const DevHMat& H, const KrylovBufs& B, bool tr, int 
   } else {
     AC3D_CUDA(cudaMemcpy(&st, B.state, sizeof(KState), cudaMemcpyDeviceToHost));
   }
-  AC3D_CUDA(cudaEventDestroy(ev));
-  AC3D_CUDA(cudaGraphExecDestroy(exec));
   *done = st.done;
   c->stats.matvecs += 2 * st.iter;
   return st.iter;
@@ -445,31 +514,20 @@ int run_gmres(ac3d_ctx* c, const DevHMat& H, const cd* b, cd* d, bool tr, double
   GmresBufs G = gmres_bufs(c, H, b);
   gmres_reset(G, s);
   gmres_enqueue_init(G, tol, s);
-  cudaGraph_t graph;
-  const long long before = t_kernel_launches;
-  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  gmres_enqueue_iterations(G, c->m->DP, H, tr, c->gm_chunk, s);
-  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
-  const long long nodes = t_kernel_launches - before;
-  unnote_launches(nodes);  // captured, not launched
-  cudaGraphExec_t exec;
-  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  AC3D_CUDA(cudaGraphDestroy(graph));
+  CapturedGraph g(s, &c->stats.ms_graph, [&] { gmres_enqueue_iterations(G, c->m->DP, H, tr, c->gm_chunk, s); });
   // keep one chunk in flight while the host reads the state after the previous one
   const int max_launch = (G.m + c->gm_chunk - 1) / c->gm_chunk + 1;
   int launched = 0;
-  AC3D_CUDA(cudaGraphLaunch(exec, s));
-  note_launch(nodes);
+  g.launch();
   AC3D_CUDA(cudaMemcpyAsync(&c->h_gstate[0], G.state, sizeof(GState), cudaMemcpyDeviceToHost, s));
   launched++;
-  cudaEvent_t ev;
-  AC3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  ScopedEvent sev;
+  cudaEvent_t ev = sev.e;
   AC3D_CUDA(cudaEventRecord(ev, s));
   while (true) {
     const bool more = launched < max_launch;
     if (more) {
-      AC3D_CUDA(cudaGraphLaunch(exec, s));
-      note_launch(nodes);
+      g.launch();
       AC3D_CUDA(cudaMemcpyAsync(&c->h_gstate[launched & 1], G.state, sizeof(GState), cudaMemcpyDeviceToHost, s));
     }
     AC3D_CUDA(cudaEventSynchronize(ev));
@@ -483,8 +541,6 @@ int run_gmres(ac3d_ctx* c, const DevHMat& H, const cd* b, cd* d, bool tr, double
   AC3D_CUDA(cudaMemcpyAsync(&c->h_gstate[0], G.state, sizeof(GState), cudaMemcpyDeviceToHost, s));
   AC3D_CUDA(cudaStreamSynchronize(s));
   st = c->h_gstate[0];
-  AC3D_CUDA(cudaEventDestroy(ev));
-  AC3D_CUDA(cudaGraphExecDestroy(exec));
   *done = st.done;
   c->stats.matvecs += st.j;
   return st.j;
@@ -622,26 +678,17 @@ int run_block_krylov(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vec
   cudaStream_t s = c->stream;
   const int maxit = c->maxit > 0 ? c->maxit : 2 * B.n;
   mkrylov_enqueue_init(B, maxit, s);
-  cudaGraph_t graph;
-  const long long before = t_kernel_launches;
-  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  mkrylov_enqueue_iterations(B, c->m->DP, H, c->chunk, s);
-  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
-  const long long nodes = t_kernel_launches - before;
-  unnote_launches(nodes);
-  cudaGraphExec_t exec;
-  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  AC3D_CUDA(cudaGraphDestroy(graph));
-  int head[4] = {0, 0, 0, 0};  // iter, maxit, done_all, nrb
-  const int max_launch = maxit / c->chunk + 2;
-  for (int launched = 0; launched < max_launch; launched++) {
-    AC3D_CUDA(cudaGraphLaunch(exec, s));
-    note_launch(nodes);
-    AC3D_CUDA(cudaMemcpyAsync(head, B.state, sizeof(head), cudaMemcpyDeviceToHost, s));
-    AC3D_CUDA(cudaStreamSynchronize(s));
-    if (head[2]) break;
+  {
+    CapturedGraph g(s, &c->stats.ms_graph, [&] { mkrylov_enqueue_iterations(B, c->m->DP, H, c->chunk, s); });
+    int head[4] = {0, 0, 0, 0};  // iter, maxit, done_all, nrb
+    const int max_launch = maxit / c->chunk + 2;
+    for (int launched = 0; launched < max_launch; launched++) {
+      g.launch();
+      AC3D_CUDA(cudaMemcpyAsync(head, B.state, sizeof(head), cudaMemcpyDeviceToHost, s));
+      AC3D_CUDA(cudaStreamSynchronize(s));
+      if (head[2]) break;
+    }
   }
-  AC3D_CUDA(cudaGraphExecDestroy(exec));
   KStateM st;
   AC3D_CUDA(cudaMemcpy(&st, B.state, sizeof(KStateM), cudaMemcpyDeviceToHost));
   done.assign(B.nrb, 0);
@@ -664,26 +711,17 @@ int run_block_gmres(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vect
   G.W2 = B.s;  // nrb columns of n
   gmres_reset(G, s);
   gmres_enqueue_init(G, 1.0, s);
-  cudaGraph_t graph;
-  const long long before = t_kernel_launches;
-  AC3D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  gmres_enqueue_iterations_block(G, B, c->m->DP, H, c->gm_chunk, s);
-  AC3D_CUDA(cudaStreamEndCapture(s, &graph));
-  const long long nodes = t_kernel_launches - before;
-  unnote_launches(nodes);
-  cudaGraphExec_t exec;
-  AC3D_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  AC3D_CUDA(cudaGraphDestroy(graph));
-  const int max_launch = (G.m + c->gm_chunk - 1) / c->gm_chunk + 1;
-  GMulti gm{};
-  for (int launched = 0; launched < max_launch; launched++) {
-    AC3D_CUDA(cudaGraphLaunch(exec, s));
-    note_launch(nodes);
-    AC3D_CUDA(cudaMemcpyAsync(&gm, G.gm, sizeof(GMulti), cudaMemcpyDeviceToHost, s));
-    AC3D_CUDA(cudaStreamSynchronize(s));
-    if (gm.done_all) break;
+  {
+    CapturedGraph g(s, &c->stats.ms_graph, [&] { gmres_enqueue_iterations_block(G, B, c->m->DP, H, c->gm_chunk, s); });
+    const int max_launch = (G.m + c->gm_chunk - 1) / c->gm_chunk + 1;
+    GMulti gm{};
+    for (int launched = 0; launched < max_launch; launched++) {
+      g.launch();
+      AC3D_CUDA(cudaMemcpyAsync(&gm, G.gm, sizeof(GMulti), cudaMemcpyDeviceToHost, s));
+      AC3D_CUDA(cudaStreamSynchronize(s));
+      if (gm.done_all) break;
+    }
   }
-  AC3D_CUDA(cudaGraphExecDestroy(exec));
   gmres_enqueue_finish(G, B.x, s);
   std::vector<GState> st(G.nrb);
   AC3D_CUDA(cudaMemcpyAsync(st.data(), G.state, G.nrb * sizeof(GState), cudaMemcpyDeviceToHost, s));
@@ -1163,6 +1201,7 @@ int ac3d_create(ac3d_ctx** out, int cluster_size, double radius_factor, const do
     AC3D_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
     uint64_t thr = UINT64_MAX;
     AC3D_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    noalloc_prepare();  // ac3d_far_field_noalloc then allocates nothing on this device
     upload_receivers(c, c->Ls.data(), (int)c->Ls.size() / 3, c->Ls_dev);
     AC3D_CUDA(cudaStreamSynchronize(c->stream));
   });
@@ -1236,6 +1275,12 @@ int ac3d_set_solver(ac3d_ctx* c, int max_iterations, double inner_tol, int max_o
   c->maxit = max_iterations;
   c->inner_tol = inner_tol;
   c->max_outer = max_outer;
+  return AC3D_OK;
+}
+
+int ac3d_set_assembly(ac3d_ctx* c, int mode) {
+  if (!c || (mode != AC3D_ASSEMBLY_DF && mode != AC3D_ASSEMBLY_FP32)) return AC3D_ERR_ARG;
+  c->assembly = mode;
   return AC3D_OK;
 }
 
@@ -1380,7 +1425,7 @@ int ac3d_pressures(ac3d_ctx* c, double f, const double* Ls, int L, double* out) 
     c->last_H = forward_one(c, f, recv, Lh, nL, c->x64.as<cd>(), y.as<cd>(), true);
     AC3D_CUDA(cudaMemcpyAsync(out, y.p, (size_t)nL * sizeof(cd), cudaMemcpyDeviceToHost, s));
     AC3D_CUDA(cudaStreamSynchronize(s));
-    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, not_converged_message(c));
   });
 }
 
@@ -1412,7 +1457,7 @@ int ac3d_pressures_dev(ac3d_ctx* c, double f, const double* Ls_dev, int L, doubl
     AC3D_CUDA(cudaEventRecord(ev, s));
     AC3D_CUDA(cudaStreamWaitEvent(us, ev, 0));
     AC3D_CUDA(cudaEventDestroy(ev));
-    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, not_converged_message(c));
   });
 }
 
@@ -1488,7 +1533,7 @@ int ac3d_solve_multi(ac3d_ctx* c, double f, int kind, const double* vecs, int nr
     }
     c->stats.ms_solve += ts.stop();
     c->last_H = std::move(H);
-    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, not_converged_message(c));
   });
 }
 
@@ -1504,7 +1549,7 @@ int ac3d_surface_values(ac3d_ctx* c, double f, double* out) {
     c->last_H = forward_one(c, f, nullptr, nullptr, 0, c->x64.as<cd>(), nullptr, true);
     AC3D_CUDA(cudaMemcpyAsync(out, c->x64.p, (size_t)c->m->Ne * sizeof(cd), cudaMemcpyDeviceToHost, s));
     AC3D_CUDA(cudaStreamSynchronize(s));
-    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, not_converged_message(c));
   });
 }
 
@@ -1797,6 +1842,17 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     // stored entries once; x read and y written once (FP32 or FP64); the FP32 shadow read once
     const long long es = H.prec == PREC_FP64 ? 16 : 8;
     *bytes = (c->m->P.near_total + H.lr_entries) * es + c->m->Ne * (vec64 == 0 ? 16LL : 32LL + (vec64 == 2 ? 8 : 0));
+  });
+}
+
+int ac3d_get_ranks(ac3d_ctx* c, int32_t* ranks, int n) {
+  if (!c || !ranks || n < 0) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    if (!c->last_H) throw Error(AC3D_ERR_STATE, "no H-matrix: call ac3d_pressures or ac3d_surface_values first");
+    const std::vector<int>& r = c->last_H->ranks_host;
+    if (n != (int)r.size())
+      throw Error(AC3D_ERR_ARG, "expected " + std::to_string(r.size()) + " admissible blocks, got " + std::to_string(n));
+    std::copy(r.begin(), r.end(), ranks);
   });
 }
 

@@ -108,6 +108,7 @@ struct AcaArgs {
   long long* term_off;
   int* rank;
   int* status;
+  int* passes;  // per block: rows (and columns) evaluated, or null
 };
 
 template <typename R, typename P4>
@@ -156,7 +157,10 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
       if (__syncthreads_and(ok)) zero_axes++;
     }
     if (zero_axes) {
-      if (tid == 0) A.rank[b] = 0;
+      if (tid == 0) {
+        A.rank[b] = 0;
+        if (A.passes) A.passes[b] = 0;
+      }
       return;
     }
   }
@@ -169,6 +173,7 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
   int nst = 0;           // stored (nonzero) terms; a term with u == 0 or v == 0 is exactly zero in
                          // every later residual, cross term and product, so it is not stored
   bool need_alloc = true;
+  int npass = 0;  // loop passes that evaluated a row and a column
   __syncthreads();
 
   while (iter < iter_lim) {
@@ -185,6 +190,7 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
       if (s_flag) break;
       need_alloc = false;
     }
+    npass++;
     cplx<R>* unew = A.pool + s_base;
     cplx<R>* vnew = unew + m;
     for (int p = tid; p < nst; p += T) uq[p] = A.pool[toff[p] + i];
@@ -278,7 +284,10 @@ __global__ void __launch_bounds__(kAcaThreads) aca_kernel(AcaArgs<R, P4> A) {
     iter++;
     __syncthreads();
   }
-  if (tid == 0) A.rank[b] = nst;
+  if (tid == 0) {
+    A.rank[b] = nst;
+    if (A.passes) A.passes[b] = npass;
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -370,14 +379,17 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (LPL == 8 ? 2 : 4) : 1)
       zero = __all_sync(0xffffffffu, ok);
     }
     if (zero) {
-      if (lane == 0) A.rank[b] = 0;
+      if (lane == 0) {
+        A.rank[b] = 0;
+        if (A.passes) A.passes[b] = 0;
+      }
       return;
     }
   }
 
   unsigned used_l = lane == 0 ? 1u : 0u;  // bit k: row lane + 32 k is used (row 0 first)
   double err = 0;
-  int i = 0, iter = 0, nst = 0;
+  int i = 0, iter = 0, nst = 0, npass = 0;
   bool need_alloc = true;
   long long base = 0;
   cplx<R> u_l[LPL], v_l[LPL];
@@ -396,6 +408,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (LPL == 8 ? 2 : 4) : 1)
       base = (long long)__shfl_sync(0xffffffffu, bb, 0);
       need_alloc = false;
     }
+    npass++;
     cplx<R>* unew = A.pool + base;
     cplx<R>* vnew = unew + m;
     for (int p = lane; p < nst; p += 32) uq[p] = A.pool[toff[p] + i];
@@ -501,7 +514,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? (LPL == 8 ? 2 : 4) : 1)
     iter++;
     __syncwarp();
   }
-  if (lane == 0) A.rank[b] = nst;
+  if (lane == 0) {
+    A.rank[b] = nst;
+    if (A.passes) A.passes[b] = npass;
+  }
 }
 
 __global__ void rank_scan_kernel(const int* __restrict__ rank, int na, int* t_off) {
@@ -597,13 +613,15 @@ void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double
     AcaArgs<double, double4> a{geo_view<double>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
                                G.cen.as<double4>(), H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cd>(),
                                H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
-                               H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
+                               H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1),
+                               H.passes.as<int>()};
     aca_launch_all(a, DP, max_rows, s, s_small);
   } else {
     AcaArgs<float, float4> a{geo_view<float>(G), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
                              G.cen32.as<float4>(), (float)H.k, eps, H.maxk, 1, iter_cap, H.pool.as<cf>(),
                              H.pool_cap, H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(),
-                             H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1)};
+                             H.rank.as<int>(), (int*)(H.pool_used.as<unsigned long long>() + 1),
+                             H.passes.as<int>()};
     aca_launch_all(a, DP, max_rows, s, s_small);
   }
 }
@@ -642,11 +660,11 @@ void launch_listener_aca(const DevGeometry& G, int prec, const void* pts, int L,
   if (iter_lim < 1) iter_lim = 1;
   if (prec == PREC_FP64) {
     AcaArgs<double, double4> a{geo_view<double>(G), block, order, (const double4*)pts, k, eps, maxk, 0, iter_lim,
-                               (cd*)pool, pool_cap, used, term_off, rank, status};
+                               (cd*)pool, pool_cap, used, term_off, rank, status, nullptr};
     aca_launch_t(a, 1, L, s);
   } else {
     AcaArgs<float, float4> a{geo_view<float>(G), block, order, (const float4*)pts, (float)k, eps, maxk, 0,
-                             iter_lim, (cf*)pool, pool_cap, used, term_off, rank, status};
+                             iter_lim, (cf*)pool, pool_cap, used, term_off, rank, status, nullptr};
     aca_launch_t(a, 1, L, s);
   }
 }

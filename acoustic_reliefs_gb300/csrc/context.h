@@ -28,6 +28,7 @@ struct ac3d_ctx {
   bool recompute = false;
   // extensions
   int prec = AC3D_PREC_MIXED;
+  int assembly = AC3D_ASSEMBLY_DF;  // arithmetic of the mixed-precision assembly
   int listener_mode = AC3D_LISTENER_DENSE;
   int maxit = 0;           // 0: twice the number of unknowns
   double inner_tol = 1e-6; // floor of the relative tolerance of each FP32 inner solve
@@ -81,6 +82,8 @@ namespace ac3d {
 
 struct ListenerLR;
 
+// Non-convergence message naming the context's Krylov method.
+std::string not_converged_message(const ac3d_ctx* c);
 double wavenumber(double f);  // k = 2 pi f / c, c = 344 m/s (helpers.h:8, constants.h:13)
 // Tree, partition and geometry of a mesh, device arrays on stream s (synchronised on return).
 std::shared_ptr<MeshState> build_mesh_state(const double* Ps, int V, const int32_t* Es, int Ne, int cluster_size,

@@ -6,13 +6,14 @@
 // rhs: point source e^{-ikr}/(4 pi r) (compute_G_r, helpers.cpp:46-50) or plane wave e^{-ik d.c}
 // (sphere_test::compute_b, sphere.h:22-26 with d = +x).
 #include "common.cuh"
+#include "entry_df.cuh"
 #include "internal.h"
 
 namespace ac3d {
 
 __global__ void geometry_kernel(const double* __restrict__ P, const int* __restrict__ E, int ne, double4* cen,
                                 double4* va, float4* cen32, float4* va32, ElemGeo<float>* eg32,
-                                ElemGeo<double>* eg64) {
+                                ElemGeo<double>* eg64, DfPt* cen_df, DfElem* el_df) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   int ia = E[3 * e], ib = E[3 * e + 1], ic = E[3 * e + 2];
@@ -53,6 +54,31 @@ __global__ void geometry_kernel(const double* __restrict__ P, const int* __restr
   f.n[2] = (float)n2;
   eg64[e] = g;
   eg32[e] = f;
+  // double-float copies: centroid, quadrature points a + m (b - a) + n (c - a) formed in FP64
+  DfPt pd;
+  pd.x = df_from_double(cx);
+  pd.y = df_from_double(cy);
+  pd.z = df_from_double(cz);
+  pd.pad[0] = pd.pad[1] = 0.f;
+  cen_df[e] = pd;
+  DfElem ed;
+  for (int q = 0; q < 6; q++)
+    for (int d = 0; d < 3; d++) ed.yq[q][d] = df_from_double(fma(quad_n(q), ac[d], fma(quad_m(q), ab[d], a[d])));
+  ed.n[0] = df_from_double(n0);
+  ed.n[1] = df_from_double(n1);
+  ed.n[2] = df_from_double(n2);
+  ed.pad[0] = ed.pad[1] = 0.f;
+  el_df[e] = ed;
+}
+
+// cos / sin of j 2 pi / 256 in FP64, stored as double-floats (the table of df_sincos)
+__global__ void df_table_kernel(float4* tab) {
+  const int j = threadIdx.x;
+  if (j >= kDfTab) return;
+  double sn, cs;
+  sincos(j * kDfStep, &sn, &cs);
+  const df64 c = df_from_double(cs), s = df_from_double(sn);
+  tab[j] = make_float4(c.hi, c.lo, s.hi, s.lo);
 }
 
 void launch_geometry(DevGeometry& G, cudaStream_t s) {
@@ -63,11 +89,20 @@ void launch_geometry(DevGeometry& G, cudaStream_t s) {
   G.va32.ensure(ne * sizeof(float4), s);
   G.eg32.ensure(ne * sizeof(ElemGeo<float>), s);
   G.eg64.ensure(ne * sizeof(ElemGeo<double>), s);
+  G.cen_df.ensure(ne * sizeof(DfPt), s);
+  G.el_df.ensure(ne * sizeof(DfElem), s);
+  if (G.df_tab.bytes == 0) {
+    G.df_tab.alloc(kDfTab * sizeof(float4), s);
+    note_launch();
+    df_table_kernel<<<1, kDfTab, 0, s>>>(G.df_tab.as<float4>());
+    AC3D_CUDA(cudaGetLastError());
+  }
   int T = 256;
   note_launch();
   geometry_kernel<<<(G.ne + T - 1) / T, T, 0, s>>>(G.P.as<double>(), G.E.as<int>(), G.ne, G.cen.as<double4>(),
                                                    G.va.as<double4>(), G.cen32.as<float4>(), G.va32.as<float4>(),
-                                                   G.eg32.as<ElemGeo<float>>(), G.eg64.as<ElemGeo<double>>());
+                                                   G.eg32.as<ElemGeo<float>>(), G.eg64.as<ElemGeo<double>>(),
+                                                   G.cen_df.as<DfPt>(), G.el_df.as<DfElem>());
   AC3D_CUDA(cudaGetLastError());
 }
 

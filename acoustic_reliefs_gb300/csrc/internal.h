@@ -146,6 +146,9 @@ struct DevGeometry {
   DevBuf cen32, va32;  // float4
   DevBuf eg32;       // ElemGeo<float>
   DevBuf eg64;       // ElemGeo<double>
+  DevBuf cen_df;     // DfPt: centroids as double-floats (mixed-precision entry evaluation)
+  DevBuf el_df;      // DfElem: quadrature points and normal as double-floats
+  DevBuf df_tab;     // float4 [256]: cos / sin of j 2 pi / 256 as double-floats
 };
 
 // One mesh: positions, elements in tree order, block partition (host and device) and element
@@ -176,12 +179,14 @@ constexpr int kWarpAcaTerms = 128;
 // An assembled H-matrix of (K - I/2) at one wavenumber.
 struct DevHMat {
   int prec = PREC_MIXED;  // storage: complex FP32 (mixed) or complex FP64
+  bool pool_df = false;   // mixed storage assembled in double-float: the ACA pool holds cdf terms
   double k = 0;
   int maxk = 100;
   DevBuf near;            // complex storage of all near blocks
   DevBuf pool;            // rank-1 terms (u | v) of all admissible blocks
   DevBuf term_off;        // int64 [na * maxk] offset of each term in the pool
   DevBuf rank;            // int [na]
+  DevBuf passes;          // int [na]: ACA loop passes (rows and columns evaluated) per block
   DevBuf t_off;           // int [na + 1] prefix of ranks
   DevBuf task_b;          // int [sum ranks] block of each stored term
   DevBuf task_off;        // int64 [sum ranks] pool offset of each stored term
@@ -204,6 +209,7 @@ struct DevHMat {
   int64_t pool_used_host = 0;
   std::vector<int> ranks_host;
   int64_t lr_entries = 0; // sum r (m + n)
+  int64_t aca_evaluated = 0;  // entries ACA evaluated: sum passes (m + n)
   size_t bytes() const {
     return near.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
            tvec.bytes + tvec64.bytes + useg.bytes + vseg.bytes + uidx.bytes + vidx.bytes + kpos_f.bytes +
@@ -222,6 +228,11 @@ void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat&
 // Large blocks run on s, small blocks (one warp each) on s_small, which may be another stream.
 void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s,
                 cudaStream_t s_small);
+// Mixed-precision assembly with double-float entries and ACA (FP64-accurate pivots and ranks,
+// FP32 storage): near field into H.near (cf), ACA terms into H.pool (cdf).
+void launch_near_assembly_df(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s);
+void launch_aca_df(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s,
+                   cudaStream_t s_small);
 void launch_rank_scan(const DevPartition& DP, DevHMat& H, cudaStream_t s);
 // Packs the pool into the U segments (row leaves, cols = false) or V segments (column leaves).
 void launch_pack(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_t s);
@@ -239,6 +250,9 @@ void launch_matvec(const DevPartition& DP, const DevHMat& H, int ne, bool transp
                    const void* x, void* y, const void* b_minus, const MatvecEpilogue& ep, cudaStream_t s);
 int matvec_grid(const DevPartition& DP, bool transposed);
 int device_sm_count();
+// Looks up the allocation-free far field's fixed scratch on the current device (noalloc.cu), so
+// that its first call there loads nothing.
+void noalloc_prepare();
 // Sets the shared-memory limits of the matvec kernels (call outside stream capture).
 void prepare_matvec_kernels();
 

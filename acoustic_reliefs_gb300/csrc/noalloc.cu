@@ -107,6 +107,9 @@ __global__ void far_noalloc_reduce(const cd* __restrict__ partial, int L, int S,
 }
 
 // Device address of g_far_scratch for each device, looked up once with that device current.
+// The lookup also loads this file's kernels on that device (CUDA loads modules lazily, and
+// loading reserves the array), so after it the entry point itself allocates nothing. The address
+// belongs to the device's primary context: it is not valid across a cudaDeviceReset.
 static cd* scratch_address(int dev) {
   static std::mutex mu;
   static cd* addr[kMaxDevices] = {nullptr};
@@ -115,12 +118,27 @@ static cd* scratch_address(int dev) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_far_scratch);
     if (e != cudaSuccess) {
+      cudaGetLastError();  // clears the error this lookup set
+      return nullptr;
+    }
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, far_noalloc_kernel) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, far_noalloc_reduce) != cudaSuccess) {
       cudaGetLastError();
       return nullptr;
     }
     addr[dev] = (cd*)p;
   }
   return addr[dev];
+}
+
+// Resolves the scratch address on the current device ahead of the first far-field call.
+void noalloc_prepare() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kMaxDevices)
+    scratch_address(dev);
+  else
+    cudaGetLastError();
 }
 
 }  // namespace ac3d
@@ -146,10 +164,23 @@ extern "C" int ac3d_far_field_noalloc(const double* Ps_dev, int V, const int32_t
   cd* scratch = scratch_address(dev);
   if (!scratch) return AC3D_ERR_CUDA;
   cudaStream_t s = (cudaStream_t)stream;
+  // each launch's own status: a pending error of unrelated earlier work is neither reported nor
+  // cleared here; the error state a failed launch sets is cleared
+  const cd* xc = (const cd*)x_dev;
+  void* a1[] = {(void*)&Ps_dev, (void*)&V, (void*)&Es_dev, (void*)&Ne, (void*)&Ls_dev, (void*)&L, (void*)&k,
+                (void*)&xc, (void*)&scratch, (void*)&S};
   note_launch();
-  far_noalloc_kernel<<<dim3((L + kNaRecv - 1) / kNaRecv, S), kNaThreads, 0, s>>>(Ps_dev, V, Es_dev, Ne, Ls_dev, L, k,
-                                                                                (const cd*)x_dev, scratch, S);
+  if (cudaLaunchKernel((const void*)far_noalloc_kernel, dim3((L + kNaRecv - 1) / kNaRecv, S), dim3(kNaThreads), a1,
+                       0, s) != cudaSuccess) {
+    cudaGetLastError();
+    return AC3D_ERR_CUDA;
+  }
+  cd* yc = (cd*)y_dev;
+  void* a2[] = {(void*)&scratch, (void*)&L, (void*)&S, (void*)&yc};
   note_launch();
-  far_noalloc_reduce<<<(L + 127) / 128, 128, 0, s>>>(scratch, L, S, (cd*)y_dev);
-  return cudaGetLastError() == cudaSuccess ? AC3D_OK : AC3D_ERR_CUDA;
+  if (cudaLaunchKernel((const void*)far_noalloc_reduce, dim3((L + 127) / 128), dim3(128), a2, 0, s) != cudaSuccess) {
+    cudaGetLastError();
+    return AC3D_ERR_CUDA;
+  }
+  return AC3D_OK;
 }

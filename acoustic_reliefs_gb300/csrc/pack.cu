@@ -11,6 +11,7 @@
 // uses to sum a term's per-leaf partial dots. Offsets are prefix sums over the ranks computed on
 // the device in a fixed order, so packing is deterministic. The pool itself is not needed after.
 #include "common.cuh"
+#include "df64.cuh"
 #include "internal.h"
 
 namespace ac3d {
@@ -58,10 +59,16 @@ __global__ void leaf_scan_kernel(const int* __restrict__ rank, const int* __rest
   }
 }
 
+// Stored value of a pool entry: the entry itself, or the FP32 rounding (the leading part) of a
+// double-float term of the mixed-precision assembly.
+template <typename R>
+__device__ __forceinline__ cplx<R> seg_value(const cplx<R>& v) { return v; }
+__device__ __forceinline__ cf seg_value(const cdf& v) { return cf(v.re.hi, v.im.hi); }
+
 // One CTA per leaf: copy the leaf's slices of every listed block's terms, write the segment
 // column indices (phase-1 output positions t_off[b] + q) and the first column of each entry.
-template <typename R>
-__global__ void pack_segments_kernel(const cplx<R>* __restrict__ pool, const long long* __restrict__ task_off,
+template <typename P, typename R>
+__global__ void pack_segments_kernel(const P* __restrict__ pool, const long long* __restrict__ task_off,
                                      const int* __restrict__ t_off, const int* __restrict__ rank,
                                      const int4* __restrict__ blocks, const int* __restrict__ leaf_start,
                                      const int* __restrict__ ptr, const int* __restrict__ items, int cols,
@@ -80,7 +87,7 @@ __global__ void pack_segments_kernel(const cplx<R>* __restrict__ pool, const lon
     const long long* to = task_off + t_off[b];
     for (int e = threadIdx.x; e < r * Rn; e += blockDim.x) {
       const int q = e / Rn, row = e - q * Rn;
-      dst[(long long)(kbase + q) * Rn + row] = pool[to[q] + off + row];
+      dst[(long long)(kbase + q) * Rn + row] = seg_value(pool[to[q] + off + row]);
     }
     for (int q = threadIdx.x; q < r; q += blockDim.x) idx[kbase + q] = t_off[b] + q;
     if (threadIdx.x == 0) kpos[pos[it]] = kseg[l] + kbase;  // block-major order
@@ -92,7 +99,7 @@ __global__ void pack_segments_kernel(const cplx<R>* __restrict__ pool, const lon
   }
 }
 
-template <typename R>
+template <typename P, typename R>
 static void pack_side(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_t s) {
   const int* ptr = cols ? DP.tr_lr_ptr.as<int>() : DP.fw_lr_ptr.as<int>();
   const int* items = cols ? DP.tr_lr.as<int>() : DP.fw_lr.as<int>();
@@ -106,7 +113,7 @@ static void pack_side(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_
                                       kseg.as<int>(), seg.as<long long>());
   AC3D_CUDA(cudaGetLastError());
   note_launch();
-  pack_segments_kernel<R><<<DP.nleaf, 256, 0, s>>>(H.pool.as<cplx<R>>(), H.task_off.as<long long>(),
+  pack_segments_kernel<P, R><<<DP.nleaf, 256, 0, s>>>(H.pool.as<P>(), H.task_off.as<long long>(),
                                                    H.t_off.as<int>(), H.rank.as<int>(), DP.blocks_a.as<int4>(),
                                                    DP.leaf_start.as<int>(), ptr, items, cols ? 1 : 0, kseg.as<int>(),
                                                    seg.as<long long>(), S.as<cplx<R>>(), idx.as<int>(),
@@ -117,9 +124,11 @@ static void pack_side(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_
 void launch_pack(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_t s) {
   if (DP.na == 0) return;
   if (H.prec == PREC_FP64)
-    pack_side<double>(DP, H, cols, s);
+    pack_side<cd, double>(DP, H, cols, s);
+  else if (H.pool_df)
+    pack_side<cdf, float>(DP, H, cols, s);
   else
-    pack_side<float>(DP, H, cols, s);
+    pack_side<cf, float>(DP, H, cols, s);
 }
 
 }  // namespace ac3d

@@ -68,6 +68,7 @@ using namespace ac3d;
 struct ac3d_server {
   int device = 0;
   int prec = AC3D_PREC_MIXED;
+  int assembly = AC3D_ASSEMBLY_DF;
   int krylov = AC3D_KRYLOV_BICGSTAB, gm_restart = 300;
   int64_t budget = 0, in_use = 0;
   int running = 0;
@@ -96,7 +97,9 @@ int64_t footprint(const ac3d_server* S, const MeshEntry& me, double f, int L) {
   int64_t lr = me.lr_per_k > 0 ? (int64_t)(me.lr_per_k * k * 1.25) : 12 * m.sum_mn;
   lr = std::min<int64_t>(std::max<int64_t>(lr, 1), std::max<int64_t>(m.worst_pool, 1));
   const int64_t pool = std::max<int64_t>(m.pool_hint[S->prec == AC3D_PREC_FP64 ? 1 : 0].load(), lr);
-  const int64_t H = (m.P.near_total + pool + lr) * es + (int64_t)m.P.aca_term_cap * 48;
+  // ACA pool terms: complex FP64, or double-float for the mixed path's default assembly
+  const int64_t pool_es = S->prec == AC3D_PREC_FP64 || S->assembly == AC3D_ASSEMBLY_DF ? 16 : 8;
+  const int64_t H = (m.P.near_total + lr) * es + pool * pool_es + (int64_t)m.P.aca_term_cap * 48;
   int64_t work = (int64_t)m.Ne * 176 + (int64_t)(m.DP.nleaf + 64) * 40 + (int64_t)L * 64 * 16 + (1 << 20);
   if (S->krylov == AC3D_KRYLOV_GMRES) {
     const int mm = std::min(S->gm_restart, m.Ne);
@@ -123,6 +126,7 @@ void run_request(ac3d_server* S, ac3d_ctx* c, Request* r, MeshEntry& me) {
   c->m = me.m;
   c->mesh_set = true;
   c->prec = S->prec;
+  c->assembly = S->assembly;
   c->aca_tol = me.aca_tol;
   c->solver_tol = me.solver_tol;
   c->cluster_size = me.cluster_size;
@@ -152,7 +156,9 @@ void run_request(ac3d_server* S, ac3d_ctx* c, Request* r, MeshEntry& me) {
   r->info.ms_assemble = st.ms_assemble;
   r->info.ms_solve = st.ms_solve;
   r->info.ms_listener = st.ms_listener;
-  if (!st.converged) throw Error(AC3D_ERR_NOT_CONVERGED, "BiCGSTAB did not reach solver_tol");
+  r->info.ms_graph = st.ms_graph;
+  r->info.aca_entries_evaluated = st.aca_entries_evaluated;
+  if (!st.converged) throw Error(AC3D_ERR_NOT_CONVERGED, not_converged_message(c));
 }
 
 void worker(ac3d_server* S, int slot) {
@@ -302,6 +308,13 @@ int ac3d_server_set_krylov(ac3d_server* S, int method, int restart) {
   std::lock_guard<std::mutex> lk(S->mu);
   S->krylov = method;
   S->gm_restart = restart > 0 ? restart : 300;
+  return AC3D_OK;
+}
+
+int ac3d_server_set_assembly(ac3d_server* S, int mode) {
+  if (!S || (mode != AC3D_ASSEMBLY_DF && mode != AC3D_ASSEMBLY_FP32)) return AC3D_ERR_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->assembly = mode;
   return AC3D_OK;
 }
 

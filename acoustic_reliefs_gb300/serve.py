@@ -32,7 +32,7 @@ def admit_next(footprints, bypassed, budget: int, in_use: int, n_running: int) -
 
 class Server:
     def __init__(self, slots: int = 4, precision: str = "mixed", hbm_budget: int = 0, device: int | None = None,
-                 krylov: str = "bicgstab", restart: int = 300):
+                 krylov: str = "bicgstab", restart: int = 300, assembly: str = "df"):
         L = _L.lib()
         if device is not None:
             rc = L.ac3d_select_device(int(device))
@@ -44,6 +44,7 @@ class Server:
             raise AC3DError(rc, "cannot create the server (no CUDA device or invalid arguments)")
         self._h = h
         self._check(L.ac3d_server_set_krylov(h, {"bicgstab": 0, "gmres": 1}[krylov], int(restart)))
+        self._check(L.ac3d_server_set_assembly(h, {"df": _L.ASSEMBLY_DF, "fp32": _L.ASSEMBLY_FP32}[assembly]))
         self.precision = precision
         self.slots = slots
         self._nL: dict[int, int] = {}

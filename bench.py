@@ -19,8 +19,8 @@ H-matrix with FP64 dots and FP64 iterative refinement), receiver far field.
 The H-matrix of one solve (~550 MB) is larger than L2, so no L2 flush is needed between steps.
 
 --impl reference times the FP64 CPU restatement of the reference algorithm (oracle/) on the
-host cores on the same workload. One untimed full solve fixes the iteration count; each step is
-then a bounded sample (assembly, a few BiCGSTAB iterations scaled to the full count, receivers).
+host cores on the same workload: each timed step is one full solve (mesh, assembly, BiCGSTAB,
+receivers); the untimed warm-up steps assemble only.
 """
 from __future__ import annotations
 
@@ -238,21 +238,14 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def traffic_profile(krylov):
-    """The committed ncu capture of the matvec variant the solver runs."""
-    return os.path.join("profiles", "gmres_solve_relief20k.md" if krylov == "gmres" else "hmatvec_relief20k_ncu.md")
-
-
 def measured_traffic(krylov):
-    """DRAM bytes of one matvec of this workload from the committed ncu capture (one pass of
-    dram__bytes_read.sum + dram__bytes_write.sum over the dot, reduce and gather kernels)."""
+    """DRAM bytes of one matvec of this workload, in the variant the solver runs, from the
+    committed ncu capture summarised in profiles/traffic.json (None if absent)."""
     try:
-        for line in open(os.path.join(ROOT, traffic_profile(krylov))):
-            if line.startswith("traffic_bytes_per_matvec:"):
-                return int(line.split(":")[1])
-    except OSError:
-        pass
-    return None
+        d = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        return int(d["matvec"][krylov]["traffic_bytes"]), d["matvec"][krylov]["command"]
+    except (OSError, KeyError, ValueError):
+        return None, None
 
 
 def cpu_baseline_sample(R, Ls, threads=None):
@@ -269,25 +262,12 @@ def cpu_baseline_sample(R, Ls, threads=None):
     return dt, cores, y, info
 
 
-REF_SAMPLE_ITERS = 8  # BiCGSTAB iterations run per reference step; the rest of the solve is scaled
-
-
-def reference_sample(R, Ls, full_iters):
-    """One bounded sample of a solve by the oracle: mesh + full H-matrix assembly, REF_SAMPLE_ITERS
-    BiCGSTAB iterations, ACA receivers. Returns (estimated full-solve seconds, wall seconds of the
-    sample): the iteration phase is scaled by full_iters / REF_SAMPLE_ITERS (each iteration costs
-    the same two H-matrix products and a fixed number of vector operations)."""
+def reference_warmup(R):
+    """Untimed warm-up step of the reference arm: mesh and H-matrix assembly by the oracle (page-in
+    of the code and the OpenMP pool; a full solve takes half a minute)."""
     import oracle
-    k = oracle.wavenumber(FREQ)
-    t0 = time.perf_counter()
     m = oracle.Mesh(R.Ps, R.Es, LEAF, FACTOR)
-    H = oracle.HMat(m, k, ACA_TOL)
-    t1 = time.perf_counter()
-    x, it, _ = H.solve(-m.rhs(k, DIRECTION, 1), SOLVER_TOL, REF_SAMPLE_ITERS)
-    t2 = time.perf_counter()
-    oracle.ListenerACA(m, k, Ls, ACA_TOL).apply(x)
-    t3 = time.perf_counter()
-    return (t1 - t0) + (t2 - t1) * full_iters / max(it, 1) + (t3 - t2), t3 - t0
+    oracle.HMat(m, oracle.wavenumber(FREQ), ACA_TOL)
 
 
 def run_reference(args):
@@ -296,31 +276,28 @@ def run_reference(args):
     if int(os.environ.get("RANK", "0")) != 0:
         return 0
     R, Ls = workload(0)
-    # one untimed full solve fixes the iteration count the samples are scaled to
-    t_full, cores, _, info = cpu_baseline_sample(R, Ls)
-    full_iters = int(info["iters"])
     for _ in range(args.warmup):
-        reference_sample(R, Ls, full_iters)
-    est, wall = [], []
+        reference_warmup(R)
+    times, iters = [], []
+    cores = 0
     for _ in range(args.steps):
-        e, w = reference_sample(R, Ls, full_iters)
-        est.append(e)
-        wall.append(w)
-    total = sum(est)
+        dt, cores, _, info = cpu_baseline_sample(R, Ls)  # one full solve per timed step
+        times.append(dt)
+        iters.append(int(info["iters"]))
+    total = sum(times)
     v = args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
         "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"},
-        "p50_ms": 1e3 * float(np.percentile(est, 50)), "p99_ms": 1e3 * float(np.percentile(est, 99)),
+        "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"per step: mesh + full H-matrix assembly, {REF_SAMPLE_ITERS} BiCGSTAB iterations "
-                                   f"(scaled to the {full_iters} of one full solve to 1e-6, measured once untimed: "
-                                   f"{t_full:.1f} s), ACA receivers; {np.mean(wall):.1f} s of CPU wall time per step; "
+                         "sample": f"per timed step one full FP64 solve of this workload by the oracle restatement "
+                                   f"(mesh, H-matrix assembly, BiCGSTAB to 1e-6 in {iters[0]} iterations, ACA "
+                                   f"receivers), OpenMP over {cores} threads; warm-up steps: mesh and assembly only; "
                                    f"the reference itself does not build here (empty Eigen submodule)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "full_solve_s": t_full,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -477,6 +454,16 @@ def run_gpu(args):
               "note": "one context, requests one after another, mesh and receivers resident (ac3d_pressures_dev)"}
     served_equal = all(np.array_equal(r[0], y_mixed) for r in res_m)
 
+    # assembly throughput of the last step: 6 kernel evaluations per near-field entry and per
+    # entry ACA evaluated (every row and column of every pass, the dropped converging term included)
+    evals = 6 * (st["near_entries"] + st["aca_entries_evaluated"])
+    assembly = {"ms": st["ms_assemble"], "near_entries": st["near_entries"],
+                "aca_entries_evaluated": st["aca_entries_evaluated"], "kernel_evaluations": int(evals),
+                "kernel_evaluations_per_s": evals / (st["ms_assemble"] / 1e3),
+                "stored_gbs": 8 * (st["near_entries"] + st["lr_entries"]) / (st["ms_assemble"] / 1e3) / 1e9,
+                "arithmetic": "double-float (about 47 bits) on the FP32 pipes, FP32 storage",
+                "note": "near field, ACA (two streams), packing; one context"}
+
     # roofline of the dominant kernel (H-matrix matvec) on the last step's H-matrix
     mv_ms, mv_bytes = bem.matvec_timing(50)
     peak, peak_kind = measured_peak()
@@ -591,10 +578,11 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(Ps_h.nbytes + Ls_h.nbytes),
                 "d2h_bytes_per_step": int(y_h.nbytes),
                 "path": "DiffBEM C-ABI (ac3d_set_points + ac3d_pressures), one request after another"},
+        "assembly": assembly,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": measured_traffic(args.krylov),
-                     "traffic_source": traffic_profile(args.krylov) + " (ncu, one matvec of this workload)",
+                     "frac": achieved / peak, "traffic": measured_traffic(args.krylov)[0],
+                     "traffic_source": "profiles/traffic.json: " + str(measured_traffic(args.krylov)[1]),
                      "kernel": "H-matrix matvec (dot + reduce + gather passes)",
                      "bytes_per_launch": int(mv_bytes), "ms_per_launch": mv_ms, "peak_kind": peak_kind},
         "clocks": clk.summary(),

@@ -37,6 +37,10 @@ extern "C" {
 #define AC3D_KRYLOV_BICGSTAB 0 /* the reference's solver (Eigen::BiCGSTAB, adjoint.cpp:92-95) */
 #define AC3D_KRYLOV_GMRES 1    /* GMRES: one matvec per iteration, restarted by the refinement loop */
 
+#define AC3D_ASSEMBLY_DF 0    /* mixed precision: entries and ACA in double-float (FP64-accurate
+                                 pivots and ranks), factors stored in FP32 (default) */
+#define AC3D_ASSEMBLY_FP32 1  /* mixed precision: entries and ACA in FP32 */
+
 #define AC3D_LISTENER_DENSE 0 /* receiver matrix evaluated exactly on the fly */
 #define AC3D_LISTENER_ACA 1   /* receiver matrix by ACA with Q_ACA_tol, as the reference */
 
@@ -57,6 +61,9 @@ typedef struct ac3d_stats {
   int converged;            /* 1 if every solve met solver_tol */
   double ms_assemble, ms_solve, ms_listener, ms_adjoint, ms_total;
   long long kernel_launches; /* kernels this library launched in the call (graph nodes counted) */
+  long long aca_entries_evaluated; /* matrix entries ACA evaluated (rows and columns of every pass,
+                                      6 kernel evaluations each) in the last assembly */
+  double ms_graph;          /* host milliseconds spent capturing and instantiating solver graphs */
 } ac3d_stats;
 
 /* DiffBEM(cluster_size, radius_factor, freq_bands, n_freqs, approx_ACA_tol, Q_ACA_tol,
@@ -85,6 +92,13 @@ int ac3d_set_solver(ac3d_ctx* ctx, int max_iterations, double inner_tol, int max
  * Block solves (ac3d_solve_multi) then run one GMRES cycle per direction, the cycles sharing each
  * block matvec, instead of block BiCGSTAB. No reference counterpart. */
 int ac3d_set_krylov(ac3d_ctx* ctx, int method, int restart);
+/* Arithmetic of the mixed-precision assembly (no effect on AC3D_PREC_FP64): AC3D_ASSEMBLY_DF
+ * (default) evaluates near-field entries and runs ACA (compute_ACA_block, aca.cpp:38-82) in
+ * double-float arithmetic on the FP32 pipes, so the low-rank blocks have the FP64 path's pivots
+ * and ranks and differ from its factors only by their FP32 rounding; AC3D_ASSEMBLY_FP32 runs
+ * them in FP32 (faster; pivots and ranks may differ from the FP64 path's where candidates are
+ * within FP32 rounding of each other). No reference counterpart. */
+int ac3d_set_assembly(ac3d_ctx* ctx, int mode);
 /* Replace the receivers used by value / values / band_value / gradient (default: the
  * hemisphere of compute_listener_pts, helpers.cpp:52-65). */
 int ac3d_set_listeners(ac3d_ctx* ctx, const double* Ls, int L);
@@ -188,6 +202,11 @@ int ac3d_get_stats(const ac3d_ctx* ctx, ac3d_stats* out);
  * + 8 Ne for the FP32 shadow of x the mixed BiCGSTAB reads; 16 Ne for the FP32 vectors of the
  * mixed GMRES). No reference counterpart. */
 int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_matvec, long long* bytes);
+/* ACA ranks (stored terms, after the dropped converging term; aca.cpp:78-79) of every admissible
+ * block of the H-matrix of the most recent ac3d_pressures / ac3d_surface_values call, in the
+ * order of ac3d_partition_get's approx list; n must equal that count (stats n_approx). No
+ * reference counterpart (the reference keeps them inside HMatrix, hmatrix.h:27-71). */
+int ac3d_get_ranks(ac3d_ctx* ctx, int32_t* ranks, int n);
 
 /* Receiver far field y_l = sum_j M(receiver l, element j) x_j (FP64), with every argument in
  * device memory: Ps_dev (V x 3 float64), Es_dev (Ne x 3 int32, the connectivity x is ordered by,
@@ -195,11 +214,17 @@ int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_
  * complex); k = 2 pi f / 344. It allocates no device memory: for callers that cannot allocate
  * at that point (a real-time audio callback, a frame loop, a host whose allocator owns the device
  * memory). Its scratch is a fixed 65536-entry (1 MiB) array reserved on every GPU that loads the
- * library; L above 65536 is rejected with AC3D_ERR_RESOURCE. The first call on a device looks up
- * that array's address, so make the first call on each device before any stream capture. All
+ * library; L above 65536 is rejected with AC3D_ERR_RESOURCE. It runs on this library's current
+ * device, which is not another CUDA runtime's (torch's) current device: select it with
+ * ac3d_select_device on the calling thread. The array's address is looked up once per device,
+ * which also loads the entry point's kernels there (CUDA loads modules lazily, and loading
+ * reserves the array): ac3d_create does this for its device, and otherwise the first call does
+ * it and may allocate, so make that first call before any stream capture and outside the
+ * allocation-free section. The address is not valid across a cudaDeviceReset of the device. All
  * calls share the array: calls that overlap on the GPU (different streams) race. Work is ordered
- * on `stream` (a cudaStream_t); the call does not wait for it. Elements whose indices fall
- * outside [0, V) are skipped. No counterpart in the reference (its far field is a host ACA
+ * on `stream` (a cudaStream_t); the call does not wait for it. A launch failure returns
+ * AC3D_ERR_CUDA; errors pending from earlier unrelated work are left alone. Elements whose
+ * indices fall outside [0, V) are skipped. No counterpart in the reference (its far field is a host ACA
  * product, aca.cpp:84-134 with adjoint.cpp:101-102). */
 int ac3d_far_field_noalloc(const double* Ps_dev, int V, const int32_t* Es_dev, int Ne, const double* x_dev, double k,
                            const double* Ls_dev, int L, double* y_dev, void* stream);
@@ -253,6 +278,8 @@ typedef struct ac3d_request_info {
   int iterations, outer_steps; /* Krylov iterations; refinement steps */
   double rel_residual;         /* final FP64 |b - A x| / |b| */
   double ms_assemble, ms_solve, ms_listener; /* device time of the phases */
+  double ms_graph;             /* host time capturing and instantiating solver graphs (within run_ms) */
+  long long aca_entries_evaluated; /* matrix entries the ACA of this request evaluated */
 } ac3d_request_info;
 
 /* precision: AC3D_PREC_*; hbm_budget_bytes <= 0 takes 85% of the device memory free at creation. */
@@ -262,6 +289,9 @@ void ac3d_server_destroy(ac3d_server* srv);
 /* Krylov method of the requests that start after the call (ac3d_set_krylov semantics). No
  * reference counterpart. */
 int ac3d_server_set_krylov(ac3d_server* srv, int method, int restart);
+/* Mixed-precision assembly arithmetic of the requests that start after the call
+ * (ac3d_set_assembly semantics). No reference counterpart. */
+int ac3d_server_set_assembly(ac3d_server* srv, int mode);
 const char* ac3d_server_last_error(const ac3d_server* srv);
 /* Registers a mesh (set_mesh semantics: Es_out, if given, receives the tree-ordered connectivity
  * the results refer to) with its H-matrix and solver parameters. */

@@ -224,6 +224,18 @@ class HMat:
         lib().orc_hmat_block_factors(self.h, b, _p(U), _p(V))
         return U.reshape(r, m).T, V.reshape(r, n)
 
+    def stored_ranks(self) -> np.ndarray:
+        """Per block, the ACA terms with u != 0 and v != 0. The reference keeps exactly-zero terms
+        (they come from coplanar panels, aca.cpp:56-60) in its rank count; they add nothing to any
+        product, and the GPU path does not store them."""
+        out = np.zeros(len(self.ranks), np.int32)
+        for b in range(len(self.ranks)):
+            if self.ranks[b] == 0:
+                continue
+            U, V = self.factors(b)
+            out[b] = int(np.sum(np.any(U != 0, axis=0) & np.any(V != 0, axis=1)))
+        return out
+
     def matvec(self, x, transposed=False) -> np.ndarray:
         x = _c(x)
         y = np.zeros_like(x)

@@ -4,8 +4,9 @@ sphere_c1.npz: the 1280-triangle icosphere case -- tree-ordered connectivity, re
 of the FP64 oracle with the reference's ACA receiver matrix (y_oracle) and with the exact receiver
 matrix (y_oracle_dense), and the analytic Mie series at the same receivers.
 relief_small.npz: the 5280-triangle relief case -- oracle receiver pressures (FP64, ACA 1e-4,
-tol 1e-6) with the exact (y_oracle) and ACA (y_oracle_aca) receiver matrix, surface solution and
-ranks, used by the GPU parity tests without re-running the oracle.
+tol 1e-6) with the exact (y_oracle) and ACA (y_oracle_aca) receiver matrix, surface solution,
+per-block ACA ranks (iterations, the reference's count) and stored ranks (terms with u != 0 and
+v != 0), used by the GPU parity tests without re-running the oracle.
 """
 import os
 import sys
@@ -36,8 +37,10 @@ def main():
     y, x, info = oracle.solve_pressures(m, k, c["vec"], 1, c["Ls"], c["aca_tol"], c["aca_tol"], c["tol"],
                                         listener="dense")
     ya = oracle.ListenerACA(m, k, c["Ls"], c["aca_tol"]).apply(x)
+    H = oracle.HMat(m, k, c["aca_tol"])
+    assert np.array_equal(H.ranks, info["ranks"])
     np.savez_compressed(os.path.join(out, "relief_small.npz"), Es_tree=m.Es, y_oracle=y, y_oracle_aca=ya,
-                        x_oracle=x, ranks=info["ranks"], iters=info["iters"])
+                        x_oracle=x, ranks=info["ranks"], ranks_stored=H.stored_ranks(), iters=info["iters"])
 
 
 if __name__ == "__main__":
