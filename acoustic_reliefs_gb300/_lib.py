@@ -33,7 +33,12 @@ SIGNATURES = {
     "ac3d_set_solver": (_I, [_P, _I, _D, _I]),
     "ac3d_set_krylov": (_I, [_P, _I, _I]),
     "ac3d_set_assembly": (_I, [_P, _I]),
+    "ac3d_set_tensor_cores": (_I, [_P, _I]),
     "ac3d_get_ranks": (_I, [_P, _P, _I]),
+    "ac3d_gradient_multi": (_I, [_P, _P, _P, _I, _P, _I, _P, _P, _P]),
+    "ac3d_block_matvec_timing": (_I, [_P, _I, _I, _I, _P, _P]),
+    "ac3d_relief_sizes": (_I, [_I, _I, _I, _I, _P, _P]),
+    "ac3d_relief_dev": (_I, [_D, _D, _D, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
     "ac3d_set_listeners": (_I, [_P, _P, _I]),
     "ac3d_set_mesh": (_I, [_P, _P, _I, _P, _I, _P]),
     "ac3d_set_diff_points": (_I, [_P, _P, _I]),

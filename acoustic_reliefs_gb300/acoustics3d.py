@@ -101,11 +101,17 @@ class DiffBEM:
         self.precision = precision
 
     def set_assembly(self, mode: str = "df") -> None:
-        """Arithmetic of the mixed-precision assembly: "df" (default) evaluates the near field and
-        runs ACA in double-float arithmetic, so the low-rank blocks have the FP64 path's pivots and
-        ranks and differ from its factors only by their FP32 rounding; "fp32" runs them in FP32."""
+        """Arithmetic of the mixed-precision assembly: "df" (default) evaluates the near field, the
+        admissible blocks' rows and columns and runs ACA in double-float arithmetic, so the low-rank
+        blocks have the FP64 path's pivots and ranks and every stored entry differs from the FP64
+        path's only by its FP32 rounding; "fp32" evaluates in FP32."""
         self._check(_L.lib().ac3d_set_assembly(self._h, {"df": _L.ASSEMBLY_DF, "fp32": _L.ASSEMBLY_FP32}[mode]))
         self.assembly = mode
+
+    def set_tensor_cores(self, on: bool = True) -> None:
+        """Block matvecs (pvals_multi, gradient_multi) form their dot pass on the tensor cores
+        (default) or on the FP32 CUDA cores."""
+        self._check(_L.lib().ac3d_set_tensor_cores(self._h, int(bool(on))))
 
     def set_listener_mode(self, mode: str) -> None:
         """"dense": receiver matrix evaluated exactly on the fly (default); "aca": partially pivoted
@@ -137,6 +143,14 @@ class DiffBEM:
         nb = ctypes.c_longlong()
         self._check(_L.lib().ac3d_matvec_timing(self._h, int(iters), int(transposed), ctypes.byref(ms),
                                                 ctypes.byref(nb)))
+        return ms.value, nb.value
+
+    def block_matvec_timing(self, nrb: int = 16, iters: int = 20, transposed: bool = False):
+        """(ms per block matvec of nrb right-hand sides, algorithmic bytes) on the last H-matrix."""
+        ms = ctypes.c_double()
+        nb = ctypes.c_longlong()
+        self._check(_L.lib().ac3d_block_matvec_timing(self._h, int(nrb), int(iters), int(transposed),
+                                                      ctypes.byref(ms), ctypes.byref(nb)))
         return ms.value, nb.value
 
     def ranks(self) -> np.ndarray:
@@ -205,6 +219,20 @@ class DiffBEM:
         c = ctypes.c_double()
         self._check(_L.lib().ac3d_gradient(self._h, _L.ptr(xx), ctypes.byref(c), _L.ptr(g)))
         return c.value, g
+
+    def gradient_multi(self, x, frequencies, directions):
+        """Multi-incidence objective (an extension): loss = 1 - mean over frequencies x plane-wave
+        directions of the single-frequency diffusion coefficient at the receivers (set_listeners),
+        with the heights x. Returns (loss, d loss / dx, coefficients (nf, nd))."""
+        xx = _f64(x)
+        fr = _f64(frequencies).reshape(-1)
+        dr = _f64(directions).reshape(-1, 3)
+        g = np.zeros(len(xx))
+        cf = np.zeros((len(fr), len(dr)))
+        loss = ctypes.c_double()
+        self._check(_L.lib().ac3d_gradient_multi(self._h, _L.ptr(xx), _L.ptr(fr), len(fr), _L.ptr(dr), len(dr),
+                                                 ctypes.byref(loss), _L.ptr(g), _L.ptr(cf)))
+        return loss.value, g, cf
 
     def value_dev(self, x_ptr: int | None, c_ptr: int, stream: int = 0) -> None:
         """value(x) with x (HH float64, or None for the stored heights) and c (one float64) in device

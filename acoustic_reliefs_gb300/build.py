@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(OUT_DIR, "libac3d.so")
 OBJ_DIR = os.path.join(HERE, "_build")
 
 SOURCES = ["api.cpp", "tree.cpp", "geometry.cu", "assemble.cu", "aca_df.cu", "matvec.cu", "pack.cu", "krylov.cu", "gmres.cu", "listener.cu",
-           "adjoint.cu", "noalloc.cu", "serve.cpp", "multi.cu", "tcselftest.cu", "obj.cpp", "texmap.cu"]
+           "adjoint.cu", "noalloc.cu", "serve.cpp", "multi.cu", "tcselftest.cu", "obj.cpp", "texmap.cu", "relief.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

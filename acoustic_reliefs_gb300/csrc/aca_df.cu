@@ -1,6 +1,8 @@
-// Mixed-precision assembly with FP64-accurate decisions: near-field entries and the ACA of the
-// admissible blocks evaluated in double-float arithmetic (about 47 bits, on the FP32 pipes),
-// stored in complex FP32.
+// Mixed-precision assembly with FP64-accurate entries: near-field entries, and the admissible
+// blocks' rows and columns with the ACA recursion, evaluated in double-float arithmetic (about 47
+// bits, on the FP32 pipes); everything is stored in complex FP32. Near-field entries of nearly
+// coplanar neighbours cancel in r.n, so FP32 evaluation from FP64 displacements is not enough
+// there (5.6e-5 instead of 1.3e-5 from the FP64 path on a 5280-triangle relief at 3.5 kHz).
 //
 // The ACA sequence is the reference's (compute_ACA_block, aca.cpp:38-82, argmax rules
 // aca.cpp:9-36) exactly as the FP32 / FP64 kernels of assemble.cu run it: first row pivot 0;
@@ -43,7 +45,8 @@ struct AcaDfArgs {
   long long* term_off;
   int* rank;
   int* status;
-  int* passes;  // per block: rows (and columns) evaluated
+  int* passes;     // per block: rows (and columns) evaluated, or null
+  int zero_guard;  // boundary blocks: v kept when v_j == 0 and exactly-zero blocks skipped
 };
 
 // One out-of-line copy of the entry (its loops are not unrolled into the callers' unrolled
@@ -144,7 +147,7 @@ __global__ void __launch_bounds__(256, LPL == 8 ? 1 : 2) aca_df_warp_kernel(AcaD
       zero_block(A, rs, m, cs, n, lane, 32, [](bool ok) { return __all_sync(0xffffffffu, ok) != 0; })) {
     if (lane == 0) {
       A.rank[b] = 0;
-      A.passes[b] = 0;
+      if (A.passes) A.passes[b] = 0;
     }
     return;
   }
@@ -281,7 +284,7 @@ __global__ void __launch_bounds__(256, LPL == 8 ? 1 : 2) aca_df_warp_kernel(AcaD
   }
   if (lane == 0) {
     A.rank[b] = nst;
-    A.passes[b] = npass;
+    if (A.passes) A.passes[b] = npass;
   }
 }
 
@@ -352,10 +355,11 @@ __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
   unsigned* used = reinterpret_cast<unsigned*>(toff + A.iter_cap);
   const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5;
 
-  if (iter_lim > 0 && zero_block(A, rs, m, cs, n, tid, T, [](bool ok) { return __syncthreads_and(ok) != 0; })) {
+  if (A.zero_guard && iter_lim > 0 &&
+      zero_block(A, rs, m, cs, n, tid, T, [](bool ok) { return __syncthreads_and(ok) != 0; })) {
     if (tid == 0) {
       A.rank[b] = 0;
-      A.passes[b] = 0;
+      if (A.passes) A.passes[b] = 0;
     }
     return;
   }
@@ -406,7 +410,7 @@ __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
     const cdf vj = vnew[j];
     for (int p = tid; p < nst; p += T) vq[p] = A.pool[toff[p] + m + j];
     __syncthreads();
-    const bool keep = df_is_zero(vj.re) && df_is_zero(vj.im);
+    const bool keep = A.zero_guard && df_is_zero(vj.re) && df_is_zero(vj.im);
     const CdfDivisor dv = keep ? CdfDivisor{cdf{}, 1.0f} : cdf_divisor(vj);
     df64 vn{0.0f, 0.0f};
     for (int c = tid; c < n; c += T) {
@@ -480,7 +484,7 @@ __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
   }
   if (tid == 0) {
     A.rank[b] = nst;
-    A.passes[b] = npass;
+    if (A.passes) A.passes[b] = npass;
   }
 }
 
@@ -528,7 +532,7 @@ void launch_aca_df(const DevGeometry& G, const DevPartition& DP, DevHMat& H, dou
               G.el_df.as<DfElem>(), G.df_tab.as<float4>(), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
               df_from_double(H.k), eps, H.maxk, H.maxk, H.pool.as<cdf>(), H.pool_cap,
               H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(), H.rank.as<int>(),
-              (int*)(H.pool_used.as<unsigned long long>() + 1), H.passes.as<int>()};
+              (int*)(H.pool_used.as<unsigned long long>() + 1), H.passes.as<int>(), 1};
   // same grouping and stream split as launch_aca: CTA blocks, then warp blocks up to 256 / 128 / 64
   const int* order = DP.aca_order.as<int>();
   const int o1 = DP.aca_split[0], o2 = o1 + DP.aca_split[1], o3 = o2 + DP.aca_split[2];
@@ -548,6 +552,37 @@ void launch_aca_df(const DevGeometry& G, const DevPartition& DP, DevHMat& H, dou
   aca_df_launch_warp<4>(a, DP.aca_split[2], s);
   a.order = order + o3;
   aca_df_launch_warp<2>(a, DP.aca_split[3], s_small);
+}
+
+// Receiver ACA (compute_ACA_listener, aca.cpp:84-134: one block of L receivers x Ne elements, no
+// zero guard) in double-float, then the terms converted in place to complex FP64 (same size).
+__global__ void cdf_to_cd_kernel(cdf* pool, const unsigned long long* used) {
+  const unsigned long long n = *used;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const cdf v = pool[i];
+    reinterpret_cast<cd*>(pool)[i] = cd(df_to_double(v.re), df_to_double(v.im));
+  }
+}
+
+void launch_listener_aca_df(const DevGeometry& G, const void* pts_df, int L, double k, double eps, int maxk,
+                            void* pool, long long pool_cap, unsigned long long* used, long long* term_off, int* rank,
+                            int* status, const int4* block, const int* order, cudaStream_t s) {
+  int iter_lim = std::min(maxk, std::min(L - 1, G.ne - 1));
+  if (iter_lim < 1) iter_lim = 1;
+  AcaDfArgs a{G.cen.as<double4>(), G.va.as<double4>(), G.eg64.as<ElemGeo<double>>(), (const DfPt*)pts_df,
+              G.el_df.as<DfElem>(), G.df_tab.as<float4>(), block, order, df_from_double(k), eps, maxk, iter_lim,
+              (cdf*)pool, pool_cap, used, term_off, rank, status, nullptr, 0};
+  const size_t smem = (size_t)iter_lim * (2 * sizeof(cdf) + sizeof(long long)) + (size_t)((L + 31) / 32) * 4;
+  if (smem > 200 * 1024) throw Error(4, "receiver ACA too large for shared memory (at most about 5000 receivers)");
+  if (smem > 48 * 1024)
+    AC3D_CUDA(cudaFuncSetAttribute(aca_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  note_launch();
+  aca_df_kernel<<<1, kDfThreads, smem, s>>>(a);
+  AC3D_CUDA(cudaGetLastError());
+  note_launch();
+  cdf_to_cd_kernel<<<4 * device_sm_count(), 256, 0, s>>>((cdf*)pool, used);
+  AC3D_CUDA(cudaGetLastError());
 }
 
 }  // namespace ac3d

@@ -220,6 +220,249 @@ static void adjoint_t(const DevGeometry& G, const AdjointArgs& a, DevBuf& scratc
   AC3D_CUDA(cudaGetLastError());
 }
 
+// ------------------------------------------------------------------------------------------
+// Several plane-wave directions of one frequency at once (up to NR per launch). The shape
+// derivatives of M and of the receiver matrix depend only on the geometry and k, so each
+// derivative entry is evaluated once and multiplied into every direction's vectors; per
+// (target, direction) the sums are reduced in the same fixed order as the single-direction path.
+// ------------------------------------------------------------------------------------------
+namespace {
+constexpr int kMTile = 2;  // targets per CTA of the multi-direction sweeps
+}  // namespace
+
+template <typename R>
+__device__ __forceinline__ cplx<R> ld_c(const cd* p) {
+  const cd v = *p;
+  return {(R)v.re, (R)v.im};
+}
+
+template <typename R, int NR>
+__global__ void __launch_bounds__(kAdjThreads) derA_multi_kernel(GeoView<R> G, AdjointMultiArgs a, double* outA) {
+  const int lane = threadIdx.x & 31;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (t >= a.npairs) return;
+  const int j = a.pair_elem[t], o = a.pair_corner[t];
+  const double4 va = G.va[j];
+  const ElemGeo<R> g = G.eg[j];
+  R sr[NR], si[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) sr[r] = si[r] = 0;
+  for (int l = lane; l < a.L; l += 32) {
+    const double4 P = a.recv[l];
+    const cplx<R> d = dM_source<R>((R)a.k, (R)(P.x - va.x), (R)(P.y - va.y), (R)(P.z - va.z), g, o);
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+      if (r < a.nr) {
+        const cplx<R> v = ld_c<R>(a.vf + (size_t)r * a.L + l);
+        sr[r] += d.re * v.re - d.im * v.im;
+        si[r] += d.re * v.im + d.im * v.re;
+      }
+  }
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    const double vr = warp_sum((double)sr[r]), vi = warp_sum((double)si[r]);
+    if (lane == 0 && r < a.nr) {
+      const cd xj = a.x[(size_t)r * G.ne + j];
+      outA[(size_t)t * NR + r] = vr * xj.re - vi * xj.im;
+    }
+  }
+}
+
+// Per-CTA reduction of acc[KT][NR] (complex) into part[((t0 + p) NR + r) S + split].
+template <int NR>
+__device__ __forceinline__ void multi_store(const double* accd, int t0, int ntarget, int split, int S, cd* part,
+                                            double (*sd)[2 * kMTile * NR]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int v = 0; v < 2 * kMTile * NR; v++) {
+    const double x = warp_sum(accd[v]);
+    if (lane == 0) sd[w][v] = x;
+  }
+  __syncthreads();
+  for (int v = threadIdx.x; v < 2 * kMTile * NR; v += blockDim.x) {
+    const int p = v / (2 * NR), r = (v / 2) % NR;
+    if (t0 + p < ntarget) {
+      double sum = 0;
+      for (int ww = 0; ww < kAdjWarps; ww++) sum += sd[ww][v];
+      double* dst = (double*)&part[((size_t)(t0 + p) * NR + r) * S + split];
+      dst[v & 1] = sum;
+    }
+  }
+}
+
+// s1 for every direction: sum_j x_r[j] dM(c_i, tri_j)/dp_y over the touched elements i
+template <typename R, int NR>
+__global__ void __launch_bounds__(kAdjThreads) derB_s1_multi_kernel(GeoView<R> G, AdjointMultiArgs a, cd* part,
+                                                                    int S) {
+  __shared__ double sd[kAdjWarps][2 * kMTile * NR];
+  const int t0 = blockIdx.x * kMTile, split = blockIdx.y;
+  const int per = (G.ne + S - 1) / S;
+  const int j0 = split * per, j1 = min(G.ne, j0 + per);
+  double4 C[kMTile];
+  for (int p = 0; p < kMTile; p++) C[p] = G.cen[a.touch_elem[min(t0 + p, a.ntouch - 1)]];
+  R ar[kMTile][NR], ai[kMTile][NR];
+#pragma unroll
+  for (int p = 0; p < kMTile; p++)
+#pragma unroll
+    for (int r = 0; r < NR; r++) ar[p][r] = ai[p][r] = 0;
+  const R k = (R)a.k;
+  for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    const double4 va = G.va[j];
+    const ElemGeo<R> g = G.eg[j];
+    cplx<R> xv[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) xv[r] = r < a.nr ? ld_c<R>(a.x + (size_t)r * G.ne + j) : cplx<R>();
+#pragma unroll
+    for (int p = 0; p < kMTile; p++) {
+      const cplx<R> d = dM_target<R>(k, (R)(C[p].x - va.x), (R)(C[p].y - va.y), (R)(C[p].z - va.z), g);
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        ar[p][r] += d.re * xv[r].re - d.im * xv[r].im;
+        ai[p][r] += d.re * xv[r].im + d.im * xv[r].re;
+      }
+    }
+  }
+  double accd[2 * kMTile * NR];
+#pragma unroll
+  for (int p = 0; p < kMTile; p++)
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      accd[2 * (p * NR + r)] = (double)ar[p][r];
+      accd[2 * (p * NR + r) + 1] = (double)ai[p][r];
+    }
+  multi_store<NR>(accd, t0, a.ntouch, split, S, part, sd);
+}
+
+// s2 for every direction: sum_j lmb_r[j] dM(c_j, tri_i)/dq_{o,y} over the incidences (i, o)
+template <typename R, int NR>
+__global__ void __launch_bounds__(kAdjThreads) derB_s2_multi_kernel(GeoView<R> G, AdjointMultiArgs a, cd* part,
+                                                                    int S) {
+  __shared__ double sd[kAdjWarps][2 * kMTile * NR];
+  const int t0 = blockIdx.x * kMTile, split = blockIdx.y;
+  const int per = (G.ne + S - 1) / S;
+  const int j0 = split * per, j1 = min(G.ne, j0 + per);
+  double4 A[kMTile];
+  ElemGeo<R> Eg[kMTile];
+  int O[kMTile];
+  for (int p = 0; p < kMTile; p++) {
+    const int t = min(t0 + p, a.npairs - 1);
+    const int i = a.pair_elem[t];
+    A[p] = G.va[i];
+    Eg[p] = G.eg[i];
+    O[p] = a.pair_corner[t];
+  }
+  R ar[kMTile][NR], ai[kMTile][NR];
+#pragma unroll
+  for (int p = 0; p < kMTile; p++)
+#pragma unroll
+    for (int r = 0; r < NR; r++) ar[p][r] = ai[p][r] = 0;
+  const R k = (R)a.k;
+  for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    const double4 c = G.cen[j];
+    cplx<R> lv[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) lv[r] = r < a.nr ? ld_c<R>(a.lmb + (size_t)r * G.ne + j) : cplx<R>();
+#pragma unroll
+    for (int p = 0; p < kMTile; p++) {
+      const cplx<R> d = dM_source<R>(k, (R)(c.x - A[p].x), (R)(c.y - A[p].y), (R)(c.z - A[p].z), Eg[p], O[p]);
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        ar[p][r] += d.re * lv[r].re - d.im * lv[r].im;
+        ai[p][r] += d.re * lv[r].im + d.im * lv[r].re;
+      }
+    }
+  }
+  double accd[2 * kMTile * NR];
+#pragma unroll
+  for (int p = 0; p < kMTile; p++)
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      accd[2 * (p * NR + r)] = (double)ar[p][r];
+      accd[2 * (p * NR + r) + 1] = (double)ai[p][r];
+    }
+  multi_store<NR>(accd, t0, a.npairs, split, S, part, sd);
+}
+
+// Per vertex h: sum over its incidences (CSR order), then over the directions, of
+// w_r (A_r - B_r + C_r), with C_r of the plane wave e^{-ik d_r.x} (sphere.h:22-26 along d_r).
+template <int NR>
+__global__ void adj_combine_multi_kernel(AdjointMultiArgs a, const double4* __restrict__ cen,
+                                         const double* __restrict__ outA, const cd* __restrict__ s1,
+                                         const cd* __restrict__ s2, int S1, int S2, int ne) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= a.HH) return;
+  double acc = 0;
+  for (int t = a.h_off[h]; t < a.h_off[h + 1]; t++) {
+    const int i = a.pair_elem[t];
+    const int ti = a.pair_touch[t];
+    const double4 c = cen[i];
+    for (int r = 0; r < a.nr; r++) {
+      double s1r = 0, s1i = 0, s2r = 0, s2i = 0;
+      for (int s = 0; s < S1; s++) {
+        const cd v = s1[((size_t)ti * NR + r) * S1 + s];
+        s1r += v.re;
+        s1i += v.im;
+      }
+      for (int s = 0; s < S2; s++) {
+        const cd v = s2[((size_t)t * NR + r) * S2 + s];
+        s2r += v.re;
+        s2i += v.im;
+      }
+      const cd li = a.lmb[(size_t)r * ne + i], xi = a.x[(size_t)r * ne + i];
+      const double B = (s1r * li.re - s1i * li.im) + (s2r * xi.re - s2i * xi.im);
+      const double ph = a.k * (a.dir[r][0] * c.x + a.dir[r][1] * c.y + a.dir[r][2] * c.z);
+      double sn, cs;
+      sincos(ph, &sn, &cs);
+      const double f = -a.k * a.dir[r][1] / 3.0;
+      const double C = -(f * sn * li.re - f * cs * li.im);
+      acc += a.w[r] * (outA[(size_t)t * NR + r] - B + C);
+    }
+  }
+  a.grad[h] += acc;
+}
+
+template <typename R, int NR>
+static void adjoint_multi_t(const DevGeometry& G, const AdjointMultiArgs& a, DevBuf& scratch, cudaStream_t s) {
+  const int sms = device_sm_count();
+  const int tiles1 = (a.ntouch + kMTile - 1) / kMTile, tiles2 = (a.npairs + kMTile - 1) / kMTile;
+  auto pick = [&](int tiles) { return std::max(1, std::min(256, (sms * 8 + tiles - 1) / std::max(1, tiles))); };
+  const int S1 = pick(tiles1), S2 = pick(tiles2);
+  const size_t bytesA = ((size_t)a.npairs * NR * sizeof(double) + 15) / 16 * 16;
+  const size_t bytes1 = (size_t)a.ntouch * NR * S1 * sizeof(cd);
+  const size_t bytes2 = (size_t)a.npairs * NR * S2 * sizeof(cd);
+  scratch.ensure(bytesA + bytes1 + bytes2 + 64, s);
+  double* outA = scratch.as<double>();
+  cd* s1 = (cd*)((char*)scratch.p + bytesA);
+  cd* s2 = s1 + (size_t)a.ntouch * NR * S1;
+  GeoView<R> gv = geo_view<R>(G);
+  note_launch();
+  derA_multi_kernel<R, NR><<<(a.npairs * 32 + kAdjThreads - 1) / kAdjThreads, kAdjThreads, 0, s>>>(gv, a, outA);
+  AC3D_CUDA(cudaGetLastError());
+  note_launch();
+  derB_s1_multi_kernel<R, NR><<<dim3(tiles1, S1), kAdjThreads, 0, s>>>(gv, a, s1, S1);
+  AC3D_CUDA(cudaGetLastError());
+  note_launch();
+  derB_s2_multi_kernel<R, NR><<<dim3(tiles2, S2), kAdjThreads, 0, s>>>(gv, a, s2, S2);
+  AC3D_CUDA(cudaGetLastError());
+  note_launch();
+  adj_combine_multi_kernel<NR><<<(a.HH + 127) / 128, 128, 0, s>>>(a, G.cen.as<double4>(), outA, s1, s2, S1, S2, G.ne);
+  AC3D_CUDA(cudaGetLastError());
+}
+
+void launch_adjoint_terms_multi(const DevGeometry& G, const AdjointMultiArgs& a, DevBuf& scratch, cudaStream_t s) {
+  if (a.npairs == 0 || a.HH == 0 || a.nr <= 0) return;
+  if (a.nr > kAdjMaxRhs) throw Error(3, "internal: too many directions in one adjoint batch");
+  if (a.prec == PREC_FP64) {
+    if (a.nr > 8) throw Error(3, "internal: FP64 adjoint batches hold at most 8 directions");
+    adjoint_multi_t<double, 8>(G, a, scratch, s);
+  } else if (a.nr <= 4) {
+    adjoint_multi_t<float, 4>(G, a, scratch, s);
+  } else if (a.nr <= 8) {
+    adjoint_multi_t<float, 8>(G, a, scratch, s);
+  } else {
+    adjoint_multi_t<float, 16>(G, a, scratch, s);
+  }
+}
+
 void launch_adjoint_terms(const DevGeometry& G, const AdjointArgs& a, DevBuf& scratch, cudaStream_t s) {
   if (a.npairs == 0 || a.HH == 0) return;
   if (a.prec == PREC_FP64)

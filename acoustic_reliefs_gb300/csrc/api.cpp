@@ -737,8 +737,8 @@ int run_block_gmres(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vect
 }
 
 // |b - A x|^2 of one column (contiguous FP64 vectors) with the double-float residual matvec
-double column_residual2(ac3d_ctx* c, const DevHMat& H, const cd* b, const cd* x, cd* r) {
-  return reduce_norm2_residual(c, H, false, b, x, r);
+double column_residual2(ac3d_ctx* c, const DevHMat& H, bool tr, const cd* b, const cd* x, cd* r) {
+  return reduce_norm2_residual(c, H, tr, b, x, r);
 }
 
 double column_norm2(ac3d_ctx* c, const cd* v) {
@@ -750,16 +750,20 @@ double column_norm2(ac3d_ctx* c, const cd* v) {
   return c->h_red[4];
 }
 
-void solve_block(ac3d_ctx* c, DevHMat& H, int nrb, int nr, const cd* b64, cd* x64, BlockWork& W) {
+// Block vectors and reduction buffers of one block solve (or block matvec timing) in W.
+MultiBufs block_bufs(ac3d_ctx* c, DevHMat& H, int nrb, BlockWork& W, bool tr) {
   cudaStream_t s = c->stream;
   ensure_work(c);
   prepare_multi_kernels();
+  if (tr) ensure_near_transposed(c->m->DP, H, s);
   const int n = c->m->Ne, nleaf = c->m->DP.nleaf;
   const size_t blk32 = (size_t)n * nrb * sizeof(cf);
   W.kv.ensure(8 * blk32, s);
   MultiBufs B;
   B.n = n;
   B.nrb = nrb;
+  B.tr = tr;
+  B.tc = c->block_tc;
   void** slots[8] = {&B.b, &B.x, &B.r, &B.rhat, &B.p, &B.v, &B.s, &B.t};
   for (int i = 0; i < 8; i++) *slots[i] = (char*)W.kv.p + (size_t)i * blk32;
   W.parts.ensure((size_t)(std::max(nleaf, 1184) + 1024) * 5 * nrb * sizeof(double), s);
@@ -773,9 +777,6 @@ void solve_block(ac3d_ctx* c, DevHMat& H, int nrb, int nr, const cd* b64, cd* x6
   W.tbuf.ensure((size_t)std::max<int64_t>(H.task_cap, 1) * nrb * sizeof(cf), s);
   W.tolb.ensure((size_t)nrb * sizeof(double), s);
   W.state.ensure(sizeof(KStateM), s);
-  W.r64.ensure((size_t)n * nrb * sizeof(cd), s);
-  for (DevBuf* b : {&W.xcol, &W.bcol, &W.rcol, &W.zcol}) b->ensure((size_t)n * sizeof(cd), s);
-  AC3D_CUDA(cudaMemsetAsync(W.zcol.p, 0, (size_t)n * sizeof(cd), s));
   B.partials = W.parts.as<double>();
   B.vpartials = W.vparts.as<double>();
   B.red = W.red.as<double>();
@@ -784,6 +785,16 @@ void solve_block(ac3d_ctx* c, DevHMat& H, int nrb, int nr, const cd* b64, cd* x6
   B.tbuf = W.tbuf.p;
   B.tol = W.tolb.as<double>();
   B.state = W.state.as<KStateM>();
+  return B;
+}
+
+void solve_block(ac3d_ctx* c, DevHMat& H, int nrb, int nr, const cd* b64, cd* x64, BlockWork& W, bool tr = false) {
+  cudaStream_t s = c->stream;
+  MultiBufs B = block_bufs(c, H, nrb, W, tr);
+  const int n = c->m->Ne;
+  W.r64.ensure((size_t)n * nrb * sizeof(cd), s);
+  for (DevBuf* b : {&W.xcol, &W.bcol, &W.rcol, &W.zcol}) b->ensure((size_t)n * sizeof(cd), s);
+  AC3D_CUDA(cudaMemsetAsync(W.zcol.p, 0, (size_t)n * sizeof(cd), s));
 
   const double tol = c->solver_tol;
   AC3D_CUDA(cudaMemsetAsync(x64, 0, (size_t)n * nrb * sizeof(cd), s));
@@ -817,7 +828,7 @@ void solve_block(ac3d_ctx* c, DevHMat& H, int nrb, int nr, const cd* b64, cd* x6
       if (!(rn2[j] > tol * tol * bn2[j])) continue;
       launch_block_get(n, nrb, j, x64, W.xcol.p, s);
       launch_block_get(n, nrb, j, b64, W.bcol.p, s);
-      rn2[j] = column_residual2(c, H, W.bcol.as<cd>(), W.xcol.as<cd>(), W.rcol.as<cd>());
+      rn2[j] = column_residual2(c, H, tr, W.bcol.as<cd>(), W.xcol.as<cd>(), W.rcol.as<cd>());
       launch_block_set(n, nrb, j, W.rcol.p, W.r64.p, s);
     }
     outer++;
@@ -873,6 +884,7 @@ void upload_receivers(ac3d_ctx* c, const double* L, int n, DevBuf& dst) {
 struct ListenerLR {
   DevBuf pool, toff, rank, used, blk, ord, pts, t;
   int L = 0, iter_lim = 0;
+  int prec = PREC_MIXED;  // precision of the stored terms (the apply's arithmetic)
 };
 
 std::unique_ptr<ListenerLR> listener_lr(ac3d_ctx* c, double k, const double* Lh, int L) {
@@ -881,7 +893,10 @@ std::unique_ptr<ListenerLR> listener_lr(ac3d_ctx* c, double k, const double* Lh,
   Q->L = L;
   const int maxk = 5000;  // Q_ACA_MAX_K (constants.h:17)
   Q->iter_lim = std::max(1, std::min(maxk, std::min(L - 1, c->m->Ne - 1)));
-  const size_t cs = c->prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
+  // mixed precision with the double-float assembly: receiver ACA in double-float, terms in FP64
+  const bool df = c->prec != PREC_FP64 && c->assembly == AC3D_ASSEMBLY_DF;
+  Q->prec = df ? PREC_FP64 : c->prec;
+  const size_t cs = Q->prec == PREC_FP64 ? sizeof(cd) : sizeof(cf);
   const long long cap = (long long)Q->iter_lim * (L + c->m->Ne);
   Q->pool.alloc((size_t)cap * cs, s);
   Q->toff.alloc((size_t)Q->iter_lim * sizeof(long long), s);
@@ -891,6 +906,20 @@ std::unique_ptr<ListenerLR> listener_lr(ac3d_ctx* c, double k, const double* Lh,
   AC3D_CUDA(cudaMemsetAsync(Q->used.p, 0, 16, s));
   upload(Q->blk, std::vector<int>{0, L, 0, c->m->Ne}, s);
   upload(Q->ord, std::vector<int>{0}, s);
+  if (df) {
+    std::vector<float> v(8 * (size_t)L, 0.f);
+    for (int i = 0; i < L; i++)
+      for (int d = 0; d < 3; d++) {
+        const float hi = (float)Lh[3 * i + d];
+        v[8 * i + 2 * d] = hi;
+        v[8 * i + 2 * d + 1] = (float)(Lh[3 * i + d] - (double)hi);
+      }
+    upload(Q->pts, v, s);
+    launch_listener_aca_df(c->m->G, Q->pts.p, L, k, c->q_tol, maxk, Q->pool.p, cap, Q->used.as<unsigned long long>(),
+                           Q->toff.as<long long>(), Q->rank.as<int>(), (int*)(Q->used.as<unsigned long long>() + 1),
+                           Q->blk.as<int4>(), Q->ord.as<int>(), s);
+    return Q;
+  }
   if (c->prec == PREC_FP64) {
     std::vector<double> v(4 * (size_t)L);
     for (int i = 0; i < L; i++)
@@ -909,7 +938,7 @@ std::unique_ptr<ListenerLR> listener_lr(ac3d_ctx* c, double k, const double* Lh,
 }
 
 void listener_apply(ac3d_ctx* c, const ListenerLR& Q, const cd* in, cd* out, bool trans) {
-  launch_lr_apply(c->prec, Q.pool.p, Q.toff.as<long long>(), Q.rank.as<int>(), Q.iter_lim, Q.L, c->m->Ne, in,
+  launch_lr_apply(Q.prec, Q.pool.p, Q.toff.as<long long>(), Q.rank.as<int>(), Q.iter_lim, Q.L, c->m->Ne, in,
                   trans ? 1 : 0, Q.t.as<cd>(), out, c->stream);
 }
 
@@ -1019,6 +1048,126 @@ double band_eval(ac3d_ctx* c, double band, bool forward_only, double* grad_dev) 
   AC3D_CUDA(cudaStreamSynchronize(s));
   c->stats.ms_adjoint += tadj.stop();
   return cval;
+}
+
+// Loss 1 - mean_{f, d} c(f, d) over the frequencies and plane-wave directions d, c(f, d) the
+// diffusion coefficient of the context's receivers for the one frequency f (compute_u,
+// adjoint.cpp:388-397, of |y|); grad_dev (HH) += d loss / d heights. Per frequency one H-matrix
+// serves every direction: forward block solves, per-direction receivers and adjoint right-hand
+// sides, transposed block solves, then the shape-derivative terms of all directions in batches
+// that share each derivative evaluation (adjoint.cpp:24-242 per direction, with the sign and
+// weight of the mean). coefs receives c(f, d), frequency-major.
+double multi_eval(ac3d_ctx* c, const std::vector<double>& freqs, const std::vector<double>& dirs, double* grad_dev,
+                  std::vector<double>& coefs) {
+  cudaStream_t s = c->stream;
+  const int L = (int)c->Ls.size() / 3;
+  const int n = c->m->Ne;
+  const int F = (int)freqs.size(), D = (int)dirs.size() / 3;
+  const bool fp64 = c->prec == AC3D_PREC_FP64;
+  const double wgt = -1.0 / ((double)F * D);
+  DevBuf X, LMB, Y, VF, ADJ, yt, u, coef, b64, x64;
+  X.alloc((size_t)D * n * sizeof(cd), s);
+  LMB.alloc((size_t)D * n * sizeof(cd), s);
+  ADJ.alloc((size_t)D * n * sizeof(cd), s);
+  Y.alloc((size_t)D * L * sizeof(cd), s);
+  VF.alloc((size_t)D * L * sizeof(cd), s);
+  yt.alloc((size_t)L * sizeof(double), s);
+  u.alloc((size_t)L * sizeof(double), s);
+  coef.alloc((size_t)F * D * sizeof(double), s);
+  ensure_work(c);
+  BlockWork W;
+  // op(A) Z = B for the D columns of B (direction-major, n each), in batches of kMaxRhs
+  auto solve_all = [&](const cd* Bm, cd* Z, DevHMat& H, bool tr) {
+    for (int start = 0; start < D; start += kMaxRhs) {
+      const int nr = std::min(kMaxRhs, D - start);
+      if (fp64) {  // FP64 storage: one right-hand side at a time through the FP64 solver
+        for (int j = 0; j < nr; j++) {
+          solve(c, H, Bm + (size_t)(start + j) * n, Z + (size_t)(start + j) * n, tr);
+          c->stats.solves++;
+        }
+        continue;
+      }
+      const int nrb = nr <= 4 ? 4 : nr <= 8 ? 8 : 16;
+      b64.ensure((size_t)n * nrb * sizeof(cd), s);
+      x64.ensure((size_t)n * nrb * sizeof(cd), s);
+      AC3D_CUDA(cudaMemsetAsync(b64.p, 0, (size_t)n * nrb * sizeof(cd), s));
+      for (int j = 0; j < nr; j++) launch_block_set(n, nrb, j, Bm + (size_t)(start + j) * n, b64.p, s);
+      solve_block(c, H, nrb, nr, b64.as<cd>(), x64.as<cd>(), W, tr);
+      for (int j = 0; j < nr; j++) launch_block_get(n, nrb, j, x64.p, Z + (size_t)(start + j) * n, s);
+    }
+  };
+  for (int fi = 0; fi < F; fi++) {
+    const double k = wavenumber(freqs[fi]);
+    GpuTimer ta(s);
+    auto H = assemble(c, k, c->prec);
+    c->stats.ms_assemble += ta.stop();
+    // forward: b = -incident field (adjoint.cpp:95), one column per direction
+    GpuTimer ts(s);
+    for (int d = 0; d < D; d++) {
+      launch_rhs(c->m->G, 1, k, AC3D_INCIDENT_PLANE, &dirs[3 * d], ADJ.as<cd>() + (size_t)d * n, s);
+      launch_negate64(n, ADJ.as<cd>() + (size_t)d * n, s);
+    }
+    solve_all(ADJ.as<cd>(), X.as<cd>(), *H, false);
+    c->stats.ms_solve += ts.stop();
+    // receivers, coefficient and adjoint right-hand side of each direction (adjoint.cpp:101-178)
+    GpuTimer tadj(s);
+    std::unique_ptr<ListenerLR> Q;
+    if (c->listener_mode == AC3D_LISTENER_ACA) Q = listener_lr(c, k, c->Ls.data(), L);
+    for (int d = 0; d < D; d++) {
+      cd* xd = X.as<cd>() + (size_t)d * n;
+      cd* yd = Y.as<cd>() + (size_t)d * L;
+      cd* vfd = VF.as<cd>() + (size_t)d * L;
+      if (Q)
+        listener_apply(c, *Q, xd, yd, false);
+      else
+        launch_far_field(c->m->G, c->prec, c->Ls_dev.as<double4>(), L, k, xd, yd, c->ff_scratch, s);
+      AC3D_CUDA(cudaMemsetAsync(yt.p, 0, (size_t)L * sizeof(double), s));
+      launch_accum_abs(yd, L, yt.as<double>(), s);
+      launch_compute_u(yt.as<double>(), L, u.as<double>(), coef.as<double>() + (size_t)fi * D + d, s);
+      launch_vf(u.as<double>(), yd, L, vfd, s);
+      if (Q)
+        listener_apply(c, *Q, vfd, ADJ.as<cd>() + (size_t)d * n, true);
+      else
+        launch_far_field_t(c->m->G, c->prec, c->Ls_dev.as<double4>(), L, k, vfd, ADJ.as<cd>() + (size_t)d * n, s);
+    }
+    solve_all(ADJ.as<cd>(), LMB.as<cd>(), *H, true);
+    H.reset();
+    // shape-derivative terms, all directions of a batch per derivative evaluation
+    const int batch = fp64 ? 8 : kAdjMaxRhs;
+    for (int start = 0; start < D; start += batch) {
+      AdjointMultiArgs a{};
+      a.prec = c->prec;
+      a.k = k;
+      a.npairs = (int)c->pair_elem.size();
+      a.pair_elem = c->d_pair_elem.as<int>();
+      a.pair_corner = c->d_pair_corner.as<int>();
+      a.ntouch = (int)c->touch.size();
+      a.touch_elem = c->d_touch.as<int>();
+      a.pair_touch = c->d_pair_touch.as<int>();
+      a.recv = c->Ls_dev.as<double4>();
+      a.L = L;
+      a.nr = std::min(batch, D - start);
+      a.vf = VF.as<cd>() + (size_t)start * L;
+      a.x = X.as<cd>() + (size_t)start * n;
+      a.lmb = LMB.as<cd>() + (size_t)start * n;
+      for (int r = 0; r < a.nr; r++) {
+        for (int q = 0; q < 3; q++) a.dir[r][q] = dirs[3 * (start + r) + q];
+        a.w[r] = wgt;
+      }
+      a.h_off = c->d_h_off.as<int>();
+      a.HH = (int)c->h_off.size() - 1;
+      a.grad = grad_dev;
+      launch_adjoint_terms_multi(c->m->G, a, c->adj_scratch, s);
+    }
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    c->stats.ms_adjoint += tadj.stop();
+  }
+  coefs.assign((size_t)F * D, 0.0);
+  AC3D_CUDA(cudaMemcpyAsync(coefs.data(), coef.p, (size_t)F * D * sizeof(double), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaStreamSynchronize(s));
+  double mean = 0;
+  for (double v : coefs) mean += v;
+  return 1.0 - mean / ((double)F * D);
 }
 
 void reset_stats(ac3d_ctx* c) {
@@ -1131,6 +1280,11 @@ std::shared_ptr<MeshState> build_mesh_state(const double* Ps, int V, const int32
       upload(DP.aca_order, all, s);
     }
     upload(DP.near_seg, std::vector<long long>(mp->P.near_seg.begin(), mp->P.near_seg.end()), s);
+    upload(DP.near_off_t, std::vector<long long>(mp->P.near_off_t.begin(), mp->P.near_off_t.end()), s);
+    upload(DP.near_seg_t, std::vector<long long>(mp->P.near_seg_t.begin(), mp->P.near_seg_t.end()), s);
+    upload(DP.didx_t_ptr, mp->P.didx_t_ptr, s);
+    upload(DP.didx_t, mp->P.didx_t, s);
+    DP.near_total_t = mp->P.near_total_t;
     upload(DP.didx_ptr, mp->P.didx_ptr, s);
     upload(DP.didx, mp->P.didx, s);
     upload(DP.blk_fw_ptr, mp->P.blk_fw_ptr, s);
@@ -1281,6 +1435,12 @@ int ac3d_set_solver(ac3d_ctx* c, int max_iterations, double inner_tol, int max_o
 int ac3d_set_assembly(ac3d_ctx* c, int mode) {
   if (!c || (mode != AC3D_ASSEMBLY_DF && mode != AC3D_ASSEMBLY_FP32)) return AC3D_ERR_ARG;
   c->assembly = mode;
+  return AC3D_OK;
+}
+
+int ac3d_set_tensor_cores(ac3d_ctx* c, int on) {
+  if (!c) return AC3D_ERR_ARG;
+  c->block_tc = on != 0;
   return AC3D_OK;
 }
 
@@ -1662,6 +1822,40 @@ int ac3d_gradient(ac3d_ctx* c, const double* x, double* cv, double* grad) {
   });
 }
 
+int ac3d_gradient_multi(ac3d_ctx* c, const double* x, const double* freqs, int nf, const double* dirs, int nd,
+                        double* loss, double* grad, double* coefs) {
+  if (!c || !freqs || nf < 1 || !dirs || nd < 1 || !loss || !grad) return AC3D_ERR_ARG;
+  for (int i = 0; i < nf; i++)
+    if (!(freqs[i] > 0)) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    require_mesh(c);
+    if (!c->diff_set)
+      throw Error(AC3D_ERR_STATE, "No differentiable points set. Set them using set_diff_pts or precompute.");
+    if (c->actual) throw Error(AC3D_ERR_ARG, "multi-direction gradients run on the H-matrix (use_actual off)");
+    std::vector<double> dv(3 * (size_t)nd);
+    for (int d = 0; d < nd; d++) {
+      const double* w = dirs + 3 * (size_t)d;
+      const double nrm = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+      if (!(nrm > 0)) throw Error(AC3D_ERR_ARG, "zero plane-wave direction");
+      for (int q = 0; q < 3; q++) dv[3 * (size_t)d + q] = w[q] / nrm;
+    }
+    reset_stats(c);
+    cudaStream_t s = c->stream;
+    upload_points(*c->m, heights_to_points(c, x), s);
+    c->m->geom_base = false;
+    const int HH = (int)c->h_off.size() - 1;
+    DevBuf g;
+    g.alloc((size_t)std::max(HH, 1) * sizeof(double), s);
+    AC3D_CUDA(cudaMemsetAsync(g.p, 0, (size_t)std::max(HH, 1) * sizeof(double), s));
+    std::vector<double> cf;
+    *loss = multi_eval(c, std::vector<double>(freqs, freqs + nf), dv, g.as<double>(), cf);
+    AC3D_CUDA(cudaMemcpyAsync(grad, g.p, (size_t)HH * sizeof(double), cudaMemcpyDeviceToHost, s));
+    AC3D_CUDA(cudaStreamSynchronize(s));
+    if (coefs) std::copy(cf.begin(), cf.end(), coefs);
+    if (!c->stats.converged) throw Error(AC3D_ERR_NOT_CONVERGED, not_converged_message(c));
+  });
+}
+
 int ac3d_value_dev(ac3d_ctx* c, const double* x_dev, double* c_dev, void* stream) {
   if (!c || !c_dev) return AC3D_ERR_ARG;
   return guard(c, [&] {
@@ -1842,6 +2036,36 @@ int ac3d_matvec_timing(ac3d_ctx* c, int iters, int transposed, double* ms, long 
     // stored entries once; x read and y written once (FP32 or FP64); the FP32 shadow read once
     const long long es = H.prec == PREC_FP64 ? 16 : 8;
     *bytes = (c->m->P.near_total + H.lr_entries) * es + c->m->Ne * (vec64 == 0 ? 16LL : 32LL + (vec64 == 2 ? 8 : 0));
+  });
+}
+
+int ac3d_block_matvec_timing(ac3d_ctx* c, int nrb, int iters, int transposed, double* ms, long long* bytes) {
+  if (!c || !ms || !bytes || iters < 1 || (nrb != 4 && nrb != 8 && nrb != 16)) return AC3D_ERR_ARG;
+  return guard(c, [&] {
+    if (!c->last_H) throw Error(AC3D_ERR_STATE, "no H-matrix: call ac3d_pressures or ac3d_solve_multi first");
+    DevHMat& H = *c->last_H;
+    if (H.prec == PREC_FP64) throw Error(AC3D_ERR_ARG, "block matvecs need the mixed-precision (FP32) H-matrix");
+    cudaStream_t s = c->stream;
+    BlockWork W;
+    MultiBufs B = block_bufs(c, H, nrb, W, transposed != 0);
+    const size_t blk32 = (size_t)c->m->Ne * nrb * sizeof(cf);
+    AC3D_CUDA(cudaMemsetAsync(B.x, 0x3c, blk32, s));  // FP32 values near 0.01
+    for (int i = 0; i < 3; i++) launch_mmatvec(c->m->DP, H, B, B.x, B.v, nullptr, nullptr, nullptr, s);
+    cudaEvent_t e0, e1;
+    AC3D_CUDA(cudaEventCreate(&e0));
+    AC3D_CUDA(cudaEventCreate(&e1));
+    AC3D_CUDA(cudaEventRecord(e0, s));
+    for (int i = 0; i < iters; i++) launch_mmatvec(c->m->DP, H, B, B.x, B.v, nullptr, nullptr, nullptr, s);
+    AC3D_CUDA(cudaEventRecord(e1, s));
+    AC3D_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    AC3D_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_pipeline(c, H);
+    *ms = t / iters;
+    // every stored matrix entry once (complex FP32), the block input read and the output written
+    *bytes = 8 * (long long)(c->m->P.near_total + H.lr_entries) + 2 * (long long)blk32;
   });
 }
 

@@ -29,6 +29,7 @@ struct ac3d_ctx {
   // extensions
   int prec = AC3D_PREC_MIXED;
   int assembly = AC3D_ASSEMBLY_DF;  // arithmetic of the mixed-precision assembly
+  bool block_tc = true;             // block matvec dot pass on the tensor cores
   int listener_mode = AC3D_LISTENER_DENSE;
   int maxit = 0;           // 0: twice the number of unknowns
   double inner_tol = 1e-6; // floor of the relative tolerance of each FP32 inner solve

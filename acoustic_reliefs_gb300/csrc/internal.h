@@ -101,6 +101,10 @@ struct Partition {
   int64_t near_total = 0;
   std::vector<int64_t> near_seg;       // per leaf: element offset of its near segment
   std::vector<int> didx_ptr, didx;     // per leaf: global column index of every near-segment column
+  // the same for the transposed near field (segments of A^T by leaf; columns = global rows)
+  std::vector<int64_t> near_off_t, near_seg_t;
+  std::vector<int> didx_t_ptr, didx_t;
+  int64_t near_total_t = 0;
   // per admissible block: its entries in the fw_lr / tr_lr lists (one per row / column leaf),
   // in leaf order; the matvec sums a term's per-leaf partial dots over these
   std::vector<int> blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
@@ -127,6 +131,8 @@ struct DevPartition {
   int aca_split[4] = {0, 0, 0, 0};
   int max_leaf = 0;
   DevBuf near_seg, didx_ptr, didx;
+  DevBuf near_off_t, near_seg_t, didx_t_ptr, didx_t;  // transposed near layout (block adjoint)
+  int64_t near_total_t = 0;
   DevBuf blk_fw_ptr, blk_fw, blk_tr_ptr, blk_tr;
   DevBuf fw_pos, tr_pos;
   DevBuf blocks_d, blocks_a;            // int4
@@ -183,6 +189,7 @@ struct DevHMat {
   double k = 0;
   int maxk = 100;
   DevBuf near;            // complex storage of all near blocks
+  DevBuf nearT;           // transposed near field (FP32; built on the first transposed block matvec)
   DevBuf pool;            // rank-1 terms (u | v) of all admissible blocks
   DevBuf term_off;        // int64 [na * maxk] offset of each term in the pool
   DevBuf rank;            // int [na]
@@ -211,7 +218,7 @@ struct DevHMat {
   int64_t lr_entries = 0; // sum r (m + n)
   int64_t aca_evaluated = 0;  // entries ACA evaluated: sum passes (m + n)
   size_t bytes() const {
-    return near.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
+    return near.bytes + nearT.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
            tvec.bytes + tvec64.bytes + useg.bytes + vseg.bytes + uidx.bytes + vidx.bytes + kpos_f.bytes +
            kpos_t.bytes + pbuf.bytes + kseg_f.bytes + kseg_t.bytes + seg_f.bytes + seg_t.bytes + xdf.bytes;
   }
@@ -228,8 +235,8 @@ void launch_near_assembly(const DevGeometry& G, const DevPartition& DP, DevHMat&
 // Large blocks run on s, small blocks (one warp each) on s_small, which may be another stream.
 void launch_aca(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s,
                 cudaStream_t s_small);
-// Mixed-precision assembly with double-float entries and ACA (FP64-accurate pivots and ranks,
-// FP32 storage): near field into H.near (cf), ACA terms into H.pool (cdf).
+// Mixed-precision assembly with double-float entries and ACA recursion (FP64-accurate entries,
+// pivots and ranks; FP32 storage): near field into H.near (cf), ACA terms into H.pool (cdf).
 void launch_near_assembly_df(const DevGeometry& G, const DevPartition& DP, DevHMat& H, cudaStream_t s);
 void launch_aca_df(const DevGeometry& G, const DevPartition& DP, DevHMat& H, double eps, int max_rows, cudaStream_t s,
                    cudaStream_t s_small);

@@ -4,7 +4,10 @@
 // vectors hold nrb complex FP32 values per element, element-major (Ne x nrb), so every matrix
 // byte streamed from HBM serves nrb products. The passes follow the single-vector matvec
 // (matvec.cu) over the same per-leaf segments and copy ring: dot pass over the V segments,
-// per-term reduce, gather pass over the near and U segments. Forward orientation only.
+// per-term reduce, gather pass over the near and U segments. The plain transpose (adjoint solves,
+// hmatrix.h:95-115) runs the same passes with the roles swapped: dot pass over the U segments of
+// the row leaves, reduce over the blocks' row-leaf entries, gather over the V segments of the
+// column leaves and a transposed copy of the near field laid out by column leaf.
 //
 // Block BiCGSTAB: nrb independent BiCGSTAB recurrences (van der Vorst 1992) sharing the matvecs,
 // with per-column scalars, FP64 dot products reduced in fixed order, and per-column convergence;
@@ -16,6 +19,7 @@
 #include "internal.h"
 #include "multi.h"
 #include "segstream.cuh"
+#include "tcgen05.cuh"
 
 namespace ac3d {
 
@@ -142,6 +146,172 @@ __global__ void __launch_bounds__(kMT) mseg_dot_kernel(SegView V, const cf* __re
                          if (h == 0) out[(size_t)(c0 + c) * NRB + j] = cf(ar, ai);
                        }
                      });
+}
+
+// ------------------------------------------------------------------------------------------
+// Dot pass on the tensor cores (tcgen05; nrb = 8 or 16, leaves of at most 32 rows). For a leaf
+// with R rows and K segment columns, P (K x nrb complex) = S^T X_leaf is the real product
+// D (K x 2 nrb) = A (K x 2R) B (2R x 2 nrb), where row k of A is segment column k exactly as
+// stored (re, im interleaved, 2R floats) and B interleaves X by row: row 2r = (Xr_r | Xi_r),
+// row 2r + 1 = (-Xi_r | Xr_r); columns 0..nrb-1 of D are Re P, nrb..2nrb-1 Im P. Tiles of 128
+// segment columns (M = 128), N = 2 nrb, K = 2R rounded up to 8. Operands are TF32, each FP32
+// value split as hi + lo, product hi hi + hi lo + lo hi (three MMAs), FP32 accumulation in
+// tensor memory. The stages of the copy ring are repacked into the canonical K-major layout
+// (8-row x 16-byte core matrices) with core matrices 144 bytes apart along K, so that eight
+// consecutive 16-byte stores of one row land in eight different bank groups.
+// ------------------------------------------------------------------------------------------
+constexpr int kTcM = 128;
+constexpr int kTcLbo = 144;  // bytes between core matrices along K
+constexpr int kTcKmax = 64;  // 2R for leaves of up to 32 rows
+constexpr size_t kTcTileBytes = (size_t)(kTcM / 8) * (kTcKmax / 4) * kTcLbo;  // one A operand (hi or lo)
+
+__device__ __forceinline__ int tc_off_bytes(int row, int kq, int kq_n) {
+  return (row >> 3) * (kq_n * kTcLbo) + kq * kTcLbo + (row & 7) * 16;
+}
+
+template <int NRB>
+constexpr size_t tc_dot_smem() {
+  return 2 * kTcTileBytes + 2 * (size_t)(2 * NRB / 8) * (kTcKmax / 4) * kTcLbo + (size_t)kStages * kStageBytes;
+}
+
+template <int NRB>
+__global__ void __launch_bounds__(kMT, 1) mseg_dot_tc_kernel(SegView V, const cf* __restrict__ seg,
+                                                             const cf* __restrict__ X, cf* __restrict__ P,
+                                                             const int* __restrict__ done) {
+  constexpr int N = 2 * NRB;
+  constexpr size_t kB = (size_t)(N / 8) * (kTcKmax / 4) * kTcLbo;
+  extern __shared__ __align__(128) unsigned char dsmem[];
+  unsigned char* Ah = dsmem;
+  unsigned char* Al = Ah + kTcTileBytes;
+  unsigned char* Bh = Al + kTcTileBytes;
+  unsigned char* Bl = Bh + kB;
+  auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(Bl + kB);
+  __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ __align__(8) uint64_t mma_bar;
+  __shared__ uint32_t s_tmem;
+  if (done && *done) return;
+  const int leaf = V.order[blockIdx.x];
+  const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
+  const int k0 = V.b_kptr[leaf], K = V.b_kptr[leaf + 1] - k0;
+  if (K == 0 || R > kTcKmax / 2) return;  // the host launches this pass only for leaves of <= 32 rows
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int Kd = (2 * R + 7) & ~7, kq_n = Kd / 4;
+  // B operand, N x Kd K-major
+  for (int e = tid; e < N * kq_n; e += blockDim.x) {
+    const int n = e / kq_n, kq = e - n * kq_n, jj = n % NRB;
+    float v[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int kk = 4 * kq + q;
+      v[q] = 0.f;
+      if (kk < 2 * R) {
+        const cf x = X[(size_t)(ls + (kk >> 1)) * NRB + jj];
+        v[q] = n < NRB ? ((kk & 1) ? -x.im : x.re) : ((kk & 1) ? x.re : x.im);
+      }
+    }
+    float4 hi, lo;
+    split_tf32(v[0], hi.x, lo.x);
+    split_tf32(v[1], hi.y, lo.y);
+    split_tf32(v[2], hi.z, lo.z);
+    split_tf32(v[3], hi.w, lo.w);
+    *reinterpret_cast<float4*>(Bh + tc_off_bytes(n, kq, kq_n)) = hi;
+    *reinterpret_cast<float4*>(Bl + tc_off_bytes(n, kq, kq_n)) = lo;
+  }
+  if (tid == 0) mbar_init(&mma_bar, 1);
+  if (warp == 0) {
+    tmem_alloc(&s_tmem, 32);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  init_ring(full);  // fences the mbarrier inits and synchronises the CTA
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t idesc = umma_idesc_tf32(kTcM, N);
+  const uint32_t sbo = (uint32_t)(kq_n * kTcLbo);
+  int fill = 0, tile_k = 0;
+  uint32_t phase = 0;
+  bool mma_ok = true;
+  cf* out = P + (size_t)k0 * NRB;
+  // MMA of the current A tile, then rows 0..nrows-1 of D to P
+  auto flush = [&](int nrows) {
+    fence_proxy_async();  // the operand stores become visible to the tensor core
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      for (int ks = 0; ks < Kd / 8; ks++) {
+        const uint32_t o = (uint32_t)ks * 2u * kTcLbo;
+        const uint64_t ah = umma_smem_desc(Ah + o, kTcLbo, sbo), al = umma_smem_desc(Al + o, kTcLbo, sbo);
+        const uint64_t bh = umma_smem_desc(Bh + o, kTcLbo, sbo), bl = umma_smem_desc(Bl + o, kTcLbo, sbo);
+        umma_tf32(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
+        umma_tf32(tmem, ah, bl, idesc, 1u);
+        umma_tf32(tmem, al, bh, idesc, 1u);
+      }
+      umma_commit(&mma_bar);
+    }
+    // one verdict for the whole CTA (the barriers below must not diverge)
+    const bool got = !__syncthreads_or(!mbar_wait_bounded(&mma_bar, phase));
+    phase ^= 1u;
+    if (!got) {
+      mma_ok = false;
+      if (tid == 0) atomicExch(V.err, 1);
+    }
+    tc_fence_after();
+    if (warp < 4 && got) {
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), v);
+      const int row = warp * 32 + lane;
+      if (row < nrows) {
+        cf* o = out + (size_t)(tile_k + row) * NRB;
+#pragma unroll
+        for (int j = 0; j < NRB; j++) o[j] = cf(v[j], v[NRB + j]);
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  };
+  stream_leaf<float>(stage, full, R, nullptr, 0, seg + V.b_seg[leaf], K, V.err,
+                     [&](const cf* S, int, int, int ncols, int, int, int nncols) {
+                       int c = 0;
+                       while (c < ncols && mma_ok) {
+                         const int take = min(ncols - c, kTcM - fill);
+                         const float* src = reinterpret_cast<const float*>(S + (size_t)c * R);
+                         for (int e = tid; e < take * kq_n; e += blockDim.x) {
+                           const int rr = e / kq_n, kq = e - rr * kq_n;
+                           const float* rowp = src + (size_t)rr * 2 * R;
+                           float v[4];
+#pragma unroll
+                           for (int q = 0; q < 4; q++) {
+                             const int kk = 4 * kq + q;
+                             v[q] = kk < 2 * R ? rowp[kk] : 0.f;
+                           }
+                           float4 hi, lo;
+                           split_tf32(v[0], hi.x, lo.x);
+                           split_tf32(v[1], hi.y, lo.y);
+                           split_tf32(v[2], hi.z, lo.z);
+                           split_tf32(v[3], hi.w, lo.w);
+                           const int ob = tc_off_bytes(fill + rr, kq, kq_n);
+                           *reinterpret_cast<float4*>(Ah + ob) = hi;
+                           *reinterpret_cast<float4*>(Al + ob) = lo;
+                         }
+                         fill += take;
+                         c += take;
+                         if (fill == kTcM) {
+                           flush(kTcM);
+                           tile_k += kTcM;
+                           fill = 0;
+                         }
+                       }
+                       if (nncols == 0 && fill > 0 && mma_ok) {  // the leaf's last chunk
+                         flush(fill);
+                         tile_k += fill;
+                         fill = 0;
+                       }
+                     });
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, 32);
 }
 
 // T[task][j] = sum over the task's block entries of P[kpos[e] + q][j], in leaf order.
@@ -650,6 +820,12 @@ int multi_vec_grid(int n, int nrb) {
 
 constexpr size_t kMRing = (size_t)kStages * kStageBytes;
 
+template <int NRB>
+static void set_tc_attrs() {
+  AC3D_CUDA(cudaFuncSetAttribute(mseg_dot_tc_kernel<NRB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc_dot_smem<NRB>()));
+}
+
 template <int NRB, int RPL>
 static void set_multi_attrs() {
   AC3D_CUDA(cudaFuncSetAttribute(mseg_dot_kernel<NRB, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMRing));
@@ -668,43 +844,55 @@ void prepare_multi_kernels() {
     set_multi_attrs<8, 2>();
     set_multi_attrs<16, 1>();
     set_multi_attrs<16, 2>();
+    set_tc_attrs<8>();
+    set_tc_attrs<16>();
   });
 }
 
 template <int NRB, int RPL>
 static void mmv_t(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, const void* x, void* y,
                   const void* dot_a, const void* dot_b, const int* done, cudaStream_t s) {
+  const bool tr = B.tr;
+  if (tr && !H.nearT.p) throw Error(3, "internal: transposed near field not built");
   SegView v{};
   v.leaf_start = DP.leaf_start.as<int>();
-  v.a_seg = DP.near_seg.as<long long>();
-  v.a_kptr = DP.didx_ptr.as<int>();
-  v.a_idx = DP.didx.as<int>();
+  v.a_seg = tr ? DP.near_seg_t.as<long long>() : DP.near_seg.as<long long>();
+  v.a_kptr = tr ? DP.didx_t_ptr.as<int>() : DP.didx_ptr.as<int>();
+  v.a_idx = tr ? DP.didx_t.as<int>() : DP.didx.as<int>();
   v.err = H.err.as<int>();
   cf* P = (cf*)B.pbuf;
   cf* T = (cf*)B.tbuf;
   if (DP.na > 0) {
+    // dot pass: V segments of the column leaves (forward) or U segments of the row leaves (A^T)
     SegView d = v;
-    d.b_seg = H.seg_t.as<long long>();
-    d.b_kptr = H.kseg_t.as<int>();
-    d.order = H.order_cols.as<int>();
+    d.b_seg = tr ? H.seg_f.as<long long>() : H.seg_t.as<long long>();
+    d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
+    d.order = tr ? H.order_rows.as<int>() : H.order_cols.as<int>();
     note_launch();
-    mseg_dot_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(d, H.vseg.as<cf>(), (const cf*)x, P, done);
+    if (NRB >= 8 && RPL == 1 && B.tc)
+      mseg_dot_tc_kernel<NRB><<<DP.nleaf, kMT, tc_dot_smem<NRB>(), s>>>(d, tr ? H.useg.as<cf>() : H.vseg.as<cf>(),
+                                                                      (const cf*)x, P, done);
+    else
+      mseg_dot_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(d, tr ? H.useg.as<cf>() : H.vseg.as<cf>(),
+                                                               (const cf*)x, P, done);
     AC3D_CUDA(cudaGetLastError());
     note_launch();
     const long long thr = H.task_cap * NRB;
     mseg_reduce_kernel<NRB><<<(int)((thr + 255) / 256), 256, 0, s>>>(
-        H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na, DP.blk_tr_ptr.as<int>(),
-        H.kpos_t.as<int>(), P, T, done);
+        H.task_b.as<int>(), H.t_off.as<int>(), (int)H.task_cap, H.t_off.as<int>() + DP.na,
+        tr ? DP.blk_fw_ptr.as<int>() : DP.blk_tr_ptr.as<int>(), tr ? H.kpos_f.as<int>() : H.kpos_t.as<int>(), P,
+        T, done);
     AC3D_CUDA(cudaGetLastError());
   }
-  v.b_seg = H.seg_f.as<long long>();
-  v.b_kptr = H.kseg_f.as<int>();
-  v.b_idx = H.uidx.as<int>();
-  v.order = H.order_rows.as<int>();
+  v.b_seg = tr ? H.seg_t.as<long long>() : H.seg_f.as<long long>();
+  v.b_kptr = tr ? H.kseg_t.as<int>() : H.kseg_f.as<int>();
+  v.b_idx = tr ? H.vidx.as<int>() : H.uidx.as<int>();
+  v.order = tr ? H.order_cols.as<int>() : H.order_rows.as<int>();
   const bool dots = dot_a || dot_b;
   note_launch();
   mseg_gather_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(
-      v, H.near.as<cf>(), H.useg.as<cf>(), T, (const cf*)x, (cf*)y, (const cf*)dot_a, (const cf*)dot_b,
+      v, tr ? H.nearT.as<cf>() : H.near.as<cf>(), tr ? H.vseg.as<cf>() : H.useg.as<cf>(), T, (const cf*)x, (cf*)y,
+      (const cf*)dot_a, (const cf*)dot_b,
       dots ? B.partials : nullptr, B.partials + (size_t)std::max(DP.nleaf, 1184) * 5 * NRB, B.ticket, B.red, done);
   if (DP.nleaf > 1024 * kGroup) throw Error(1, "block solves support at most 32768 leaf clusters");
   AC3D_CUDA(cudaGetLastError());
@@ -719,6 +907,34 @@ static void mmv_rpl(const DevPartition& DP, const DevHMat& H, const MultiBufs& B
     mmv_t<NRB, 2>(DP, H, B, x, y, dot_a, dot_b, done, s);
   else
     throw Error(1, "block solves need leaf clusters of at most 64 elements");
+}
+
+// One CTA per near block: block b (m x n, column-major at near_off[b]) transposed to n x m
+// column-major at near_off_t[b]. Padding columns of the transposed segments stay zero.
+__global__ void near_transpose_kernel(const int4* __restrict__ blocks, const long long* __restrict__ off,
+                                      const long long* __restrict__ off_t, const cf* __restrict__ near, cf* nearT) {
+  const int b = blockIdx.x;
+  const int4 q = blocks[b];
+  const int m = q.y - q.x, n = q.w - q.z;
+  const cf* src = near + off[b];
+  cf* dst = nearT + off_t[b];
+  for (int t = threadIdx.x; t < m * n; t += blockDim.x) {
+    const int r = t / n, c = t - r * n;
+    dst[t] = src[c * m + r];
+  }
+}
+
+void ensure_near_transposed(const DevPartition& DP, DevHMat& H, cudaStream_t s) {
+  if (H.nearT.p) return;
+  if (H.prec == PREC_FP64) throw Error(3, "internal: block matvec needs FP32 storage");
+  const size_t bytes = (size_t)std::max<int64_t>(DP.near_total_t, 2) * sizeof(cf);
+  H.nearT.alloc(bytes, s);
+  AC3D_CUDA(cudaMemsetAsync(H.nearT.p, 0, bytes, s));
+  if (DP.nd == 0) return;
+  note_launch();
+  near_transpose_kernel<<<DP.nd, 256, 0, s>>>(DP.blocks_d.as<int4>(), DP.near_off.as<long long>(),
+                                              DP.near_off_t.as<long long>(), H.near.as<cf>(), H.nearT.as<cf>());
+  AC3D_CUDA(cudaGetLastError());
 }
 
 void launch_mmatvec(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, const void* x, void* y,

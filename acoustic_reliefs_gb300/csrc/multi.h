@@ -27,6 +27,8 @@ struct KStateM {
 // Block vectors: nrb complex FP32 values per element, element-major (Ne x nrb).
 struct MultiBufs {
   int n = 0, nrb = 0;
+  bool tr = false;             // plain transpose A^T (adjoint solves) instead of A
+  bool tc = true;              // dot pass on the tensor cores (nrb 8 or 16, leaves of <= 32 rows)
   void *b = nullptr, *x = nullptr, *r = nullptr, *rhat = nullptr, *p = nullptr, *v = nullptr, *s = nullptr,
        *t = nullptr;
   double* partials = nullptr;  // (max(nleaf, 1184) + 1024) x 5 x nrb: matvec partials, group totals
@@ -41,10 +43,14 @@ struct MultiBufs {
 
 int multi_vec_grid(int n, int nrb);
 void prepare_multi_kernels();
-// y = A x for block vectors; optional dot partials per column (dot_a: conj(a).y, dot_b: conj(y).b
-// and |y|^2), reduced in fixed order into red (5 x nrb). Forward orientation, FP32 storage only.
+// y = A x (or A^T x with B.tr) for block vectors; optional dot partials per column (dot_a:
+// conj(a).y, dot_b: conj(y).b and |y|^2), reduced in fixed order into red (5 x nrb). FP32 storage
+// only. The transposed orientation streams the same per-leaf segments with the roles of U and V
+// swapped and a transposed copy of the near field (ensure_near_transposed).
 void launch_mmatvec(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, const void* x, void* y,
                     const void* dot_a, const void* dot_b, const int* done, cudaStream_t s);
+// Builds H.nearT, the near blocks transposed into the segment layout of A^T (once per H-matrix).
+void ensure_near_transposed(const DevPartition& DP, DevHMat& H, cudaStream_t s);
 void mkrylov_enqueue_init(const MultiBufs& B, int maxit, cudaStream_t s);
 void mkrylov_enqueue_iterations(const MultiBufs& B, const DevPartition& DP, const DevHMat& H, int count,
                                 cudaStream_t s);

@@ -191,6 +191,30 @@ void build_leaf_lists(Partition& P, int maxk) {
   }
   P.near_seg[nleaf] = off;
   P.near_total = off;
+  // near storage of the transpose (block adjoint solves): the blocks whose columns are leaf l,
+  // each transposed to (its columns) x (its rows) column-major, in row order, form leaf l's
+  // segment; its columns are the blocks' rows
+  P.near_off_t.assign(nd, 0);
+  P.near_seg_t.assign(nleaf + 1, 0);
+  P.didx_t_ptr.assign(nleaf + 1, 0);
+  P.didx_t.clear();
+  off = 0;
+  for (int l = 0; l < nleaf; l++) {
+    P.near_seg_t[l] = off;
+    for (int b : tn[l]) {
+      const int* q = &P.direct[4 * b];
+      P.near_off_t[b] = off;
+      off += (int64_t)(q[1] - q[0]) * (q[3] - q[2]);
+      for (int r = q[0]; r < q[1]; r++) P.didx_t.push_back(r);
+    }
+    if ((P.didx_t.size() - P.didx_t_ptr[l]) & 1) {
+      P.didx_t.push_back(-1);
+      off += P.leaf_start[l + 1] - P.leaf_start[l];
+    }
+    P.didx_t_ptr[l + 1] = (int)P.didx_t.size();
+  }
+  P.near_seg_t[nleaf] = off;
+  P.near_total_t = off;
   csr(fl, P.fw_lr_ptr, P.fw_lr);
   csr(tn, P.tr_near_ptr, P.tr_near);
   csr(tl, P.tr_lr_ptr, P.tr_lr);

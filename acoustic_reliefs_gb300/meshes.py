@@ -173,6 +173,38 @@ def relief(w: float = 0.6, b: float = 0.6, h: float = 0.05, nx: int = 64, ny: in
     return Relief(Ps, Es, top, uvs)
 
 
+def relief_device(w: float = 0.6, b: float = 0.6, h: float = 0.05, nx: int = 64, ny: int = 8, nz: int = 64,
+                  subdiv_top: int = 0, device=None):
+    """The base box, top-face subdivision and top uvs of ``relief`` generated by CUDA kernels
+    (``ac3d_relief_dev``) into torch device tensors: (Ps (V,3) float64, Es (F,3) int32, top ids,
+    uvs (n_top,2) float64), bitwise the host generator's. Heights are then the texture lookup at
+    the uvs (``autograd.TexMap``)."""
+    import ctypes
+
+    import torch
+
+    from . import _lib as _L
+    L = _L.lib()
+    V, F = ctypes.c_int(), ctypes.c_int()
+    rc = L.ac3d_relief_sizes(int(nx), int(ny), int(nz), int(subdiv_top), ctypes.byref(V), ctypes.byref(F))
+    if rc != _L.OK:
+        raise _L.AC3DError(rc, "invalid relief parameters")
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    Ps = torch.empty((V.value, 3), dtype=torch.float64, device=dev)
+    Es = torch.empty((F.value, 3), dtype=torch.int32, device=dev)
+    top = torch.empty(V.value, dtype=torch.int32, device=dev)
+    uvs = torch.empty((V.value, 2), dtype=torch.float64, device=dev)
+    nt = ctypes.c_int()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    rc = L.ac3d_relief_dev(float(w), float(b), float(h), int(nx), int(ny), int(nz), int(subdiv_top),
+                           ctypes.c_void_p(Ps.data_ptr()), ctypes.c_void_p(Es.data_ptr()),
+                           ctypes.c_void_p(top.data_ptr()), ctypes.c_void_p(uvs.data_ptr()), ctypes.byref(nt),
+                           ctypes.c_void_p(stream))
+    if rc != _L.OK:
+        raise _L.AC3DError(rc, "relief generation failed")
+    return Ps, Es, top[:nt.value], uvs[:nt.value]
+
+
 def icosphere(subdivisions: int = 3, radius: float = 1.0):
     """Geodesic sphere: icosahedron with `subdivisions` midpoint refinements (20 * 4^s
     triangles), vertices projected to the sphere, triangles wound outward."""

@@ -47,9 +47,10 @@ WORKLOAD = ("0.6 m relief, 64x64 smoothed seeded heightmap, 20480 triangles, 2 k
             "181 receivers on a 5 m semicircle, leaf 32, eta 2, ACA 1e-4, BiCGSTAB 1e-6")
 
 
-SWEEP_BANDS = (125, 160, 200, 250, 315, 400, 500, 630, 800, 1000, 1250, 1600, 2000, 2500, 3150, 4000)
+# the reference pipeline's third-octave bands (acoustics_pipeline.py:7), 3 frequencies each
+SWEEP_BANDS = (100, 125, 160, 200, 250, 315, 400, 500, 630, 800, 1000, 1250, 1600, 2000, 2500, 3150, 4000)
 SWEEP_WORKLOAD = ("served sweep: 0.6 m reliefs (30x7x30 box, subdiv_top {subdivs}: {sizes} triangles), seeded "
-                  "smoothed 64x64 heightmap, 3 frequencies per third-octave band 125 Hz - 4 kHz (48 per relief), "
+                  "smoothed 64x64 heightmap, 3 frequencies per third-octave band 100 Hz - 4 kHz (51 per relief), "
                   "normal plane wave, 181 receivers on a 5 m semicircle, leaf 32, eta 2, ACA 1e-4, BiCGSTAB 1e-6")
 
 
@@ -119,16 +120,104 @@ def served_sweep(args, Ls):
     thr_l, lat_l, _ = run_served("mixed", reliefs, reqs, Ls, args.slots, rate, 0, args.krylov)
     out["mixed"].update({"poisson_rate_per_s": rate, "solves_per_s_at_rate": thr_l,
                          "p50_ms": float(np.percentile(lat_l, 50)), "p99_ms": float(np.percentile(lat_l, 99))})
+    info = [r[1] for r in res_m]
+    out["mixed"].update({
+        "run_ms_p50": float(np.percentile([i["run_ms"] for i in info], 50)),
+        "run_ms_p99": float(np.percentile([i["run_ms"] for i in info], 99)),
+        "ms_graph_mean": float(np.mean([i["ms_graph"] for i in info])),
+        "note": "saturated latency = queueing + run; run_ms = admitted to result; ms_graph = host time capturing "
+                "and instantiating the request's solver graphs"})
     if not args.no_fp64_sweep:
         thr64, lat64, res_d = run_served("fp64", reliefs, reqs, Ls, args.slots, None, 0, args.krylov)
-        err = max(float(np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0])) for a, b in zip(res_m, res_d))
+        errs = [float(np.linalg.norm(a[0] - b[0]) / np.linalg.norm(b[0])) for a, b in zip(res_m, res_d)]
         out["fp64"] = {"solves_per_s": thr64, "offered": "all requests at t=0 (saturated)",
                        "p50_ms_saturated": float(np.percentile(lat64, 50)),
                        "p99_ms_saturated": float(np.percentile(lat64, 99))}
         out["speedup_mixed_over_fp64"] = thr / thr64
-        out["max_pressure_rel_err_mixed_vs_fp64"] = err
+        out["max_pressure_rel_err_mixed_vs_fp64"] = max(errs)
+        out["requests_above_1e-4"] = int(sum(e > 1e-4 for e in errs))
+        out["max_pressure_rel_err_by_relief"] = {
+            str(len(R.Es)): max(e for e, (mi, _) in zip(errs, reqs) if mi == i) for i, R in enumerate(reliefs)}
     out["max_rel_residual"] = max(r[1]["rel_residual"] for r in res_m)
     return out
+
+
+def gradient_leg():
+    """configs[3] at size: 0.9 m relief with a 128 x 128 heightmap (81024 triangles, 37445
+    differentiable heights), 1, 2 and 4 kHz, 37 incidence angles in the xy plane, receivers on a
+    10 m semicircle: loss = 1 - mean coefficient and its gradient in one call, timed once after a
+    small warm-up call."""
+    from acoustic_reliefs_gb300 import meshes
+    from acoustic_reliefs_gb300.acoustics3d import DiffBEM
+    R = meshes.relief(0.9, 0.9, 0.05, 48, 7, 48, 2, meshes.smooth_heightmap(128, 0))
+    th = np.radians(np.linspace(-90.0, 90.0, 37))
+    dirs = np.stack([np.sin(th), -np.cos(th), np.zeros_like(th)], 1)
+    freqs = [1000.0, 2000.0, 4000.0]
+    x = np.random.default_rng(4).uniform(0.0, 0.01, size=len(R.diff_pts))
+    bem = DiffBEM(LEAF, FACTOR, [1000.0], 1, ACA_TOL, ACA_TOL, SOLVER_TOL, precision="mixed")
+    bem.silent = True
+    bem.set_krylov("gmres", RESTART)
+    bem.set_listeners(meshes.semicircle(10.0, 181))
+    bem.precompute(R.Ps, R.Es, R.diff_pts)
+    bem.gradient_multi(x, [1000.0], dirs[:2])
+    t0 = time.perf_counter()
+    loss, g, cf = bem.gradient_multi(x, freqs, dirs)
+    dt = time.perf_counter() - t0
+    st = bem.stats()
+    return {"workload": "0.9 m relief, 128x128 smoothed seeded heightmap, 81024 triangles, 37445 heights; 1/2/4 kHz x "
+                        "37 plane-wave angles (-90..90 deg in the xy plane); 181 receivers on a 10 m semicircle; "
+                        "loss 1 - mean coefficient; mixed precision, GMRES, leaf 32, eta 2, ACA 1e-4, tol 1e-6",
+            "seconds": dt, "gradients_per_s": 1.0 / dt, "loss": loss, "grad_norm": float(np.linalg.norm(g)),
+            "solves": st["solves"], "iterations": st["iterations"], "ms_assemble": st["ms_assemble"],
+            "ms_solve": st["ms_solve"], "ms_adjoint": st["ms_adjoint"],
+            "note": "per frequency one H-matrix: forward and transposed block solves (16 directions per block), "
+                    "shape-derivative terms of 16 directions per derivative evaluation (ac3d_gradient_multi)"}
+
+
+def block_c5_leg():
+    """configs[4] at size: 0.9 m relief with a 256 x 256 heightmap (210240 triangles) at 4 kHz,
+    16 plane-wave directions as one block; error against the FP64 solve of the first direction."""
+    from acoustic_reliefs_gb300 import meshes
+    from acoustic_reliefs_gb300.acoustics3d import DiffBEM
+    R = meshes.relief(0.9, 0.9, 0.05, 40, 7, 40, 3, meshes.smooth_heightmap(256, 0))
+    Ls = meshes.semicircle(5.0, 181)
+    rng = np.random.default_rng(1)
+    dirs = rng.normal(size=(16, 3))
+    dirs[:, 1] = -np.abs(dirs[:, 1]) - 0.5
+    dirs[0] = DIRECTION
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    bem = DiffBEM(LEAF, FACTOR, [4000.0], 1, ACA_TOL, ACA_TOL, SOLVER_TOL, precision="mixed")
+    bem.silent = True
+    bem.set_krylov("gmres", RESTART)
+    bem.set_mesh(R.Ps, R.Es)
+    t0 = time.perf_counter()
+    P = bem.pvals_multi(4000.0, dirs, Ls)
+    dt = time.perf_counter() - t0
+    st = bem.stats()
+    mv_ms, mv_bytes = bem.block_matvec_timing(16, 10)
+    bem.set_tensor_cores(False)
+    mv_ms_cc, _ = bem.block_matvec_timing(16, 10)
+    bem.set_tensor_cores(True)
+    b64 = DiffBEM(LEAF, FACTOR, [4000.0], 1, ACA_TOL, ACA_TOL, SOLVER_TOL, precision="fp64",
+                  incident=("plane", dirs[0]))
+    b64.silent = True
+    b64.set_krylov("gmres", RESTART)
+    b64.set_mesh(R.Ps, R.Es)
+    t1 = time.perf_counter()
+    y64 = b64.pvals(4000.0, Ls)
+    dt64 = time.perf_counter() - t1
+    peak, _ = measured_peak()
+    gbs = mv_bytes / (mv_ms / 1e3) / 1e9
+    return {"workload": "0.9 m relief, 256x256 smoothed seeded heightmap, 210240 triangles, 4 kHz, 16 plane-wave "
+                        "directions as one block, 181 receivers on a 5 m semicircle, leaf 32, eta 2, ACA 1e-4, tol 1e-6",
+            "seconds_per_block": dt, "solves_per_s": 16 / dt, "hmat_bytes": st["hmat_bytes"],
+            "ms_assemble": st["ms_assemble"], "ms_solve": st["ms_solve"], "iterations": st["iterations"],
+            "near_entries": st["near_entries"], "lr_entries": st["lr_entries"],
+            "block_matvec_ms": mv_ms, "block_matvec_bytes": int(mv_bytes), "block_matvec_gbs": gbs,
+            "block_matvec_frac_of_hbm": gbs / peak, "block_matvec_ms_cuda_cores": mv_ms_cc,
+            "dot_pass": "tensor cores (tcgen05.mma kind::tf32, hi/lo split, three products, FP32 accumulation in TMEM)",
+            "fp64_single_solve_s": dt64,
+            "pressure_rel_err_vs_fp64": float(np.linalg.norm(P[0] - y64) / np.linalg.norm(y64))}
 
 
 def workload(seed: int = 0):
@@ -593,6 +682,10 @@ def run_gpu(args):
         line["multi_rhs"] = multi
     if args.sweep_subdivs not in ("", "none") and world == 1:
         line["served_sweep"] = served_sweep(args, Ls)
+    if not args.no_gradient_leg and world == 1:
+        line["gradient_c4"] = gradient_leg()
+    if not args.no_c5_leg and world == 1:
+        line["block_c5"] = block_c5_leg()
     print(json.dumps(line), flush=True)
     return 0
 
@@ -605,10 +698,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--inner-tol", type=float, default=1e-6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sweep-subdivs", default="0,1,2",
-                    help="subdiv_top levels of the served sweep ('none' to skip; 3 adds the 118680-triangle relief)")
+    ap.add_argument("--sweep-subdivs", default="0,1,2,3",
+                    help="subdiv_top levels of the served sweep ('none' to skip; 5280/10680/32280/118680 triangles)")
     ap.add_argument("--slots", type=int, default=4, help="server slots (concurrent requests)")
     ap.add_argument("--no-fp64-sweep", action="store_true")
+    ap.add_argument("--no-gradient-leg", action="store_true", help="skip the 81k-triangle 37-angle gradient")
+    ap.add_argument("--no-c5-leg", action="store_true", help="skip the 210k-triangle 16-direction block solve")
     ap.add_argument("--multi-rhs", type=int, default=16, help="directions of the block-solve leg (0 to skip)")
     ap.add_argument("--krylov", default="gmres", choices=["gmres", "bicgstab"],
                     help="inner solver of every GPU leg (BiCGSTAB is the reference's; a served BiCGSTAB leg is "

@@ -38,7 +38,7 @@ extern "C" {
 #define AC3D_KRYLOV_GMRES 1    /* GMRES: one matvec per iteration, restarted by the refinement loop */
 
 #define AC3D_ASSEMBLY_DF 0    /* mixed precision: entries and ACA in double-float (FP64-accurate
-                                 pivots and ranks), factors stored in FP32 (default) */
+                                 pivots and ranks), stored in FP32 (default) */
 #define AC3D_ASSEMBLY_FP32 1  /* mixed precision: entries and ACA in FP32 */
 
 #define AC3D_LISTENER_DENSE 0 /* receiver matrix evaluated exactly on the fly */
@@ -93,12 +93,18 @@ int ac3d_set_solver(ac3d_ctx* ctx, int max_iterations, double inner_tol, int max
  * block matvec, instead of block BiCGSTAB. No reference counterpart. */
 int ac3d_set_krylov(ac3d_ctx* ctx, int method, int restart);
 /* Arithmetic of the mixed-precision assembly (no effect on AC3D_PREC_FP64): AC3D_ASSEMBLY_DF
- * (default) evaluates near-field entries and runs ACA (compute_ACA_block, aca.cpp:38-82) in
- * double-float arithmetic on the FP32 pipes, so the low-rank blocks have the FP64 path's pivots
- * and ranks and differ from its factors only by their FP32 rounding; AC3D_ASSEMBLY_FP32 runs
- * them in FP32 (faster; pivots and ranks may differ from the FP64 path's where candidates are
- * within FP32 rounding of each other). No reference counterpart. */
+ * (default) evaluates near-field entries, the admissible blocks' rows and columns, and runs ACA
+ * (compute_ACA_block, aca.cpp:38-82; receivers aca.cpp:84-134) in double-float arithmetic on the
+ * FP32 pipes, so the low-rank blocks have the FP64 path's pivots and ranks and every stored entry
+ * differs from the FP64 path's only by its FP32 rounding; AC3D_ASSEMBLY_FP32 evaluates in FP32
+ * (faster; pivots and ranks may differ from the FP64 path's where candidates are within FP32
+ * rounding of each other). No reference counterpart. */
 int ac3d_set_assembly(ac3d_ctx* ctx, int mode);
+/* Block matvecs of 8 or 16 right-hand sides (ac3d_solve_multi, ac3d_gradient_multi) form their
+ * dot pass S^T X on the tensor cores (tcgen05.mma, TF32 operands split in three products, FP32
+ * accumulation) when on (default) and leaves have at most 32 elements; off: FP32 CUDA cores.
+ * No reference counterpart. */
+int ac3d_set_tensor_cores(ac3d_ctx* ctx, int on);
 /* Replace the receivers used by value / values / band_value / gradient (default: the
  * hemisphere of compute_listener_pts, helpers.cpp:52-65). */
 int ac3d_set_listeners(ac3d_ctx* ctx, const double* Ls, int L);
@@ -150,6 +156,16 @@ int ac3d_gradient(ac3d_ctx* ctx, const double* x, double* c, double* grad);
  * after `stream` (a cudaStream_t) and `stream` waits for its completion. */
 int ac3d_value_dev(ac3d_ctx* ctx, const double* x_dev, double* c_dev, void* stream);
 int ac3d_gradient_dev(ac3d_ctx* ctx, const double* x_dev, double* c_dev, double* grad_dev, void* stream);
+/* Multi-incidence objective: loss = 1 - mean over the nf frequencies and nd plane-wave directions
+ * (nd x 3, normalised here) of the diffusion coefficient of the context's receivers for that one
+ * frequency and direction (compute_u, adjoint.cpp:388-397, on one |y|), with heights x (HH);
+ * grad (HH) receives d loss / dx, coefs (nf x nd, frequency-major, may be NULL) the coefficients.
+ * The gradient is the reference's adjoint (adjoint.cpp:24-242) per frequency and direction; here
+ * the directions of a frequency share one H-matrix, forward and transposed block solves and every
+ * shape-derivative evaluation. No reference counterpart as one call (the reference's objective has
+ * one point source). */
+int ac3d_gradient_multi(ac3d_ctx* ctx, const double* x, const double* freqs, int nf, const double* dirs, int nd,
+                        double* loss, double* grad, double* coefs);
 
 /* sphere(sphere_mesh, freq, LL, lrad, actual) -- sphere.h:28-85, with the mesh passed as
  * arrays instead of an OBJ path: leaf 128, factor 1.5, ACA and solver tolerance 1e-10, plane
@@ -207,6 +223,12 @@ int ac3d_matvec_timing(ac3d_ctx* ctx, int iters, int transposed, double* ms_per_
  * order of ac3d_partition_get's approx list; n must equal that count (stats n_approx). No
  * reference counterpart (the reference keeps them inside HMatrix, hmatrix.h:27-71). */
 int ac3d_get_ranks(ac3d_ctx* ctx, int32_t* ranks, int n);
+/* Times the block matvec of nrb (4, 8 or 16) right-hand sides (A, or its plain transpose with
+ * transposed != 0) on the FP32 H-matrix of the most recent solve, as the block solvers launch it,
+ * with CUDA events on the context stream. Outputs the mean milliseconds per block matvec and its
+ * algorithmic bytes: stored entries x 8 + the block input and output (8 Ne nrb each). No reference
+ * counterpart. */
+int ac3d_block_matvec_timing(ac3d_ctx* ctx, int nrb, int iters, int transposed, double* ms, long long* bytes);
 
 /* Receiver far field y_l = sum_j M(receiver l, element j) x_j (FP64), with every argument in
  * device memory: Ps_dev (V x 3 float64), Es_dev (Ne x 3 int32, the connectivity x is ordered by,
@@ -228,6 +250,18 @@ int ac3d_get_ranks(ac3d_ctx* ctx, int32_t* ranks, int n);
  * product, aca.cpp:84-134 with adjoint.cpp:101-102). */
 int ac3d_far_field_noalloc(const double* Ps_dev, int V, const int32_t* Es_dev, int Ne, const double* x_dev, double k,
                            const double* Ls_dev, int L, double* y_dev, void* stream);
+
+/* Relief mesh generated on the device (generate_base_mesh + face_subdivision,
+ * pyoptim/mesher.py:87-231; top vertices and uvs as acoustics_opt.py:182-210): a w x h x b box of
+ * six unwelded structured face grids (nx x ny, nx x nz, ny x nz quads, two triangles each), the
+ * top face (y = h) subdivided subdiv_top times 1 -> 4. ac3d_relief_sizes gives the vertex and
+ * triangle counts; ac3d_relief_dev writes Ps_dev (V x 3 float64), Es_dev (F x 3 int32), the top
+ * vertex ids top_dev and their uvs uvs_dev (n_top x 2 float64; both sized for up to V entries), on
+ * `stream`, and waits for it. Bitwise the host generator's output. Heights from a heightmap are then
+ * the texture lookup of ac3d_texmap_sample_dev at these uvs. */
+int ac3d_relief_sizes(int nx, int ny, int nz, int subdiv_top, int* V, int* F);
+int ac3d_relief_dev(double w, double b, double h, int nx, int ny, int nz, int subdiv_top, double* Ps_dev,
+                    int32_t* Es_dev, int32_t* top_dev, double* uvs_dev, int* n_top, void* stream);
 
 /* Host-only cluster tree and block partition (ClusterTree, clustertree.cpp:49-137, as used by
  * set_mesh, acoustics3d.cpp:43-58). No GPU work: for inspection and tests. */

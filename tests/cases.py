@@ -22,5 +22,13 @@ def relief_small(seed=0, nx=30, ny=7, subdiv=0, freq=2000.0):
                 Ls=meshes.semicircle(5.0, 181), leaf=32, factor=2.0, aca_tol=1e-4, tol=1e-6)
 
 
+def relief_c2(seed=0):
+    """The bench workload: 0.6 m relief with a seeded smoothed 64 x 64 heightmap, 20480 triangles,
+    2 kHz, normal plane wave (-y), 181 receivers on a 5 m semicircle."""
+    R = meshes.relief_20k(seed)
+    return dict(Ps=R.Ps, Es=R.Es, relief=R, freq=2000.0, kind=1, vec=np.array([0.0, -1.0, 0.0]),
+                Ls=meshes.semicircle(5.0, 181), leaf=32, factor=2.0, aca_tol=1e-4, tol=1e-6)
+
+
 def rel_l2(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))

@@ -7,6 +7,9 @@ relief_small.npz: the 5280-triangle relief case -- oracle receiver pressures (FP
 tol 1e-6) with the exact (y_oracle) and ACA (y_oracle_aca) receiver matrix, surface solution,
 per-block ACA ranks (iterations, the reference's count) and stored ranks (terms with u != 0 and
 v != 0), used by the GPU parity tests without re-running the oracle.
+relief_c2.npz: the bench workload (0.6 m relief, 20480 triangles, 2 kHz, normal plane wave, 181
+receivers on a 5 m semicircle, leaf 32, factor 2, ACA 1e-4, tol 1e-6) -- oracle pressures with the
+exact receiver matrix and the stored ranks.
 """
 import os
 import sys
@@ -41,6 +44,14 @@ def main():
     assert np.array_equal(H.ranks, info["ranks"])
     np.savez_compressed(os.path.join(out, "relief_small.npz"), Es_tree=m.Es, y_oracle=y, y_oracle_aca=ya,
                         x_oracle=x, ranks=info["ranks"], ranks_stored=H.stored_ranks(), iters=info["iters"])
+    c = cases.relief_c2()
+    m = oracle.Mesh(c["Ps"], c["Es"], c["leaf"], c["factor"])
+    k = oracle.wavenumber(c["freq"])
+    y, x, info = oracle.solve_pressures(m, k, c["vec"], 1, c["Ls"], c["aca_tol"], c["aca_tol"], c["tol"],
+                                        listener="dense")
+    H = oracle.HMat(m, k, c["aca_tol"])
+    np.savez_compressed(os.path.join(out, "relief_c2.npz"), Es_tree=m.Es, y_oracle=y,
+                        ranks_stored=H.stored_ranks(), iters=info["iters"])
 
 
 if __name__ == "__main__":

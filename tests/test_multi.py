@@ -79,3 +79,26 @@ def test_block_solve_point_sources_and_repeatable(gpu_lib):
     assert np.array_equal(P1, P2)
     bem.set_incident("point", srcs[1])
     assert cases.rel_l2(P1[1], bem.pvals(c["freq"], c["Ls"])) < 1e-4
+
+
+@pytest.mark.parametrize("nrhs", [6, 16])
+def test_tensor_core_dot_pass_matches_cuda_cores(gpu_lib, nrhs):
+    """The block dot pass on the tensor cores (tcgen05, TF32 split in three products) and on the
+    FP32 CUDA cores solve to the same answers: both runs reach relative residual 1e-8 on the same
+    H-matrix, so their pressures agree to about that level."""
+    c = cases.relief_small()
+    rng = np.random.default_rng(3)
+    dirs = rng.normal(size=(nrhs, 3))
+    dirs[:, 1] = -np.abs(dirs[:, 1]) - 0.5
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    out = {}
+    for tc in (True, False):
+        bem = DiffBEM(c["leaf"], c["factor"], [c["freq"]], 1, c["aca_tol"], c["aca_tol"], 1e-8, precision="mixed")
+        bem.silent = True
+        bem.set_krylov("gmres")
+        bem.set_tensor_cores(tc)
+        bem.set_mesh(c["Ps"], c["Es"])
+        out[tc] = bem.pvals_multi(c["freq"], dirs, c["Ls"])
+        st = bem.stats()
+        assert st["converged"] == 1 and st["rel_residual"] <= 1e-8
+    assert cases.rel_l2(out[True], out[False]) < 1e-6
