@@ -81,6 +81,7 @@ def test_block_solve_point_sources_and_repeatable(gpu_lib):
     assert cases.rel_l2(P1[1], bem.pvals(c["freq"], c["Ls"])) < 1e-4
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("nrhs", [6, 16])
 def test_tensor_core_dot_pass_matches_cuda_cores(gpu_lib, nrhs):
     """The block dot pass on the tensor cores (tcgen05, TF32 split in three products) and on the
