@@ -226,10 +226,6 @@ static void adjoint_t(const DevGeometry& G, const AdjointArgs& a, DevBuf& scratc
 // derivative entry is evaluated once and multiplied into every direction's vectors; per
 // (target, direction) the sums are reduced in the same fixed order as the single-direction path.
 // ------------------------------------------------------------------------------------------
-namespace {
-constexpr int kMTile = 2;  // targets per CTA of the multi-direction sweeps
-}  // namespace
-
 template <typename R>
 __device__ __forceinline__ cplx<R> ld_c(const cd* p) {
   const cd v = *p;
@@ -268,118 +264,83 @@ __global__ void __launch_bounds__(kAdjThreads) derA_multi_kernel(GeoView<R> G, A
   }
 }
 
-// Per-CTA reduction of acc[KT][NR] (complex) into part[((t0 + p) NR + r) S + split].
-template <int NR>
-__device__ __forceinline__ void multi_store(const double* accd, int t0, int ntarget, int split, int S, cd* part,
-                                            double (*sd)[2 * kMTile * NR]) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int v = 0; v < 2 * kMTile * NR; v++) {
-    const double x = warp_sum(accd[v]);
-    if (lane == 0) sd[w][v] = x;
-  }
-  __syncthreads();
-  for (int v = threadIdx.x; v < 2 * kMTile * NR; v += blockDim.x) {
-    const int p = v / (2 * NR), r = (v / 2) % NR;
-    if (t0 + p < ntarget) {
-      double sum = 0;
-      for (int ww = 0; ww < kAdjWarps; ww++) sum += sd[ww][v];
-      double* dst = (double*)&part[((size_t)(t0 + p) * NR + r) * S + split];
-      dst[v & 1] = sum;
-    }
-  }
-}
+// der_B's sweeps for every direction as tiled products: a CTA takes kBT targets; per tile of kBJ
+// elements every derivative entry (target, element) is evaluated once into shared memory, the
+// tile's kBJ x NR vector values are staged beside it, and each thread accumulates two (target,
+// direction) sums over the tile in element order. Partials per element split, summed in split
+// order by the combine kernel.
+namespace {
+constexpr int kBT = 32;  // targets per CTA
+template <typename R>
+constexpr int bj() { return sizeof(R) == 4 ? 64 : 32; }  // elements per tile (FP64 tiles are half as long)
+}  // namespace
 
-// s1 for every direction: sum_j x_r[j] dM(c_i, tri_j)/dp_y over the touched elements i
-template <typename R, int NR>
-__global__ void __launch_bounds__(kAdjThreads) derB_s1_multi_kernel(GeoView<R> G, AdjointMultiArgs a, cd* part,
-                                                                    int S) {
-  __shared__ double sd[kAdjWarps][2 * kMTile * NR];
-  const int t0 = blockIdx.x * kMTile, split = blockIdx.y;
+// s1[(i, r)] = sum_j x_r[j] dM(c_i, tri_j)/dp_y over the touched elements i (kind 0), or
+// s2[(pair, r)] = sum_j lmb_r[j] dM(c_j, tri_i)/dq_{o,y} over the incidences (i, o) (kind 1)
+template <typename R, int NR, int KIND>
+__global__ void __launch_bounds__(kAdjThreads) derB_tiled_kernel(GeoView<R> G, AdjointMultiArgs a, cd* part, int S) {
+  static_assert(kBT * NR == 2 * kAdjThreads, "two (target, direction) sums per thread");
+  constexpr int kBJ = bj<R>();
+  __shared__ cplx<R> Dt[kBT][kBJ + 1];
+  __shared__ cplx<R> Vt[kBJ][NR];
+  __shared__ double4 Tp[kBT];     // target point (kind 0: centroid of i) or vertex a of i (kind 1)
+  __shared__ ElemGeo<R> Tg[kBT];  // kind 1: geometry of i
+  __shared__ int To[kBT];         // kind 1: corner o
+  const int ntarget = KIND == 0 ? a.ntouch : a.npairs;
+  const int t0 = blockIdx.x * kBT, split = blockIdx.y;
   const int per = (G.ne + S - 1) / S;
   const int j0 = split * per, j1 = min(G.ne, j0 + per);
-  double4 C[kMTile];
-  for (int p = 0; p < kMTile; p++) C[p] = G.cen[a.touch_elem[min(t0 + p, a.ntouch - 1)]];
-  R ar[kMTile][NR], ai[kMTile][NR];
-#pragma unroll
-  for (int p = 0; p < kMTile; p++)
-#pragma unroll
-    for (int r = 0; r < NR; r++) ar[p][r] = ai[p][r] = 0;
+  const cd* vec = KIND == 0 ? a.x : a.lmb;
+  for (int p = threadIdx.x; p < kBT; p += blockDim.x) {
+    const int t = min(t0 + p, ntarget - 1);
+    if (KIND == 0) {
+      Tp[p] = G.cen[a.touch_elem[t]];
+    } else {
+      const int i = a.pair_elem[t];
+      Tp[p] = G.va[i];
+      Tg[p] = G.eg[i];
+      To[p] = a.pair_corner[t];
+    }
+  }
+  const int p_acc = threadIdx.x / (NR / 2), r_acc = 2 * (threadIdx.x % (NR / 2));
+  R ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
   const R k = (R)a.k;
-  for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-    const double4 va = G.va[j];
-    const ElemGeo<R> g = G.eg[j];
-    cplx<R> xv[NR];
-#pragma unroll
-    for (int r = 0; r < NR; r++) xv[r] = r < a.nr ? ld_c<R>(a.x + (size_t)r * G.ne + j) : cplx<R>();
-#pragma unroll
-    for (int p = 0; p < kMTile; p++) {
-      const cplx<R> d = dM_target<R>(k, (R)(C[p].x - va.x), (R)(C[p].y - va.y), (R)(C[p].z - va.z), g);
-#pragma unroll
-      for (int r = 0; r < NR; r++) {
-        ar[p][r] += d.re * xv[r].re - d.im * xv[r].im;
-        ai[p][r] += d.re * xv[r].im + d.im * xv[r].re;
+  for (int jt = j0; jt < j1; jt += kBJ) {
+    __syncthreads();  // the previous tile is consumed (and the targets are staged)
+    for (int e = threadIdx.x; e < kBT * kBJ; e += blockDim.x) {
+      const int p = e / kBJ, jj = e - p * kBJ, j = jt + jj;
+      cplx<R> d;
+      if (j < j1) {
+        if (KIND == 0) {
+          const double4 va = G.va[j];
+          const ElemGeo<R> g = G.eg[j];
+          d = dM_target<R>(k, (R)(Tp[p].x - va.x), (R)(Tp[p].y - va.y), (R)(Tp[p].z - va.z), g);
+        } else {
+          const double4 c = G.cen[j];
+          d = dM_source<R>(k, (R)(c.x - Tp[p].x), (R)(c.y - Tp[p].y), (R)(c.z - Tp[p].z), Tg[p], To[p]);
+        }
       }
+      Dt[p][jj] = d;
+    }
+    for (int e = threadIdx.x; e < kBJ * NR; e += blockDim.x) {
+      const int jj = e / NR, r = e - jj * NR, j = jt + jj;
+      Vt[jj][r] = (j < j1 && r < a.nr) ? ld_c<R>(vec + (size_t)r * G.ne + j) : cplx<R>();
+    }
+    __syncthreads();
+    const int nj = min(kBJ, j1 - jt);
+    for (int jj = 0; jj < nj; jj++) {
+      const cplx<R> d = Dt[p_acc][jj], v0 = Vt[jj][r_acc], v1 = Vt[jj][r_acc + 1];
+      ar0 += d.re * v0.re - d.im * v0.im;
+      ai0 += d.re * v0.im + d.im * v0.re;
+      ar1 += d.re * v1.re - d.im * v1.im;
+      ai1 += d.re * v1.im + d.im * v1.re;
     }
   }
-  double accd[2 * kMTile * NR];
-#pragma unroll
-  for (int p = 0; p < kMTile; p++)
-#pragma unroll
-    for (int r = 0; r < NR; r++) {
-      accd[2 * (p * NR + r)] = (double)ar[p][r];
-      accd[2 * (p * NR + r) + 1] = (double)ai[p][r];
-    }
-  multi_store<NR>(accd, t0, a.ntouch, split, S, part, sd);
-}
-
-// s2 for every direction: sum_j lmb_r[j] dM(c_j, tri_i)/dq_{o,y} over the incidences (i, o)
-template <typename R, int NR>
-__global__ void __launch_bounds__(kAdjThreads) derB_s2_multi_kernel(GeoView<R> G, AdjointMultiArgs a, cd* part,
-                                                                    int S) {
-  __shared__ double sd[kAdjWarps][2 * kMTile * NR];
-  const int t0 = blockIdx.x * kMTile, split = blockIdx.y;
-  const int per = (G.ne + S - 1) / S;
-  const int j0 = split * per, j1 = min(G.ne, j0 + per);
-  double4 A[kMTile];
-  ElemGeo<R> Eg[kMTile];
-  int O[kMTile];
-  for (int p = 0; p < kMTile; p++) {
-    const int t = min(t0 + p, a.npairs - 1);
-    const int i = a.pair_elem[t];
-    A[p] = G.va[i];
-    Eg[p] = G.eg[i];
-    O[p] = a.pair_corner[t];
+  if (t0 + p_acc < ntarget) {
+    cd* dst = part + ((size_t)(t0 + p_acc) * NR + r_acc) * S + split;
+    dst[0] = cd((double)ar0, (double)ai0);
+    dst[S] = cd((double)ar1, (double)ai1);
   }
-  R ar[kMTile][NR], ai[kMTile][NR];
-#pragma unroll
-  for (int p = 0; p < kMTile; p++)
-#pragma unroll
-    for (int r = 0; r < NR; r++) ar[p][r] = ai[p][r] = 0;
-  const R k = (R)a.k;
-  for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-    const double4 c = G.cen[j];
-    cplx<R> lv[NR];
-#pragma unroll
-    for (int r = 0; r < NR; r++) lv[r] = r < a.nr ? ld_c<R>(a.lmb + (size_t)r * G.ne + j) : cplx<R>();
-#pragma unroll
-    for (int p = 0; p < kMTile; p++) {
-      const cplx<R> d = dM_source<R>(k, (R)(c.x - A[p].x), (R)(c.y - A[p].y), (R)(c.z - A[p].z), Eg[p], O[p]);
-#pragma unroll
-      for (int r = 0; r < NR; r++) {
-        ar[p][r] += d.re * lv[r].re - d.im * lv[r].im;
-        ai[p][r] += d.re * lv[r].im + d.im * lv[r].re;
-      }
-    }
-  }
-  double accd[2 * kMTile * NR];
-#pragma unroll
-  for (int p = 0; p < kMTile; p++)
-#pragma unroll
-    for (int r = 0; r < NR; r++) {
-      accd[2 * (p * NR + r)] = (double)ar[p][r];
-      accd[2 * (p * NR + r) + 1] = (double)ai[p][r];
-    }
-  multi_store<NR>(accd, t0, a.npairs, split, S, part, sd);
 }
 
 // Per vertex h: sum over its incidences (CSR order), then over the directions, of
@@ -423,7 +384,7 @@ __global__ void adj_combine_multi_kernel(AdjointMultiArgs a, const double4* __re
 template <typename R, int NR>
 static void adjoint_multi_t(const DevGeometry& G, const AdjointMultiArgs& a, DevBuf& scratch, cudaStream_t s) {
   const int sms = device_sm_count();
-  const int tiles1 = (a.ntouch + kMTile - 1) / kMTile, tiles2 = (a.npairs + kMTile - 1) / kMTile;
+  const int tiles1 = (a.ntouch + kBT - 1) / kBT, tiles2 = (a.npairs + kBT - 1) / kBT;
   auto pick = [&](int tiles) { return std::max(1, std::min(256, (sms * 8 + tiles - 1) / std::max(1, tiles))); };
   const int S1 = pick(tiles1), S2 = pick(tiles2);
   const size_t bytesA = ((size_t)a.npairs * NR * sizeof(double) + 15) / 16 * 16;
@@ -438,10 +399,10 @@ static void adjoint_multi_t(const DevGeometry& G, const AdjointMultiArgs& a, Dev
   derA_multi_kernel<R, NR><<<(a.npairs * 32 + kAdjThreads - 1) / kAdjThreads, kAdjThreads, 0, s>>>(gv, a, outA);
   AC3D_CUDA(cudaGetLastError());
   note_launch();
-  derB_s1_multi_kernel<R, NR><<<dim3(tiles1, S1), kAdjThreads, 0, s>>>(gv, a, s1, S1);
+  derB_tiled_kernel<R, NR, 0><<<dim3(tiles1, S1), kAdjThreads, 0, s>>>(gv, a, s1, S1);
   AC3D_CUDA(cudaGetLastError());
   note_launch();
-  derB_s2_multi_kernel<R, NR><<<dim3(tiles2, S2), kAdjThreads, 0, s>>>(gv, a, s2, S2);
+  derB_tiled_kernel<R, NR, 1><<<dim3(tiles2, S2), kAdjThreads, 0, s>>>(gv, a, s2, S2);
   AC3D_CUDA(cudaGetLastError());
   note_launch();
   adj_combine_multi_kernel<NR><<<(a.HH + 127) / 128, 128, 0, s>>>(a, G.cen.as<double4>(), outA, s1, s2, S1, S2, G.ne);
@@ -451,16 +412,10 @@ static void adjoint_multi_t(const DevGeometry& G, const AdjointMultiArgs& a, Dev
 void launch_adjoint_terms_multi(const DevGeometry& G, const AdjointMultiArgs& a, DevBuf& scratch, cudaStream_t s) {
   if (a.npairs == 0 || a.HH == 0 || a.nr <= 0) return;
   if (a.nr > kAdjMaxRhs) throw Error(3, "internal: too many directions in one adjoint batch");
-  if (a.prec == PREC_FP64) {
-    if (a.nr > 8) throw Error(3, "internal: FP64 adjoint batches hold at most 8 directions");
-    adjoint_multi_t<double, 8>(G, a, scratch, s);
-  } else if (a.nr <= 4) {
-    adjoint_multi_t<float, 4>(G, a, scratch, s);
-  } else if (a.nr <= 8) {
-    adjoint_multi_t<float, 8>(G, a, scratch, s);
-  } else {
-    adjoint_multi_t<float, 16>(G, a, scratch, s);
-  }
+  if (a.prec == PREC_FP64)
+    adjoint_multi_t<double, kAdjMaxRhs>(G, a, scratch, s);
+  else
+    adjoint_multi_t<float, kAdjMaxRhs>(G, a, scratch, s);
 }
 
 void launch_adjoint_terms(const DevGeometry& G, const AdjointArgs& a, DevBuf& scratch, cudaStream_t s) {

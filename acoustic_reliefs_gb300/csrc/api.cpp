@@ -1133,7 +1133,7 @@ double multi_eval(ac3d_ctx* c, const std::vector<double>& freqs, const std::vect
     solve_all(ADJ.as<cd>(), LMB.as<cd>(), *H, true);
     H.reset();
     // shape-derivative terms, all directions of a batch per derivative evaluation
-    const int batch = fp64 ? 8 : kAdjMaxRhs;
+    const int batch = kAdjMaxRhs;
     for (int start = 0; start < D; start += batch) {
       AdjointMultiArgs a{};
       a.prec = c->prec;
