@@ -757,6 +757,21 @@ MultiBufs block_bufs(ac3d_ctx* c, DevHMat& H, int nrb, BlockWork& W, bool tr) {
   prepare_multi_kernels();
   if (tr) ensure_near_transposed(c->m->DP, H, s);
   const int n = c->m->Ne, nleaf = c->m->DP.nleaf;
+  if (c->block_tc && nrb >= 8 && c->m->DP.max_leaf <= 32 && !(tr ? H.tcseg_f.p : H.tcseg_t.p)) {
+    // byte offsets of the split dot-pass segments: V by column leaf (A), U by row leaf (A^T)
+    const Partition& P = c->m->P;
+    const std::vector<int>& ptr = tr ? P.fw_lr_ptr : P.tr_lr_ptr;
+    const std::vector<int>& items = tr ? P.fw_lr : P.tr_lr;
+    std::vector<long long> off(nleaf + 1, 0);
+    for (int l = 0; l < nleaf; l++) {
+      int K = 0;
+      for (int it = ptr[l]; it < ptr[l + 1]; it++) K += H.ranks_host[items[it]];
+      K += K & 1;
+      off[l + 1] = off[l] + tc_segment_bytes(P.leaf_start[l + 1] - P.leaf_start[l], K);
+    }
+    build_tc_segments(c->m->DP, H, tr, off, s);
+    c->stats.hmat_bytes = (long long)H.bytes();  // the split segments are part of the H-matrix's footprint
+  }
   const size_t blk32 = (size_t)n * nrb * sizeof(cf);
   W.kv.ensure(8 * blk32, s);
   MultiBufs B;

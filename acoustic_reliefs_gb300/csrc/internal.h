@@ -190,6 +190,8 @@ struct DevHMat {
   int maxk = 100;
   DevBuf near;            // complex storage of all near blocks
   DevBuf nearT;           // transposed near field (FP32; built on the first transposed block matvec)
+  DevBuf tcseg_f, tcseg_t;  // TF32 hi / lo split of the U / V segments (tensor-core block dot pass)
+  DevBuf tcoff_f, tcoff_t;  // int64 [nleaf + 1]: byte offsets into tcseg_f / tcseg_t
   DevBuf pool;            // rank-1 terms (u | v) of all admissible blocks
   DevBuf term_off;        // int64 [na * maxk] offset of each term in the pool
   DevBuf rank;            // int [na]
@@ -218,7 +220,7 @@ struct DevHMat {
   int64_t lr_entries = 0; // sum r (m + n)
   int64_t aca_evaluated = 0;  // entries ACA evaluated: sum passes (m + n)
   size_t bytes() const {
-    return near.bytes + nearT.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
+    return near.bytes + nearT.bytes + tcseg_f.bytes + tcseg_t.bytes + tcoff_f.bytes + tcoff_t.bytes + pool.bytes + term_off.bytes + rank.bytes + t_off.bytes + task_b.bytes + task_off.bytes +
            tvec.bytes + tvec64.bytes + useg.bytes + vseg.bytes + uidx.bytes + vidx.bytes + kpos_f.bytes +
            kpos_t.bytes + pbuf.bytes + kseg_f.bytes + kseg_t.bytes + seg_f.bytes + seg_t.bytes + xdf.bytes;
   }

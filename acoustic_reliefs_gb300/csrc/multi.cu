@@ -151,44 +151,97 @@ __global__ void __launch_bounds__(kMT) mseg_dot_kernel(SegView V, const cf* __re
 // ------------------------------------------------------------------------------------------
 // Dot pass on the tensor cores (tcgen05; nrb = 8 or 16, leaves of at most 32 rows). For a leaf
 // with R rows and K segment columns, P (K x nrb complex) = S^T X_leaf is the real product
-// D (K x 2 nrb) = A (K x 2R) B (2R x 2 nrb), where row k of A is segment column k exactly as
-// stored (re, im interleaved, 2R floats) and B interleaves X by row: row 2r = (Xr_r | Xi_r),
-// row 2r + 1 = (-Xi_r | Xr_r); columns 0..nrb-1 of D are Re P, nrb..2nrb-1 Im P. Tiles of 128
-// segment columns (M = 128), N = 2 nrb, K = 2R rounded up to 8. Operands are TF32, each FP32
-// value split as hi + lo, product hi hi + hi lo + lo hi (three MMAs), FP32 accumulation in
-// tensor memory. The stages of the copy ring are repacked into the canonical K-major layout
-// (8-row x 16-byte core matrices) with core matrices 144 bytes apart along K, so that eight
-// consecutive 16-byte stores of one row land in eight different bank groups.
+// D (K x 2 nrb) = A (K x 2R) B (2R x 2 nrb), where row k of A is segment column k (re, im
+// interleaved, 2R floats) and B interleaves X by row: row 2r = (Xr_r | Xi_r), row 2r + 1 =
+// (-Xi_r | Xr_r); columns 0..nrb-1 of D are Re P, nrb..2nrb-1 Im P. Operands are TF32 with every
+// FP32 value split as hi + lo, and the product hi hi + hi lo + lo hi takes two MMAs per K step:
+// A_hi [B_hi | B_lo] (N = 4 nrb; the two halves are summed when D is read back) and A_lo B_hi
+// accumulated onto the first half. Tiles of 128 segment columns (M = 128), K = 2R rounded up to
+// 8 (Kd), FP32 accumulation in tensor memory.
+//
+// The segments are split once per H-matrix (tc_split_kernel) into their hi and lo parts, stored
+// tile by tile in the canonical K-major layout the MMA reads: 8-row x 16-byte core matrices,
+// adjacent along K, 8-row groups Kd / 4 core matrices apart; a tile's lo part follows its hi
+// part, and only the leaf's last tile is shorter than 128 rows (rounded up to 8). The pass is
+// then a pipeline without repacking, in three warp roles: warp 0 bulk-copies tile pairs into a
+// ring of stages, warp 1 issues the MMAs of each landed tile into one of two accumulators, and
+// warps 4..7 (tensor-memory lanes 0..127) read finished accumulators back into P. The roles meet
+// only on mbarriers; every wait is bounded, and a role that gives up records the failure so the
+// others stop at their next wait.
 // ------------------------------------------------------------------------------------------
 constexpr int kTcM = 128;
-constexpr int kTcLbo = 144;  // bytes between core matrices along K
 constexpr int kTcKmax = 64;  // 2R for leaves of up to 32 rows
-constexpr size_t kTcTileBytes = (size_t)(kTcM / 8) * (kTcKmax / 4) * kTcLbo;  // one A operand (hi or lo)
+constexpr int kTcStages = 3;
+constexpr size_t kTcStageBytes = 2ull * kTcM * kTcKmax * sizeof(float);  // largest tile pair
 
-__device__ __forceinline__ int tc_off_bytes(int row, int kq, int kq_n) {
-  return (row >> 3) * (kq_n * kTcLbo) + kq * kTcLbo + (row & 7) * 16;
+__host__ __device__ constexpr int tc_tile_off(int row, int kq, int kq_n) {
+  return (row >> 3) * (kq_n * 128) + kq * 128 + (row & 7) * 16;
+}
+
+// B operand: 4 nrb rows (hi parts, then lo parts) of up to kTcKmax values
+template <int NRB>
+__host__ __device__ constexpr size_t tc_b_bytes() {
+  return (size_t)(4 * NRB) * kTcKmax * sizeof(float);
 }
 
 template <int NRB>
 constexpr size_t tc_dot_smem() {
-  return 2 * kTcTileBytes + 2 * (size_t)(2 * NRB / 8) * (kTcKmax / 4) * kTcLbo + (size_t)kStages * kStageBytes;
+  return tc_b_bytes<NRB>() + (size_t)kTcStages * kTcStageBytes;
+}
+
+// Bytes of a leaf's split segment: hi and lo parts of ceil8(K) rows of Kd floats.
+__host__ __device__ constexpr long long tc_leaf_bytes(int R, int K) {
+  return 8ll * ((2 * R + 7) & ~7) * ((K + 7) & ~7);
+}
+
+// One CTA per leaf: the leaf's segment (R x K column-major complex) into split TF32 tiles.
+__global__ void tc_split_kernel(const cf* __restrict__ seg, const long long* __restrict__ seg_off,
+                                const int* __restrict__ kseg, const int* __restrict__ leaf_start,
+                                const long long* __restrict__ tc_off, unsigned char* __restrict__ tc) {
+  const int l = blockIdx.x;
+  const int R = leaf_start[l + 1] - leaf_start[l], K = kseg[l + 1] - kseg[l];
+  const int Kd = (2 * R + 7) & ~7, kq_n = Kd / 4;
+  const float* S = reinterpret_cast<const float*>(seg + seg_off[l]);
+  unsigned char* dst = tc + tc_off[l];
+  for (int t = 0; t * kTcM < K; t++) {
+    const int rows = min(kTcM, K - t * kTcM), g8 = (rows + 7) & ~7;
+    unsigned char* hi_base = dst + (size_t)t * 2 * kTcM * Kd * sizeof(float);
+    unsigned char* lo_base = hi_base + (size_t)g8 * Kd * sizeof(float);
+    for (int e = threadIdx.x; e < g8 * kq_n; e += blockDim.x) {
+      const int rr = e % g8, kq = e / g8;
+      const int k = t * kTcM + rr;
+      float v[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int kk = 4 * kq + q;
+        v[q] = rr < rows && kk < 2 * R ? S[(size_t)k * 2 * R + kk] : 0.f;
+      }
+      float4 hi, lo;
+      split_tf32(v[0], hi.x, lo.x);
+      split_tf32(v[1], hi.y, lo.y);
+      split_tf32(v[2], hi.z, lo.z);
+      split_tf32(v[3], hi.w, lo.w);
+      const int o = tc_tile_off(rr, kq, kq_n);
+      *reinterpret_cast<float4*>(hi_base + o) = hi;
+      *reinterpret_cast<float4*>(lo_base + o) = lo;
+    }
+  }
 }
 
 template <int NRB>
-__global__ void __launch_bounds__(kMT, 1) mseg_dot_tc_kernel(SegView V, const cf* __restrict__ seg,
+__global__ void __launch_bounds__(kMT, 1) mseg_dot_tc_kernel(SegView V, const unsigned char* __restrict__ tcs,
+                                                             const long long* __restrict__ tc_off,
                                                              const cf* __restrict__ X, cf* __restrict__ P,
                                                              const int* __restrict__ done) {
-  constexpr int N = 2 * NRB;
-  constexpr size_t kB = (size_t)(N / 8) * (kTcKmax / 4) * kTcLbo;
+  constexpr int N = 2 * NRB;  // columns of D
+  constexpr int NT = 2 * N;   // accumulator columns in tensor memory (hi | lo halves)
+  static_assert(NT == 32 || NT == 64, "nrb 8 or 16");
   extern __shared__ __align__(128) unsigned char dsmem[];
-  unsigned char* Ah = dsmem;
-  unsigned char* Al = Ah + kTcTileBytes;
-  unsigned char* Bh = Al + kTcTileBytes;
-  unsigned char* Bl = Bh + kB;
-  auto stage = reinterpret_cast<unsigned char(*)[kStageBytes]>(Bl + kB);
-  __shared__ __align__(8) uint64_t full[kStages];
-  __shared__ __align__(8) uint64_t mma_bar;
+  unsigned char* Bt = dsmem;
+  unsigned char* ring = dsmem + tc_b_bytes<NRB>();
+  __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], accf[2], acce[2];
   __shared__ uint32_t s_tmem;
+  __shared__ int s_fail, s_issued, s_consumed;
   if (done && *done) return;
   const int leaf = V.order[blockIdx.x];
   const int ls = V.leaf_start[leaf], R = V.leaf_start[leaf + 1] - ls;
@@ -196,9 +249,11 @@ __global__ void __launch_bounds__(kMT, 1) mseg_dot_tc_kernel(SegView V, const cf
   if (K == 0 || R > kTcKmax / 2) return;  // the host launches this pass only for leaves of <= 32 rows
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int Kd = (2 * R + 7) & ~7, kq_n = Kd / 4;
-  // B operand, N x Kd K-major
+  const int ntiles = (K + kTcM - 1) / kTcM;
+  const unsigned char* src = tcs + tc_off[leaf];
+  // B operand, 2N x Kd K-major: rows n < N the hi parts, N + n the lo parts
   for (int e = tid; e < N * kq_n; e += blockDim.x) {
-    const int n = e / kq_n, kq = e - n * kq_n, jj = n % NRB;
+    const int n = e % N, kq = e / N, jj = n % NRB;
     float v[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -214,104 +269,120 @@ __global__ void __launch_bounds__(kMT, 1) mseg_dot_tc_kernel(SegView V, const cf
     split_tf32(v[1], hi.y, lo.y);
     split_tf32(v[2], hi.z, lo.z);
     split_tf32(v[3], hi.w, lo.w);
-    *reinterpret_cast<float4*>(Bh + tc_off_bytes(n, kq, kq_n)) = hi;
-    *reinterpret_cast<float4*>(Bl + tc_off_bytes(n, kq, kq_n)) = lo;
+    *reinterpret_cast<float4*>(Bt + tc_tile_off(n, kq, kq_n)) = hi;
+    *reinterpret_cast<float4*>(Bt + tc_tile_off(N + n, kq, kq_n)) = lo;
   }
-  if (tid == 0) mbar_init(&mma_bar, 1);
+  if (tid == 0) {
+    for (int s = 0; s < kTcStages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 128);
+    }
+    s_fail = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    fence_barrier_init();
+  }
   if (warp == 0) {
-    tmem_alloc(&s_tmem, 32);
+    tmem_alloc(&s_tmem, 2 * NT);
     tmem_relinquish();
   }
-  tc_fence_before();
-  init_ring(full);  // fences the mbarrier inits and synchronises the CTA
-  tc_fence_after();
-  const uint32_t tmem = s_tmem;
-  const uint32_t idesc = umma_idesc_tf32(kTcM, N);
-  const uint32_t sbo = (uint32_t)(kq_n * kTcLbo);
-  int fill = 0, tile_k = 0;
-  uint32_t phase = 0;
-  bool mma_ok = true;
-  cf* out = P + (size_t)k0 * NRB;
-  // MMA of the current A tile, then rows 0..nrows-1 of D to P
-  auto flush = [&](int nrows) {
-    fence_proxy_async();  // the operand stores become visible to the tensor core
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (tid == 0) {
-      for (int ks = 0; ks < Kd / 8; ks++) {
-        const uint32_t o = (uint32_t)ks * 2u * kTcLbo;
-        const uint64_t ah = umma_smem_desc(Ah + o, kTcLbo, sbo), al = umma_smem_desc(Al + o, kTcLbo, sbo);
-        const uint64_t bh = umma_smem_desc(Bh + o, kTcLbo, sbo), bl = umma_smem_desc(Bl + o, kTcLbo, sbo);
-        umma_tf32(tmem, ah, bh, idesc, ks > 0 ? 1u : 0u);
-        umma_tf32(tmem, ah, bl, idesc, 1u);
-        umma_tf32(tmem, al, bh, idesc, 1u);
-      }
-      umma_commit(&mma_bar);
-    }
-    // one verdict for the whole CTA (the barriers below must not diverge)
-    const bool got = !__syncthreads_or(!mbar_wait_bounded(&mma_bar, phase));
-    phase ^= 1u;
-    if (!got) {
-      mma_ok = false;
-      if (tid == 0) atomicExch(V.err, 1);
-    }
-    tc_fence_after();
-    if (warp < 4 && got) {
-      float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), v);
-      const int row = warp * 32 + lane;
-      if (row < nrows) {
-        cf* o = out + (size_t)(tile_k + row) * NRB;
-#pragma unroll
-        for (int j = 0; j < NRB; j++) o[j] = cf(v[j], v[NRB + j]);
-      }
-    }
-    tc_fence_before();
-    __syncthreads();
-  };
-  stream_leaf<float>(stage, full, R, nullptr, 0, seg + V.b_seg[leaf], K, V.err,
-                     [&](const cf* S, int, int, int ncols, int, int, int nncols) {
-                       int c = 0;
-                       while (c < ncols && mma_ok) {
-                         const int take = min(ncols - c, kTcM - fill);
-                         const float* src = reinterpret_cast<const float*>(S + (size_t)c * R);
-                         for (int e = tid; e < take * kq_n; e += blockDim.x) {
-                           const int rr = e / kq_n, kq = e - rr * kq_n;
-                           const float* rowp = src + (size_t)rr * 2 * R;
-                           float v[4];
-#pragma unroll
-                           for (int q = 0; q < 4; q++) {
-                             const int kk = 4 * kq + q;
-                             v[q] = kk < 2 * R ? rowp[kk] : 0.f;
-                           }
-                           float4 hi, lo;
-                           split_tf32(v[0], hi.x, lo.x);
-                           split_tf32(v[1], hi.y, lo.y);
-                           split_tf32(v[2], hi.z, lo.z);
-                           split_tf32(v[3], hi.w, lo.w);
-                           const int ob = tc_off_bytes(fill + rr, kq, kq_n);
-                           *reinterpret_cast<float4*>(Ah + ob) = hi;
-                           *reinterpret_cast<float4*>(Al + ob) = lo;
-                         }
-                         fill += take;
-                         c += take;
-                         if (fill == kTcM) {
-                           flush(kTcM);
-                           tile_k += kTcM;
-                           fill = 0;
-                         }
-                       }
-                       if (nncols == 0 && fill > 0 && mma_ok) {  // the leaf's last chunk
-                         flush(fill);
-                         tile_k += fill;
-                         fill = 0;
-                       }
-                     });
+  fence_proxy_async();  // the B stores become visible to the tensor core
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) tmem_dealloc(tmem, 32);
+  const uint32_t tmem = s_tmem;
+  const uint32_t sbo = (uint32_t)(kq_n * 128);
+  volatile int* fail = &s_fail;
+  auto give_up = [&]() {
+    *fail = 1;
+    atomicExch(V.err, 1);
+  };
+  if (warp == 0) {
+    if (lane == 0) {  // producer
+      int t = 0;
+      for (; t < ntiles && !*fail; t++) {
+        const int s = t % kTcStages;
+        if (t >= kTcStages && !mbar_wait_bounded(&empty[s], (uint32_t)(t / kTcStages - 1) & 1u)) {
+          give_up();
+          break;
+        }
+        const int rows = min(kTcM, K - t * kTcM), g8 = (rows + 7) & ~7;
+        const uint32_t bytes = 8u * (uint32_t)(g8 * Kd);
+        mbar_expect_tx(&full[s], bytes);
+        bulk_copy_g2s(ring + (size_t)s * kTcStageBytes, src + (size_t)t * 2 * kTcM * Kd * sizeof(float), bytes,
+                      &full[s]);
+      }
+      s_issued = t;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idw = umma_idesc_tf32(kTcM, NT), idn = umma_idesc_tf32(kTcM, N);
+      int t = 0;
+      for (; t < ntiles && !*fail; t++) {
+        const int s = t % kTcStages, b = t & 1;
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(t / kTcStages) & 1u) ||
+            (t >= 2 && !mbar_wait_bounded(&acce[b], (uint32_t)((t >> 1) - 1) & 1u))) {
+          give_up();
+          break;
+        }
+        tc_fence_after();
+        const int rows = min(kTcM, K - t * kTcM), g8 = (rows + 7) & ~7;
+        const unsigned char* Ah = ring + (size_t)s * kTcStageBytes;
+        const unsigned char* Al = Ah + (size_t)4 * g8 * Kd;
+        const uint32_t d = tmem + (uint32_t)(b * NT);
+        for (int ks = 0; ks < Kd / 8; ks++) {
+          const uint32_t o = (uint32_t)ks * 256u;
+          const uint64_t bd = umma_smem_desc(Bt + o, 128, sbo);
+          umma_tf32(d, umma_smem_desc(Ah + o, 128, sbo), bd, idw, ks > 0 ? 1u : 0u);
+          umma_tf32(d, umma_smem_desc(Al + o, 128, sbo), bd, idn, 1u);
+        }
+        umma_commit(&empty[s]);
+        umma_commit(&accf[b]);
+      }
+      s_consumed = t;
+    }
+  } else if (warp >= 4) {  // accumulator read-back: warp 4 + w reads tensor-memory lanes 32 w ..
+    const int ew = warp - 4;
+    cf* out = P + (size_t)k0 * NRB;
+    for (int t = 0; t < ntiles; t++) {
+      const int b = t & 1;
+      int got = 1;
+      if (lane == 0) got = !*fail && mbar_wait_bounded(&accf[b], (uint32_t)(t >> 1) & 1u);
+      if (!__shfl_sync(0xffffffffu, got, 0)) {
+        if (lane == 0 && !*fail) give_up();
+        break;
+      }
+      tc_fence_after();
+      const uint32_t ta = tmem + ((uint32_t)(ew * 32) << 16) + (uint32_t)(b * NT);
+      float v[64];
+      tmem_ld32(ta, *reinterpret_cast<float(*)[32]>(v));
+      if constexpr (NT == 64) tmem_ld32(ta + 32, *reinterpret_cast<float(*)[32]>(v + 32));
+      const int row = ew * 32 + lane, rows = min(kTcM, K - t * kTcM);
+      if (row < rows) {
+        float4* o = reinterpret_cast<float4*>(out + (size_t)(t * kTcM + row) * NRB);
+#pragma unroll
+        for (int j = 0; j < NRB; j += 2)
+          o[j / 2] = make_float4(v[j] + v[N + j], v[NRB + j] + v[N + NRB + j], v[j + 1] + v[N + j + 1],
+                                 v[NRB + j + 1] + v[N + NRB + j + 1]);
+      }
+      tc_fence_before();
+      mbar_arrive(&acce[b]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && s_fail) {
+    // after a failure: let the copies that were issued but not consumed land before the CTA exits
+    for (int t = s_consumed; t < s_issued; t++)
+      mbar_wait_bounded(&full[t % kTcStages], (uint32_t)(t / kTcStages) & 1u);
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, 2 * NT);
 }
 
 // T[task][j] = sum over the task's block entries of P[kpos[e] + q][j], in leaf order.
@@ -461,8 +532,7 @@ __global__ void __launch_bounds__(kMT) mseg_gather_kernel(SegView V, const cf* _
   int c = 0;
   for (; c < nch; c++) {
     const int s = c % kStages;
-    const bool got = mbar_wait_bounded(&full[s], (uint32_t)(c / kStages) & 1u);
-    if (__syncthreads_or(!got)) {
+    if (!cta_wait(&full[s], (uint32_t)(c / kStages) & 1u)) {
       ok = false;
       break;
     }
@@ -869,10 +939,16 @@ static void mmv_t(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, 
     d.b_kptr = tr ? H.kseg_f.as<int>() : H.kseg_t.as<int>();
     d.order = tr ? H.order_rows.as<int>() : H.order_cols.as<int>();
     note_launch();
-    if (NRB >= 8 && RPL == 1 && B.tc)
-      mseg_dot_tc_kernel<NRB><<<DP.nleaf, kMT, tc_dot_smem<NRB>(), s>>>(d, tr ? H.useg.as<cf>() : H.vseg.as<cf>(),
-                                                                      (const cf*)x, P, done);
-    else
+    bool launched = false;
+    if constexpr (NRB >= 8 && RPL == 1) {
+      const DevBuf& tcs = tr ? H.tcseg_f : H.tcseg_t;
+      if (B.tc && tcs.p) {
+        mseg_dot_tc_kernel<NRB><<<DP.nleaf, kMT, tc_dot_smem<NRB>(), s>>>(
+            d, tcs.as<unsigned char>(), (tr ? H.tcoff_f : H.tcoff_t).as<long long>(), (const cf*)x, P, done);
+        launched = true;
+      }
+    }
+    if (!launched)
       mseg_dot_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(d, tr ? H.useg.as<cf>() : H.vseg.as<cf>(),
                                                                (const cf*)x, P, done);
     AC3D_CUDA(cudaGetLastError());
@@ -890,10 +966,13 @@ static void mmv_t(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, 
   v.order = tr ? H.order_cols.as<int>() : H.order_rows.as<int>();
   const bool dots = dot_a || dot_b;
   note_launch();
-  mseg_gather_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(
-      v, tr ? H.nearT.as<cf>() : H.near.as<cf>(), tr ? H.vseg.as<cf>() : H.useg.as<cf>(), T, (const cf*)x, (cf*)y,
-      (const cf*)dot_a, (const cf*)dot_b,
-      dots ? B.partials : nullptr, B.partials + (size_t)std::max(DP.nleaf, 1184) * 5 * NRB, B.ticket, B.red, done);
+  const cf* g_near = tr ? H.nearT.as<cf>() : H.near.as<cf>();
+  const cf* g_lr = tr ? H.vseg.as<cf>() : H.useg.as<cf>();
+  double* g_part = dots ? B.partials : nullptr;
+  double* g_gpart = B.partials + (size_t)std::max(DP.nleaf, 1184) * 5 * NRB;
+  mseg_gather_kernel<NRB, RPL><<<DP.nleaf, kMT, kMRing, s>>>(v, g_near, g_lr, T, (const cf*)x, (cf*)y,
+                                                              (const cf*)dot_a, (const cf*)dot_b, g_part, g_gpart,
+                                                              B.ticket, B.red, done);
   if (DP.nleaf > 1024 * kGroup) throw Error(1, "block solves support at most 32768 leaf clusters");
   AC3D_CUDA(cudaGetLastError());
 }
@@ -936,6 +1015,29 @@ void ensure_near_transposed(const DevPartition& DP, DevHMat& H, cudaStream_t s) 
                                               DP.near_off_t.as<long long>(), H.near.as<cf>(), H.nearT.as<cf>());
   AC3D_CUDA(cudaGetLastError());
 }
+
+void build_tc_segments(const DevPartition& DP, DevHMat& H, bool tr, const std::vector<long long>& off,
+                       cudaStream_t s) {
+  DevBuf& tcs = tr ? H.tcseg_f : H.tcseg_t;
+  DevBuf& tco = tr ? H.tcoff_f : H.tcoff_t;
+  if (tcs.p) return;
+  if (H.prec == PREC_FP64) throw Error(3, "internal: block matvec needs FP32 storage");
+  if ((int)off.size() != DP.nleaf + 1) throw Error(3, "internal: split segment offsets");
+  tco.alloc(off.size() * sizeof(long long), s);
+  // pageable source: the copy is staged before the call returns, so off may go away after it
+  AC3D_CUDA(cudaMemcpyAsync(tco.p, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice, s));
+  tcs.alloc((size_t)std::max<long long>(off.back(), 16), s);
+  if (DP.nleaf == 0) return;
+  note_launch();
+  tc_split_kernel<<<DP.nleaf, 256, 0, s>>>(tr ? H.useg.as<cf>() : H.vseg.as<cf>(),
+                                          (tr ? H.seg_f : H.seg_t).as<long long>(),
+                                          (tr ? H.kseg_f : H.kseg_t).as<int>(), DP.leaf_start.as<int>(),
+                                          tco.as<long long>(), tcs.as<unsigned char>());
+  AC3D_CUDA(cudaGetLastError());
+}
+
+long long tc_segment_bytes(int R, int K) { return tc_leaf_bytes(R, K); }
+
 
 void launch_mmatvec(const DevPartition& DP, const DevHMat& H, const MultiBufs& B, const void* x, void* y,
                     const void* dot_a, const void* dot_b, const int* done, cudaStream_t s) {

@@ -51,6 +51,12 @@ void launch_mmatvec(const DevPartition& DP, const DevHMat& H, const MultiBufs& B
                     const void* dot_a, const void* dot_b, const int* done, cudaStream_t s);
 // Builds H.nearT, the near blocks transposed into the segment layout of A^T (once per H-matrix).
 void ensure_near_transposed(const DevPartition& DP, DevHMat& H, cudaStream_t s);
+// Builds the TF32 hi / lo split of the dot-pass segments (V by column leaf for A, U by row leaf
+// for A^T with tr) that the tensor-core dot pass streams (once per H-matrix and orientation).
+// off: nleaf + 1 byte offsets, off[l + 1] - off[l] = tc_segment_bytes(R_l, K_l).
+void build_tc_segments(const DevPartition& DP, DevHMat& H, bool tr, const std::vector<long long>& off,
+                       cudaStream_t s);
+long long tc_segment_bytes(int R, int K);
 void mkrylov_enqueue_init(const MultiBufs& B, int maxit, cudaStream_t s);
 void mkrylov_enqueue_iterations(const MultiBufs& B, const DevPartition& DP, const DevHMat& H, int count,
                                 cudaStream_t s);

@@ -93,6 +93,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// CTA-wide bounded wait: thread 0 polls the mbarrier while the other threads wait at the CTA
+// barrier, which costs them no issue slots; every thread gets the same verdict. The barrier
+// orders what the completed phase covers (bulk copies, cp.async arrivals, MMA completion) before
+// every thread's later accesses.
+__device__ __forceinline__ bool cta_wait(uint64_t* bar, uint32_t parity) {
+  bool got = true;
+  if (threadIdx.x == 0) got = mbar_wait_bounded(bar, parity);
+  return !__syncthreads_or(!got);
+}
+
 // ------------------------------------------------------------------------------------------
 // Per-leaf segment views and the copy ring shared by the matvec passes
 // ------------------------------------------------------------------------------------------
@@ -162,8 +172,7 @@ __device__ __forceinline__ bool stream_leaf(unsigned char (*stage)[kStageBytes],
   for (; c < nch; c++) {
     const int s = c % kStages;
     const uint32_t parity = (uint32_t)(c / kStages) & 1u;
-    const bool got = mbar_wait_bounded(&full[s], parity);
-    if (__syncthreads_or(!got)) {
+    if (!cta_wait(&full[s], parity)) {
       ok = false;
       break;
     }

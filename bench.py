@@ -215,7 +215,9 @@ def block_c5_leg():
             "near_entries": st["near_entries"], "lr_entries": st["lr_entries"],
             "block_matvec_ms": mv_ms, "block_matvec_bytes": int(mv_bytes), "block_matvec_gbs": gbs,
             "block_matvec_frac_of_hbm": gbs / peak, "block_matvec_ms_cuda_cores": mv_ms_cc,
-            "dot_pass": "tensor cores (tcgen05.mma kind::tf32, hi/lo split, three products, FP32 accumulation in TMEM)",
+            "dot_pass": "tensor cores (tcgen05.mma kind::tf32 from the segments split once into TF32 hi/lo tiles: "
+                        "hi*hi + hi*lo + lo*hi in two MMAs per K step, FP32 accumulation in tensor memory); "
+                        "gather and reduce passes on the CUDA cores",
             "fp64_single_solve_s": dt64,
             "pressure_rel_err_vs_fp64": float(np.linalg.norm(P[0] - y64) / np.linalg.norm(y64))}
 

@@ -52,7 +52,8 @@ typedef struct ac3d_stats {
   long long near_entries, lr_entries; /* stored complex entries */
   double mean_rank;
   int max_rank;
-  long long hmat_bytes;     /* device bytes of the last H-matrix */
+  long long hmat_bytes;     /* device bytes of the last H-matrix (including the split segments of
+                               tensor-core block matvecs once they are built) */
   int solves;               /* linear solves in the call */
   int iterations;           /* Krylov iterations, summed over solves and refinement steps */
   int outer_steps;          /* refinement steps (mixed precision) summed over solves */
@@ -101,9 +102,10 @@ int ac3d_set_krylov(ac3d_ctx* ctx, int method, int restart);
  * rounding of each other). No reference counterpart. */
 int ac3d_set_assembly(ac3d_ctx* ctx, int mode);
 /* Block matvecs of 8 or 16 right-hand sides (ac3d_solve_multi, ac3d_gradient_multi) form their
- * dot pass S^T X on the tensor cores (tcgen05.mma, TF32 operands split in three products, FP32
- * accumulation) when on (default) and leaves have at most 32 elements; off: FP32 CUDA cores.
- * No reference counterpart. */
+ * dot pass S^T X on the tensor cores (tcgen05.mma, TF32 operands split so that three products
+ * keep FP32 accuracy, FP32 accumulation) when on (default) and leaves have at most 32 elements;
+ * off: FP32 CUDA cores. The first such matvec of an H-matrix stores the split segments it
+ * streams (about twice the low-rank V or U storage). No reference counterpart. */
 int ac3d_set_tensor_cores(ac3d_ctx* ctx, int on);
 /* Replace the receivers used by value / values / band_value / gradient (default: the
  * hemisphere of compute_listener_pts, helpers.cpp:52-65). */

@@ -97,3 +97,20 @@ def test_multi_gradient_mixed_vs_fp64(gpu_lib, exact_case):
     g64 = _bem(R, freqs[0], "fp64", factor=1e3, tol=1e-10).gradient_multi(x, freqs, dirs)[1]
     g32 = _bem(R, freqs[0], "mixed", factor=1e3, tol=1e-10).gradient_multi(x, freqs, dirs)[1]
     assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-3
+
+
+
+def test_multi_gradient_tensor_cores(gpu_lib):
+    """The transposed block solves with the tensor-core dot pass give the gradient of the
+    CUDA-core run within 1e-5 relative L2 (every solve to 1e-8)."""
+    R = meshes.relief(0.6, 0.6, 0.05, 16, 4, 16, 0, meshes.smooth_heightmap(64, 1))
+    x = np.random.default_rng(4).uniform(0.0, 0.01, size=len(R.diff_pts))
+    dirs = _dirs(9, 5)
+    out = {}
+    for tc in (True, False):
+        bem = _bem(R, 1200.0, "mixed")
+        bem.set_krylov("gmres")
+        bem.set_tensor_cores(tc)
+        out[tc] = bem.gradient_multi(x, [1200.0], dirs)
+    assert abs(out[True][0] - out[False][0]) < 1e-7
+    assert np.linalg.norm(out[True][1] - out[False][1]) / np.linalg.norm(out[False][1]) < 1e-5

@@ -84,9 +84,9 @@ def test_block_solve_point_sources_and_repeatable(gpu_lib):
 @pytest.mark.gpu
 @pytest.mark.parametrize("nrhs", [6, 16])
 def test_tensor_core_dot_pass_matches_cuda_cores(gpu_lib, nrhs):
-    """The block dot pass on the tensor cores (tcgen05, TF32 split in three products) and on the
-    FP32 CUDA cores solve to the same answers: both runs reach relative residual 1e-8 on the same
-    H-matrix, so their pressures agree to about that level."""
+    """The block dot pass on the tensor cores (tcgen05, TF32 split in three products, from the
+    split segments) and on the FP32 CUDA cores solve to the same answers: both runs reach relative
+    residual 1e-8 on the same H-matrix, so their pressures agree to about that level."""
     c = cases.relief_small()
     rng = np.random.default_rng(3)
     dirs = rng.normal(size=(nrhs, 3))
