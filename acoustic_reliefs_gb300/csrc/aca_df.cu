@@ -12,7 +12,8 @@
 // |u|^2 over unused rows. Entries, residuals, the pivot magnitudes and the norms are double-float,
 // so the pivots and ranks are the FP64 path's (the two differ only where two candidates agree to
 // about 1e-12); the cross terms of the error estimate are FP32 sums of the leading parts (they
-// only scale err). The terms live in a double-float pool while the recursion needs them; packing
+// only scale err). The estimate, the norms and the stopping test are double-float too (the FP64
+// pipes of GB300 are too slow to hold them), the test as |u|^2 |v|^2 <= eps^2 err. The terms live in a double-float pool while the recursion needs them; packing
 // rounds them to the FP32 per-leaf segments the matvec streams.
 #include "common.cuh"
 #include "df64.cuh"
@@ -37,6 +38,7 @@ struct AcaDfArgs {
   const int* order;
   df64 k;
   double eps;
+  df64 eps2;       // eps^2 as a double-float (the stopping test)
   int maxk;
   int iter_cap;
   cdf* pool;
@@ -86,6 +88,28 @@ __device__ __forceinline__ bool zero_block(const AcaDfArgs& A, int rs, int m, in
 
 __device__ __forceinline__ df64 shfl_df(df64 v, int src) {
   return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// Sum over the warp by butterfly; every lane ends with the same value (the double-float add is
+// commutative bit for bit: TwoSum's error term is exact).
+__device__ __forceinline__ df64 warp_sum_df(df64 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = v + df64{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+  return v;
+}
+
+// a * b of two FP32 values, exactly, as a double-float
+__device__ __forceinline__ df64 df_prod_ff(float a, float b) {
+  float p, e;
+  two_prod(a, b, p, e);
+  return {p, e};
+}
+
+// The ACA stopping test of the FP64 path, sqrt(|u|^2 |v|^2 / err) <= eps, as uv <= eps^2 err
+// without a square root or a division; with err = 0 (then uv = 0) the FP64 test sees 0 / 0 and
+// does not stop, and neither does this one.
+__device__ __forceinline__ bool aca_converged(df64 uv, df64 err, df64 eps2) {
+  return !df_is_zero(err) && !(uv > eps2 * err);
 }
 
 // (value, index) argmax over the warp: larger value wins, smaller index on ties
@@ -153,7 +177,7 @@ __global__ void __launch_bounds__(256, LPL == 8 ? 1 : 2) aca_df_warp_kernel(AcaD
   }
 
   unsigned used_l = lane == 0 ? 1u : 0u;  // bit k: row lane + 32 k is used (row 0 first)
-  double err = 0;
+  df64 err{0.0f, 0.0f};
   int i = 0, iter = 0, nst = 0, npass = 0;
   bool need_alloc = true;
   long long base = 0;
@@ -232,8 +256,9 @@ __global__ void __launch_bounds__(256, LPL == 8 ? 1 : 2) aca_df_warp_kernel(AcaD
         un += cdf_abs2(u);
       }
     }
-    // cross terms sum_q |u^T U_q| |v V_q^T| (FP32 on the leading parts)
-    double dots = 0;
+    // cross terms sum_q |u^T U_q| |v V_q^T| (FP32 on the leading parts, exact products summed as
+    // double-floats: all on the FP32 pipes)
+    df64 dots{0.0f, 0.0f};
     for (int p = 0; p < nst; p++) {
       const cdf* Up = A.pool + toff[p];
       const cdf* Vp = Up + m;
@@ -248,12 +273,13 @@ __global__ void __launch_bounds__(256, LPL == 8 ? 1 : 2) aca_df_warp_kernel(AcaD
       udi = warp_sum(udi);
       vdr = warp_sum(vdr);
       vdi = warp_sum(vdi);
-      dots += (double)sqrtf(udr * udr + udi * udi) * (double)sqrtf(vdr * vdr + vdi * vdi);
+      dots += df_prod_ff(sqrtf(udr * udr + udi * udi), sqrtf(vdr * vdr + vdi * vdi));
     }
-    const double unt = warp_sum(df_to_double(un)), vnt = warp_sum(df_to_double(vn));
-    err += unt * vnt + 2 * dots;
-    if (sqrt(unt * vnt / err) <= A.eps) break;
-    const bool zero_term = (unt == 0.0) || (vnt == 0.0);
+    const df64 unt = warp_sum_df(un), vnt = warp_sum_df(vn);
+    const df64 uv = unt * vnt;
+    err += uv + df_ldexp(dots, 2.0f);
+    if (aca_converged(uv, err, A.eps2)) break;
+    const bool zero_term = df_is_zero(unt) || df_is_zero(vnt);
     // next row pivot over unused rows
     best = df64{-1.0f, 0.0f};
     bidx = 0;
@@ -316,20 +342,21 @@ __device__ __forceinline__ void block_argmax_df(df64& val, int& idx, df64* sv, i
   __syncthreads();
 }
 
-__device__ __forceinline__ double block_sum_d(double v, double* sd) {
-  v = warp_sum(v);
+// Sum over the CTA: warp sums, then the warps' sums in order by thread 0; every thread gets it.
+__device__ __forceinline__ df64 block_sum_df(df64 v, df64* sd) {
+  v = warp_sum_df(v);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) sd[w] = v;
   __syncthreads();
-  double s = 0;
   if (threadIdx.x == 0) {
-    for (int k = 0; k < kDfWarps; k++) s += sd[k];
+    df64 s = sd[0];
+    for (int k = 1; k < kDfWarps; k++) s += sd[k];
     sd[0] = s;
   }
   __syncthreads();
-  s = sd[0];
+  v = sd[0];
   __syncthreads();
-  return s;
+  return v;
 }
 
 __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
@@ -337,7 +364,7 @@ __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
   __shared__ float4 s_tab[kDfTab];
   __shared__ df64 s_rv[kDfWarps];
   __shared__ int s_ri[kDfWarps];
-  __shared__ double s_d[kDfWarps];
+  __shared__ df64 s_d[kDfWarps];
   __shared__ long long s_base;
   __shared__ int s_flag;
   load_table(A.tab, s_tab);
@@ -367,7 +394,7 @@ __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
   for (int w = tid; w < (m + 31) / 32; w += T) used[w] = 0;
   __syncthreads();
   if (tid == 0) used[0] = 1u;
-  double err = 0;  // meaningful in thread 0
+  df64 err{0.0f, 0.0f};  // meaningful in thread 0
   int i = 0, iter = 0, nst = 0, npass = 0;
   bool need_alloc = true;
   __syncthreads();
@@ -430,8 +457,9 @@ __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
     }
     __syncthreads();
 
-    // cross terms (one warp per earlier stored term, FP32 on the leading parts)
-    double dots = 0;
+    // cross terms (one warp per earlier stored term, FP32 on the leading parts, exact products
+    // summed as double-floats)
+    df64 dots{0.0f, 0.0f};
     for (int p = warp; p < nst; p += kDfWarps) {
       const cdf* Up = A.pool + toff[p];
       const cdf* Vp = Up + m;
@@ -442,18 +470,19 @@ __global__ void __launch_bounds__(kDfThreads) aca_df_kernel(AcaDfArgs A) {
       udi = warp_sum(udi);
       vdr = warp_sum(vdr);
       vdi = warp_sum(vdi);
-      if (lane == 0) dots += (double)sqrtf(udr * udr + udi * udi) * (double)sqrtf(vdr * vdr + vdi * vdi);
+      if (lane == 0) dots += df_prod_ff(sqrtf(udr * udr + udi * udi), sqrtf(vdr * vdr + vdi * vdi));
     }
-    const double unt = block_sum_d(df_to_double(un), s_d);
-    const double vnt = block_sum_d(df_to_double(vn), s_d);
-    dots = block_sum_d(dots, s_d);
+    const df64 unt = block_sum_df(un, s_d);
+    const df64 vnt = block_sum_df(vn, s_d);
+    dots = block_sum_df(lane == 0 ? dots : df64{0.0f, 0.0f}, s_d);
     if (tid == 0) {
-      err += unt * vnt + 2 * dots;
-      s_flag = (sqrt(unt * vnt / err) <= A.eps) ? 1 : 0;
+      const df64 uv = unt * vnt;
+      err += uv + df_ldexp(dots, 2.0f);
+      s_flag = aca_converged(uv, err, A.eps2) ? 1 : 0;
     }
     __syncthreads();
     if (s_flag) break;
-    const bool zero_term = (unt == 0.0) || (vnt == 0.0);
+    const bool zero_term = df_is_zero(unt) || df_is_zero(vnt);
 
     // next row pivot: first max |u|^2 over unused rows
     best = df64{-1.0f, 0.0f};
@@ -530,7 +559,7 @@ void launch_aca_df(const DevGeometry& G, const DevPartition& DP, DevHMat& H, dou
   if (DP.na == 0) return;
   AcaDfArgs a{G.cen.as<double4>(), G.va.as<double4>(), G.eg64.as<ElemGeo<double>>(), G.cen_df.as<DfPt>(),
               G.el_df.as<DfElem>(), G.df_tab.as<float4>(), DP.blocks_a.as<int4>(), DP.aca_order.as<int>(),
-              df_from_double(H.k), eps, H.maxk, H.maxk, H.pool.as<cdf>(), H.pool_cap,
+              df_from_double(H.k), eps, df_from_double(eps * eps), H.maxk, H.maxk, H.pool.as<cdf>(), H.pool_cap,
               H.pool_used.as<unsigned long long>(), H.term_off.as<long long>(), H.rank.as<int>(),
               (int*)(H.pool_used.as<unsigned long long>() + 1), H.passes.as<int>(), 1};
   // same grouping and stream split as launch_aca: CTA blocks, then warp blocks up to 256 / 128 / 64
@@ -571,7 +600,8 @@ void launch_listener_aca_df(const DevGeometry& G, const void* pts_df, int L, dou
   int iter_lim = std::min(maxk, std::min(L - 1, G.ne - 1));
   if (iter_lim < 1) iter_lim = 1;
   AcaDfArgs a{G.cen.as<double4>(), G.va.as<double4>(), G.eg64.as<ElemGeo<double>>(), (const DfPt*)pts_df,
-              G.el_df.as<DfElem>(), G.df_tab.as<float4>(), block, order, df_from_double(k), eps, maxk, iter_lim,
+              G.el_df.as<DfElem>(), G.df_tab.as<float4>(), block, order, df_from_double(k), eps,
+              df_from_double(eps * eps), maxk, iter_lim,
               (cdf*)pool, pool_cap, used, term_off, rank, status, nullptr, 0};
   const size_t smem = (size_t)iter_lim * (2 * sizeof(cdf) + sizeof(long long)) + (size_t)((L + 31) / 32) * 4;
   if (smem > 200 * 1024) throw Error(4, "receiver ACA too large for shared memory (at most about 5000 receivers)");

@@ -489,6 +489,39 @@ def run_single(args):
     return 0
 
 
+def block_dirs(n):
+    """n seeded plane-wave directions from the upper half space, the first the headline's."""
+    rng = np.random.default_rng(1)
+    dirs = rng.normal(size=(n, 3))
+    dirs[:, 1] = -np.abs(dirs[:, 1]) - 0.5
+    dirs[0] = DIRECTION
+    return dirs / np.linalg.norm(dirs, axis=1, keepdims=True)
+
+
+def run_single_block(args):
+    """One context, one block solve after another (16 directions on the 20k relief at 2 kHz, the
+    multi_rhs leg's workload): the command line for captures of the block-matvec kernels."""
+    from acoustic_reliefs_gb300.acoustics3d import DiffBEM
+    R, Ls = workload(0)
+    bem = DiffBEM(LEAF, FACTOR, [FREQ], 1, ACA_TOL, ACA_TOL, SOLVER_TOL, precision="mixed")
+    bem.silent = True
+    bem.set_krylov(args.krylov, RESTART)
+    bem.set_mesh(R.Ps, R.Es)
+    dirs = block_dirs(max(args.multi_rhs, 1))
+    for _ in range(args.warmup):
+        bem.pvals_multi(FREQ, dirs, Ls)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bem.pvals_multi(FREQ, dirs, Ls)
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    st = bem.stats()
+    mv_ms, mv_bytes = bem.block_matvec_timing(16, 10)
+    print(json.dumps({"mode": "single context, block solves (kernel captures)", "rhs": len(dirs),
+                      "ms_per_block": 1e3 * dt, "iterations": st["iterations"], "block_matvec_ms": mv_ms,
+                      "block_matvec_bytes": int(mv_bytes)}), flush=True)
+    return 0
+
+
 def run_gpu(args):
     import torch
     world, rank, local = dist_init()
@@ -606,11 +639,7 @@ def run_gpu(args):
     # block solve: 16 incidence directions of the same frequency against one H-matrix
     multi = None
     if args.multi_rhs > 0:
-        rng = np.random.default_rng(1)
-        dirs = rng.normal(size=(args.multi_rhs, 3))
-        dirs[:, 1] = -np.abs(dirs[:, 1]) - 0.5
-        dirs[0] = DIRECTION
-        dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+        dirs = block_dirs(args.multi_rhs)
         bem.pvals_multi(FREQ, dirs, Ls)  # warm-up
         reps = 3
         t0 = time.perf_counter()
@@ -712,9 +741,13 @@ def main():
                          "reported beside a GMRES headline)")
     ap.add_argument("--single-context", action="store_true",
                     help="only one context on one stream (no request server): the command for kernel captures")
+    ap.add_argument("--single-block", action="store_true",
+                    help="one context, block solves of --multi-rhs directions: the command for block-kernel captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.single_block:
+        return run_single_block(args)
     if args.single_context:
         return run_single(args)
     return run_gpu(args)
