@@ -23,6 +23,7 @@
 // right-hand side of a block solve) run together and share each block matvec; their inputs and
 // outputs are element-major block vectors (stride nrb).
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "gmres.h"
@@ -37,6 +38,7 @@ namespace {
 constexpr int kGmThreads = 256;
 constexpr int kGmWarps = kGmThreads / 32;
 constexpr int kSliceMax = 1024;  // elements per CTA of the dot and update passes
+constexpr int kGmMaxRestart = 600;  // longest cycle (ac3d_set_krylov accepts up to 600)
 
 struct Dc {  // complex FP64 scalar arithmetic of the small dense part
   double re, im;
@@ -170,17 +172,28 @@ __device__ __forceinline__ void gs_dot_partials(const cplx<VT>* __restrict__ V, 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
     VT ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
-    for (int t = lane; t < len; t += 32) {
-      const cplx<VT> x = xsm[t];
-      cplx<VT> v[4];
+    // four elements per lane per step: sixteen loads in flight before their products, which keep
+    // the element order t, t + 32, t + 64, t + 96
+    for (int t0 = 0; t0 < len; t0 += 128) {
+      cplx<VT> v[4][4];
 #pragma unroll
-      for (int u = 0; u < 4; u++) v[u] = kb + u <= j ? V[(size_t)(kb + u) * n + lo + t] : cplx<VT>();
+      for (int e = 0; e < 4; e++) {
+        const int t = t0 + 32 * e + lane;
 #pragma unroll
-      for (int u = 0; u < 4; u++) {  // conj(v) x
-        ar[u] = fma(v[u].re, x.re, ar[u]);
-        ar[u] = fma(v[u].im, x.im, ar[u]);
-        ai[u] = fma(v[u].re, x.im, ai[u]);
-        ai[u] = fma(-v[u].im, x.re, ai[u]);
+        for (int u = 0; u < 4; u++)
+          v[e][u] = (t < len && kb + u <= j) ? V[(size_t)(kb + u) * n + lo + t] : cplx<VT>();
+      }
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int t = t0 + 32 * e + lane;
+        const cplx<VT> x = t < len ? xsm[t] : cplx<VT>();
+#pragma unroll
+        for (int u = 0; u < 4; u++) {  // conj(v) x
+          ar[u] = fma(v[e][u].re, x.re, ar[u]);
+          ar[u] = fma(v[e][u].im, x.im, ar[u]);
+          ai[u] = fma(v[e][u].re, x.im, ai[u]);
+          ai[u] = fma(-v[e][u].im, x.re, ai[u]);
+        }
       }
     }
 #pragma unroll
@@ -209,13 +222,24 @@ __device__ __forceinline__ void gs_dot_tail(GState* st, double* gd, const GmLayo
     VT a[8];
 #pragma unroll
     for (int u = 0; u < 8; u++) a[u] = 0;
-    for (int c = lane; c < L.G; c += 32)
+    // two partials per lane per step (sixteen loads in flight), summed in CTA order per lane
+    for (int c0 = lane; c0 < L.G; c0 += 64) {
+      double w[2][8];
 #pragma unroll
-      for (int u = 0; u < 4; u++)
-        if (kb + u <= j) {
-          a[2 * u] += (VT)__ldcg(&gd[L.part() + ((size_t)(kb + u) * L.G + c) * 2]);
-          a[2 * u + 1] += (VT)__ldcg(&gd[L.part() + ((size_t)(kb + u) * L.G + c) * 2 + 1]);
+      for (int e = 0; e < 2; e++) {
+        const int c = c0 + 32 * e;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const bool ok = c < L.G && kb + u <= j;
+          w[e][2 * u] = ok ? __ldcg(&gd[L.part() + ((size_t)(kb + u) * L.G + c) * 2]) : 0.0;
+          w[e][2 * u + 1] = ok ? __ldcg(&gd[L.part() + ((size_t)(kb + u) * L.G + c) * 2 + 1]) : 0.0;
         }
+      }
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+#pragma unroll
+        for (int u = 0; u < 8; u++) a[u] += (VT)w[e][u];
+    }
 #pragma unroll
     for (int u = 0; u < 8; u++) a[u] = warp_sum(a[u]);
     if (lane < 4 && kb + lane <= j) {
@@ -370,6 +394,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n
   Dc* hs = reinterpret_cast<Dc*>(gsm);      // h: j + 2 entries (the coefficients are no longer needed)
   Dc* tc = hs + (j + 2);                    // conj(c_i) h_{i+1}: j entries
   Dc* xs = tc + j;                          // chain values x_i: j + 1 entries
+  Dc* ss = xs + (j + 1);                    // conj(s_i): j entries (the chain reads shared memory only)
   __syncthreads();
   if (threadIdx.x < 32) {
     const double u2 = warp_sum_run<VT>(gd + L.npart(), L.G, threadIdx.x);
@@ -384,15 +409,14 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n
   for (int i = threadIdx.x; i < j; i += blockDim.x) {
     const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
     tc[i] = conjd(c) * hs[i + 1];
+    ss[i] = dc(gd[L.sn() + 2 * i], -gd[L.sn() + 2 * i + 1]);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const double* snp = gd + L.sn();
     Dc x = hs[0];
     xs[0] = x;
     for (int i = 0; i < j; i++) {
-      const Dc s = dc(snp[2 * i], -snp[2 * i + 1]);  // conj(s_i)
-      x = tc[i] - s * x;
+      x = tc[i] - ss[i] * x;
       xs[i + 1] = x;
     }
   }
@@ -533,8 +557,8 @@ void gmres_enqueue_init(const GmresBufs& B, double tol, cudaStream_t s) {
 }
 
 size_t gmres_update_smem(int m) {
-  // the update pass keeps j + 1 coefficients, then 3 j + 3 complex FP64 values of the rotation
-  return std::max(sizeof(cplx<double>) * ((size_t)m + 1), sizeof(double) * 2 * (3 * (size_t)m + 3));
+  // the update pass keeps j + 1 coefficients, then 4 j + 3 complex FP64 values of the rotation
+  return std::max(sizeof(cplx<double>) * ((size_t)m + 1), sizeof(double) * 2 * (4 * (size_t)m + 3));
 }
 
 // The Gram-Schmidt passes of one iteration, after the matvec into B.W.
@@ -542,6 +566,13 @@ template <typename VT>
 static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
   const dim3 grid(gmres_grid(B.n), B.nrb);
   const size_t smem = gmres_update_smem(B.m);
+  // with the static arrays, long cycles pass the 48 KB that needs no opt-in
+  static std::once_flag once;
+  std::call_once(once, [] {
+    AC3D_CUDA(cudaFuncSetAttribute(k_gm_update<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)gmres_update_smem(kGmMaxRestart)));
+  });
+  if (B.m > kGmMaxRestart) throw Error(3, "internal: GMRES cycle longer than the update pass supports");
   const GmCols C = cols(B);
   launch_k(true, k_gm_dots<VT>, grid, dim3(kGmThreads), 0, s, C, B.m, B.n, (const cplx<VT>*)B.V,
            (const cplx<VT>*)B.W, 0);
