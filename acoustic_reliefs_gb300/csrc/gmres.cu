@@ -26,6 +26,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "df64.cuh"
 #include "gmres.h"
 #include "internal.h"
 #include "krylov.h"
@@ -63,7 +64,9 @@ struct GmLayout {
   __host__ __device__ size_t R() const { return sn() + 2 * (size_t)m; }                  // 2 m m
   __host__ __device__ size_t part() const { return R() + 2 * (size_t)m * m; }            // 2 (m + 1) G
   __host__ __device__ size_t npart() const { return part() + 2 * ((size_t)m + 1) * G; }  // G
-  __host__ __device__ size_t total() const { return npart() + (size_t)G; }
+  __host__ __device__ size_t part2() const { return npart() + (size_t)G; }               // 2 (m + 1) G
+  __host__ __device__ size_t h2() const { return part2() + 2 * ((size_t)m + 1) * G; }     // 2 (m + 1)
+  __host__ __device__ size_t total() const { return h2() + 2 * ((size_t)m + 1); }
 };
 
 // Column r = blockIdx.y of a batch: its state, scalars and basis.
@@ -111,6 +114,117 @@ __device__ __forceinline__ double warp_sum_run(const double* p, int G, int lane,
   VT a = 0;
   for (int c = lane; c < G; c += 32) a += (VT)__ldcg(&p[(size_t)c * stride]);
   return (double)warp_sum(a);
+}
+
+// The new Hessenberg column h (j + 1 entries in gd, h_{j+1} = nrm) by one CTA: rotate it by the
+// earlier Givens rotations, form the new rotation, update the residual estimate |g_{j+1}| and
+// decide whether the cycle goes on (the final step of an iteration). Shared memory: 4 j + 3
+// entries of 16 bytes (dynamic).
+__device__ __noinline__ void gm_rotate(GmCols C, GState* st, double* gd, GmLayout L, int m, int j, double nrm) {
+  // Rotate the new column h (j + 2 entries) by the earlier rotations: with x_0 = h_0,
+  //   r_i = c_i x_i + s_i h_{i+1},  x_{i+1} = conj(c_i) h_{i+1} - conj(s_i) x_i  (i < j).
+  // The recurrence is a composition of affine maps x -> M_i x + N_i (M_i = -conj(s_i), N_i =
+  // conj(c_i) h_{i+1}), so it runs as a parallel inclusive scan of the maps, composing later after
+  // earlier, (M2, N2) o (M1, N1) = (M2 M1, M2 N1 + N2), and then x_{i+1} = M_i x_0 + N_i. The scan
+  // is in double-float complex arithmetic on the FP32 pipes: a chain of dependent FP64 operations
+  // runs at a small fraction of that rate on this GPU.
+  extern __shared__ __align__(16) unsigned char gsm[];
+  Dc* hs = reinterpret_cast<Dc*>(gsm);      // h: j + 2 entries (the coefficients are no longer needed)
+  Dc* xs = hs + (j + 2);                    // x_i: j + 1 entries
+  cdf* sm = reinterpret_cast<cdf*>(xs + (j + 1));  // M_i: j entries
+  cdf* sn = sm + j;                                // N_i: j entries
+  __syncthreads();
+  // the column was completed by other CTAs before this CTA's ticket or barrier (read past L1)
+  for (int k = threadIdx.x; k <= j; k += blockDim.x)
+    hs[k] = dc(__ldcg(&gd[L.hcol() + 2 * k]), __ldcg(&gd[L.hcol() + 2 * k + 1]));
+  __syncthreads();
+  if (threadIdx.x == 0) hs[j + 1] = dc(nrm, 0.0);
+  for (int i = threadIdx.x; i < j; i += blockDim.x) {
+    const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
+    const Dc t = conjd(c) * hs[i + 1];
+    sn[i] = cdf{df_from_double(t.re), df_from_double(t.im)};
+    sm[i] = cdf{df_from_double(-gd[L.sn() + 2 * i]), df_from_double(gd[L.sn() + 2 * i + 1])};
+  }
+  __syncthreads();
+  constexpr int kPer = (kGmMaxRestart + kGmThreads - 1) / kGmThreads;  // scan entries per thread
+  for (int d = 1; d < j; d <<= 1) {
+    cdf nm[kPer], nn[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; u++) {
+      const int i = threadIdx.x + u * kGmThreads;
+      if (i < j) {
+        nm[u] = sm[i];
+        nn[u] = sn[i];
+        if (i >= d) {
+          const cdf m1 = sm[i - d], n1 = sn[i - d];
+          nn[u] = nm[u] * n1 + nn[u];
+          nm[u] = nm[u] * m1;
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < kPer; u++) {
+      const int i = threadIdx.x + u * kGmThreads;
+      if (i < j) {
+        sm[i] = nm[u];
+        sn[i] = nn[u];
+      }
+    }
+    __syncthreads();
+  }
+  {
+    const cdf x0{df_from_double(hs[0].re), df_from_double(hs[0].im)};
+    if (threadIdx.x == 0) xs[0] = hs[0];
+    for (int i = threadIdx.x; i < j; i += blockDim.x) {
+      const cdf x = sm[i] * x0 + sn[i];
+      xs[i + 1] = dc(df_to_double(x.re), df_to_double(x.im));
+    }
+  }
+  __syncthreads();
+  double* R = gd + L.R() + 2 * (size_t)j * m;  // column j: rows 0..j
+  for (int i = threadIdx.x; i < j; i += blockDim.x) {
+    const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
+    const Dc s = dc(gd[L.sn() + 2 * i], gd[L.sn() + 2 * i + 1]);
+    const Dc rv = c * xs[i] + s * hs[i + 1];
+    R[2 * i] = rv.re;
+    R[2 * i + 1] = rv.im;
+  }
+  if (threadIdx.x == 0) {
+    const Dc a0 = xs[j], b0 = hs[j + 1];
+    const double d = sqrt(abs2(a0) + abs2(b0));
+    Dc c = dc(1.0, 0.0), s = dc(0.0, 0.0);
+    if (d > 0.0) {
+      c = dc(a0.re / d, -a0.im / d);  // conj(a) / d
+      s = dc(b0.re / d, -b0.im / d);  // conj(b) / d
+    }
+    R[2 * j] = d;
+    R[2 * j + 1] = 0.0;
+    gd[L.cs() + 2 * j] = c.re;
+    gd[L.cs() + 2 * j + 1] = c.im;
+    gd[L.sn() + 2 * j] = s.re;
+    gd[L.sn() + 2 * j + 1] = s.im;
+    const Dc gj = dc(gd[L.g() + 2 * j], gd[L.g() + 2 * j + 1]);
+    const Dc g1 = dc(0.0, 0.0) - conjd(s) * gj;
+    const Dc g0 = c * gj;
+    gd[L.g() + 2 * j] = g0.re;
+    gd[L.g() + 2 * j + 1] = g0.im;
+    gd[L.g() + 2 * (j + 1)] = g1.re;
+    gd[L.g() + 2 * (j + 1) + 1] = g1.im;
+    const double res = sqrt(abs2(g1));
+    gd[L.s() + j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    st->resid = res;
+    st->j = j + 1;
+    st->ticket = 0u;
+    int code = 0;
+    if (!isfinite(res) || !isfinite(d) || d == 0.0)
+      code = (d == 0.0 && isfinite(res) && res <= st->tol_abs) ? 1 : 3;
+    else if (res <= st->tol_abs || nrm == 0.0)
+      code = 1;
+    else if (j + 1 >= m)
+      code = 2;
+    gm_mark_done(st, C.gm, code);
+  }
 }
 
 // V_0 = b (rounded to VT), q = V_0, s_0 = 1 / |V_0|, g = (|V_0|, 0, ...).
@@ -387,83 +501,279 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n
     gd[L.npart() + blockIdx.x] = (double)t;
   }
   if (!gm_last_cta(&st->ticket)) return;
-  // Rotate the new column h (j + 2 entries) by the earlier rotations: with x_0 = h_0,
-  //   r_i = c_i x_i + s_i h_{i+1},  x_{i+1} = conj(c_i) h_{i+1} - conj(s_i) x_i  (i < j),
-  // so the terms conj(c_i) h_{i+1} are formed in parallel and one thread runs the short chain.
   __shared__ double nrm_s;
-  Dc* hs = reinterpret_cast<Dc*>(gsm);      // h: j + 2 entries (the coefficients are no longer needed)
-  Dc* tc = hs + (j + 2);                    // conj(c_i) h_{i+1}: j entries
-  Dc* xs = tc + j;                          // chain values x_i: j + 1 entries
-  Dc* ss = xs + (j + 1);                    // conj(s_i): j entries (the chain reads shared memory only)
   __syncthreads();
   if (threadIdx.x < 32) {
     const double u2 = warp_sum_run<VT>(gd + L.npart(), L.G, threadIdx.x);
     if (threadIdx.x == 0) nrm_s = sqrt(u2);
   }
-  // CTA 0 of this pass completed the column before its ticket (read past L1)
-  for (int k = threadIdx.x; k <= j; k += blockDim.x)
-    hs[k] = dc(__ldcg(&gd[L.hcol() + 2 * k]), __ldcg(&gd[L.hcol() + 2 * k + 1]));
   __syncthreads();
-  const double nrm = nrm_s;
-  if (threadIdx.x == 0) hs[j + 1] = dc(nrm, 0.0);
-  for (int i = threadIdx.x; i < j; i += blockDim.x) {
-    const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
-    tc[i] = conjd(c) * hs[i + 1];
-    ss[i] = dc(gd[L.sn() + 2 * i], -gd[L.sn() + 2 * i + 1]);
-  }
+  gm_rotate(C, st, gd, L, m, j, nrm_s);
+}
+
+// ------------------------------------------------------------------------------------------
+// Fused Gram-Schmidt iteration: one cooperative launch in place of the dot and update passes.
+// All CTAs of the batch are resident (cooperative launch), and the phases are separated by grid
+// barriers instead of kernel boundaries and last-CTA reductions:
+//   1  dots: per-CTA partials of V_k^H X over the CTA's elements (k <= j);
+//   2  reduce: CTA c sums the partials of k = c, c + G, ... in CTA order into h_k (Hessenberg
+//      column) and the update coefficients h_k s_k;
+//   3  update: U = s_j X - sum_k coef_k V_k over the CTA's elements; with two passes U goes to
+//      W2 with the second pass's partials (and |U|^2 partials), then
+//   4  reduce as in 2 (h_k added to the column, |h_k|^2 kept), and
+//   5  the second update into V_{j+1}; |V_{j+1}|^2 = |U|^2 - sum_k |h_k|^2 (the second pass
+//      removes only a rounding-sized part of U); with one pass phase 3 writes V_{j+1} and its
+//      |.|^2 partials directly.
+// CTA 0 of each cycle then rotates the new column and updates the residual estimate, as the
+// final update pass does. Sums run in fixed orders, so results do not depend on timing. A cycle
+// that has ended passes the barriers without work.
+// ------------------------------------------------------------------------------------------
+constexpr uint32_t kBarSpin = 1u << 22;  // polls (with a short sleep) before a barrier gives up
+
+// Grid-wide barrier over all CTAs of a cooperative launch (every CTA calls it the same number of
+// times). Returns false on every thread if this CTA's wait gave up (recorded in bar_fail).
+__device__ __forceinline__ bool gm_grid_barrier(GMulti* gm, unsigned total) {
+  __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    Dc x = hs[0];
-    xs[0] = x;
-    for (int i = 0; i < j; i++) {
-      x = tc[i] - ss[i] * x;
-      xs[i + 1] = x;
+    volatile unsigned* genp = &gm->bar_gen;
+    const unsigned g = *genp;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(&gm->bar_count, 1u) == total - 1) {
+      atomicExch(&gm->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&gm->bar_gen, 1u);
+    } else {
+      uint32_t it = 0;
+      while (*genp == g) {
+        if (++it > kBarSpin) {
+          ok = 0;
+          atomicExch(&gm->bar_fail, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
     }
+    __threadfence();
+    s_ok = ok;
   }
   __syncthreads();
-  double* R = gd + L.R() + 2 * (size_t)j * m;  // column j: rows 0..j
-  for (int i = threadIdx.x; i < j; i += blockDim.x) {
-    const Dc c = dc(gd[L.cs() + 2 * i], gd[L.cs() + 2 * i + 1]);
-    const Dc s = dc(gd[L.sn() + 2 * i], gd[L.sn() + 2 * i + 1]);
-    const Dc rv = c * xs[i] + s * hs[i + 1];
-    R[2 * i] = rv.re;
-    R[2 * i + 1] = rv.im;
-  }
-  if (threadIdx.x == 0) {
-    const Dc a0 = xs[j], b0 = hs[j + 1];
-    const double d = sqrt(abs2(a0) + abs2(b0));
-    Dc c = dc(1.0, 0.0), s = dc(0.0, 0.0);
-    if (d > 0.0) {
-      c = dc(a0.re / d, -a0.im / d);  // conj(a) / d
-      s = dc(b0.re / d, -b0.im / d);  // conj(b) / d
+  return s_ok != 0;
+}
+
+// Per-CTA partial dots conj(V_k) . X over elements [lo, hi) (X from global memory with stride
+// xs), k = 0..j, into part[(k G + c) 2]; same ordering as gs_dot_partials.
+template <typename VT>
+__device__ __forceinline__ void gf_dot_partials(const cplx<VT>* __restrict__ V, const cplx<VT>* X, int xs, int lo,
+                                                int len, int n, int j, double* part, int G) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
+    VT ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
+    for (int t0 = 0; t0 < len; t0 += 128) {
+      cplx<VT> v[4][4], x[4];
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int t = t0 + 32 * e + lane;
+        x[e] = t < len ? X[(size_t)(lo + t) * xs] : cplx<VT>();
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          v[e][u] = (t < len && kb + u <= j) ? V[(size_t)(kb + u) * n + lo + t] : cplx<VT>();
+      }
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+#pragma unroll
+        for (int u = 0; u < 4; u++) {  // conj(v) x
+          ar[u] = fma(v[e][u].re, x[e].re, ar[u]);
+          ar[u] = fma(v[e][u].im, x[e].im, ar[u]);
+          ai[u] = fma(v[e][u].re, x[e].im, ai[u]);
+          ai[u] = fma(-v[e][u].im, x[e].re, ai[u]);
+        }
     }
-    R[2 * j] = d;
-    R[2 * j + 1] = 0.0;
-    gd[L.cs() + 2 * j] = c.re;
-    gd[L.cs() + 2 * j + 1] = c.im;
-    gd[L.sn() + 2 * j] = s.re;
-    gd[L.sn() + 2 * j + 1] = s.im;
-    const Dc gj = dc(gd[L.g() + 2 * j], gd[L.g() + 2 * j + 1]);
-    const Dc g1 = dc(0.0, 0.0) - conjd(s) * gj;
-    const Dc g0 = c * gj;
-    gd[L.g() + 2 * j] = g0.re;
-    gd[L.g() + 2 * j + 1] = g0.im;
-    gd[L.g() + 2 * (j + 1)] = g1.re;
-    gd[L.g() + 2 * (j + 1) + 1] = g1.im;
-    const double res = sqrt(abs2(g1));
-    gd[L.s() + j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
-    st->resid = res;
-    st->j = j + 1;
-    st->ticket = 0u;
-    int code = 0;
-    if (!isfinite(res) || !isfinite(d) || d == 0.0)
-      code = (d == 0.0 && isfinite(res) && res <= st->tol_abs) ? 1 : 3;
-    else if (res <= st->tol_abs || nrm == 0.0)
-      code = 1;
-    else if (j + 1 >= m)
-      code = 2;
-    gm_mark_done(st, C.gm, code);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      ar[u] = warp_sum(ar[u]);
+      ai[u] = warp_sum(ai[u]);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (kb + u <= j) {
+          part[((size_t)(kb + u) * G + blockIdx.x) * 2] = (double)ar[u];
+          part[((size_t)(kb + u) * G + blockIdx.x) * 2 + 1] = (double)ai[u];
+        }
   }
+}
+
+// Phase 2 / 4: this CTA's coefficients k = c, c + G, ... <= j (a warp each): h_k = s_k sx times
+// the sum of the partials in CTA order; the Hessenberg column gets h_k (set, or added on the
+// second pass), the update coefficient h_k s_k goes to coef, and on the second pass h_k to h2.
+template <typename VT>
+__device__ __forceinline__ void gf_reduce(double* gd, const GmLayout& L, const double* part, int G, int j, double sx,
+                                          int second) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = blockIdx.x + warp * G; k <= j; k += kGmWarps * G) {
+    VT ar = 0, ai = 0;
+    for (int c = lane; c < G; c += 32) {
+      ar += (VT)__ldcg(&part[((size_t)k * G + c) * 2]);
+      ai += (VT)__ldcg(&part[((size_t)k * G + c) * 2 + 1]);
+    }
+    ar = warp_sum(ar);
+    ai = warp_sum(ai);
+    if (lane == 0) {
+      const double sk = gd[L.s() + k];
+      const double hr = (double)ar * sk * sx, hi2 = (double)ai * sk * sx;
+      if (second) {
+        gd[L.hcol() + 2 * k] += hr;
+        gd[L.hcol() + 2 * k + 1] += hi2;
+        gd[L.h2() + 2 * k] = hr;
+        gd[L.h2() + 2 * k + 1] = hi2;
+      } else {
+        gd[L.hcol() + 2 * k] = hr;
+        gd[L.hcol() + 2 * k + 1] = hi2;
+      }
+      gd[L.coef() + 2 * k] = hr * sk;
+      gd[L.coef() + 2 * k + 1] = hi2 * sk;
+    }
+  }
+}
+
+// U = sx X - sum_k coef_k V_k over [lo, hi), written to out (and to q, stride qs, if q); returns
+// this thread's |U|^2.
+template <typename VT>
+__device__ __forceinline__ VT gf_update(const cplx<VT>* __restrict__ V, const cplx<VT>* X, int xs, VT sx,
+                                        const cplx<VT>* coef, int lo, int hi, int n, int j, cplx<VT>* out,
+                                        cplx<VT>* q, int qs) {
+  VT a = 0;
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const cplx<VT> x = X[(size_t)i * xs];
+    VT ur = sx * x.re, ui = sx * x.im;
+    const cplx<VT>* Vi = V + i;
+    int k = 0;
+    for (; k + 16 <= j + 1; k += 16) {
+      cplx<VT> v[16];
+#pragma unroll
+      for (int u = 0; u < 16; u++) v[u] = Vi[(size_t)(k + u) * n];
+#pragma unroll
+      for (int u = 0; u < 16; u++) {
+        const cplx<VT> c = coef[k + u];
+        ur = fma(-c.re, v[u].re, ur);
+        ur = fma(c.im, v[u].im, ur);
+        ui = fma(-c.re, v[u].im, ui);
+        ui = fma(-c.im, v[u].re, ui);
+      }
+    }
+    for (; k <= j; k++) {
+      const cplx<VT> v = Vi[(size_t)k * n];
+      const cplx<VT> c = coef[k];
+      ur = fma(-c.re, v.re, ur);
+      ur = fma(c.im, v.im, ur);
+      ui = fma(-c.re, v.im, ui);
+      ui = fma(-c.im, v.re, ui);
+    }
+    const cplx<VT> u(ur, ui);
+    out[i] = u;
+    if (q) q[(size_t)i * qs] = u;
+    a = fma(ur, ur, fma(ui, ui, a));
+  }
+  return a;
+}
+
+// Sum of a CTA's per-thread values in warp order, written to dst by thread 0.
+template <typename VT>
+__device__ __forceinline__ void gf_cta_sum(VT a, double* dst) {
+  __shared__ VT sw[kGmWarps];
+  a = warp_sum(a);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    VT t = 0;
+    for (int w = 0; w < kGmWarps; w++) t += sw[w];
+    *dst = (double)t;
+  }
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_fused(GmCols C, int m, int n, int LG, cplx<VT>* V,
+                                                         const cplx<VT>* __restrict__ W, cplx<VT>* W2, cplx<VT>* q,
+                                                         int reorth) {
+  const int r = blockIdx.y, G = (int)gridDim.x;
+  const unsigned total = gridDim.x * gridDim.y;
+  GState* st = C.st + r;
+  double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  const cplx<VT>* X = W + r;  // the matvec output (block vectors)
+  W2 += (size_t)r * n;
+  q += r;
+  const GmLayout L{m, LG};
+  const bool run = st->done == 0;  // CTA 0 changes it only after the last barrier
+  const int j = st->j;
+  int lo, hi;
+  gm_range(n, lo, hi);
+  extern __shared__ __align__(16) unsigned char gsm[];
+  cplx<VT>* coef = reinterpret_cast<cplx<VT>*>(gsm);
+  const double sj = run ? gd[L.s() + j] : 0.0;
+  bool ok = true;
+  auto load_coef = [&]() {
+    for (int k = threadIdx.x; k <= j; k += blockDim.x)
+      coef[k] = cplx<VT>((VT)__ldcg(&gd[L.coef() + 2 * k]), (VT)__ldcg(&gd[L.coef() + 2 * k + 1]));
+    __syncthreads();
+  };
+  // 1, 2: first-pass dots and their reduction
+  if (run) gf_dot_partials<VT>(V, X, C.vs, lo, hi - lo, n, j, gd + L.part(), G);
+  ok = gm_grid_barrier(C.gm, total) && ok;
+  if (run && ok) gf_reduce<VT>(gd, L, gd + L.part(), G, j, sj, 0);
+  ok = gm_grid_barrier(C.gm, total) && ok;
+  if (run && ok) load_coef();
+  VT a = 0;
+  if (reorth) {
+    // 3: U into W2, second-pass dots of U and |U|^2
+    if (run && ok) {
+      a = gf_update<VT>(V, X, C.vs, (VT)sj, coef, lo, hi, n, j, W2, nullptr, 0);
+      __syncthreads();  // W2 of this CTA's elements is complete
+      gf_dot_partials<VT>(V, W2, 1, lo, hi - lo, n, j, gd + L.part2(), G);
+    }
+    if (run && ok) gf_cta_sum<VT>(a, gd + L.npart() + blockIdx.x);
+    ok = gm_grid_barrier(C.gm, total) && ok;
+    // 4: second-pass coefficients
+    if (run && ok) gf_reduce<VT>(gd, L, gd + L.part2(), G, j, 1.0, 1);
+    ok = gm_grid_barrier(C.gm, total) && ok;
+    // 5: V_{j+1} = U - sum_k coef_k V_k
+    if (run && ok) {
+      load_coef();
+      gf_update<VT>(V, W2, 1, (VT)1, coef, lo, hi, n, j, V + (size_t)(j + 1) * n, q, C.vs);
+    }
+  } else {
+    // 3: V_{j+1} with its |.|^2 partials
+    if (run && ok) {
+      a = gf_update<VT>(V, X, C.vs, (VT)sj, coef, lo, hi, n, j, V + (size_t)(j + 1) * n, q, C.vs);
+      gf_cta_sum<VT>(a, gd + L.npart() + blockIdx.x);
+    }
+    ok = gm_grid_barrier(C.gm, total) && ok;
+  }
+  if (blockIdx.x != 0 || !run) return;
+  if (!ok) {
+    if (threadIdx.x == 0) gm_mark_done(st, C.gm, 3);
+    return;
+  }
+  // CTA 0: the new column's norm, its rotation and the residual estimate
+  __shared__ double nrm_s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double u2 = warp_sum_run<VT>(gd + L.npart(), G, threadIdx.x);
+    if (reorth) {  // |V_{j+1}|^2 = |U|^2 - sum_k |h2_k|^2 (k in order)
+      double s2 = 0;
+      for (int k = threadIdx.x; k <= j; k += 32) {
+        const double hr = __ldcg(&gd[L.h2() + 2 * k]), hi2 = __ldcg(&gd[L.h2() + 2 * k + 1]);
+        s2 += hr * hr + hi2 * hi2;
+      }
+      s2 = warp_sum(s2);
+      u2 = fmax(u2 - s2, 0.0);
+    }
+    if (threadIdx.x == 0) nrm_s = sqrt(u2);
+  }
+  __syncthreads();
+  gm_rotate(C, st, gd, L, m, j, nrm_s);
 }
 
 // y = R^{-1} g over the completed columns, then coef_k = y_k s_k (one CTA).
@@ -568,11 +878,34 @@ static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
   const size_t smem = gmres_update_smem(B.m);
   // with the static arrays, long cycles pass the 48 KB that needs no opt-in
   static std::once_flag once;
+  static int fused_per_sm = 0;  // resident CTAs per SM of the fused kernel
   std::call_once(once, [] {
-    AC3D_CUDA(cudaFuncSetAttribute(k_gm_update<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)gmres_update_smem(kGmMaxRestart)));
+    const int sm = (int)gmres_update_smem(kGmMaxRestart);
+    AC3D_CUDA(cudaFuncSetAttribute(k_gm_update<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    AC3D_CUDA(cudaFuncSetAttribute(k_gm_fused<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    AC3D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fused_per_sm, k_gm_fused<VT>, kGmThreads, sm));
   });
   if (B.m > kGmMaxRestart) throw Error(3, "internal: GMRES cycle longer than the update pass supports");
+  // one cooperative launch when every cycle of the batch can have a CTA resident at once
+  const int LG = gmres_grid(B.n);
+  const int Gc = std::min(LG, fused_per_sm * device_sm_count() / std::max(B.nrb, 1));
+  if (Gc >= 1 && (!B.reorth || B.W2)) {
+    const GmCols C = cols(B);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(Gc, B.nrb);
+    cfg.blockDim = dim3(kGmThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    note_launch();
+    AC3D_CUDA(cudaLaunchKernelEx(&cfg, k_gm_fused<VT>, C, B.m, B.n, LG, (cplx<VT>*)B.V, (const cplx<VT>*)B.W,
+                                 (cplx<VT>*)B.W2, (cplx<VT>*)B.q, B.reorth));
+    return;
+  }
   const GmCols C = cols(B);
   launch_k(true, k_gm_dots<VT>, grid, dim3(kGmThreads), 0, s, C, B.m, B.n, (const cplx<VT>*)B.V,
            (const cplx<VT>*)B.W, 0);

@@ -23,7 +23,9 @@ struct GState {
 struct GMulti {
   int ndone;     // cycles that have ended
   int done_all;
-  int pad[2];
+  unsigned bar_count, bar_gen;  // grid barrier of the fused Gram-Schmidt kernel (zero at init)
+  int bar_fail;                 // a grid barrier gave up waiting
+  int pad[3];
 };
 
 // Device buffers of one cycle, or of a batch of nrb independent cycles that share their matvecs
