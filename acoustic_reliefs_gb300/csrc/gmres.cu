@@ -116,6 +116,20 @@ __device__ __forceinline__ double warp_sum_run(const double* p, int G, int lane,
   return (double)warp_sum(a);
 }
 
+// sqrt(x) and 1 / x of an FP64 scalar through double-float arithmetic on the FP32 pipes (about 47
+// bits): on this GPU FP64 square roots and divisions are long dependent sequences, and these sit on
+// the serial tail of every iteration. Outside FP32's comfortable range, or for 0, negative and
+// non-finite values, the FP64 operation.
+__device__ __forceinline__ double gm_sqrt(double x) {
+  if (x > 1e-30 && x < 1e30) return df_to_double(df_sqrt(df_from_double(x)));
+  return sqrt(x);
+}
+__device__ __forceinline__ double gm_rcp(double x) {
+  const double a = fabs(x);
+  if (a > 1e-30 && a < 1e30) return df_to_double(df_rcp(df_from_double(x)));
+  return 1.0 / x;
+}
+
 // The new Hessenberg column h (j + 1 entries in gd, h_{j+1} = nrm) by one CTA: rotate it by the
 // earlier Givens rotations, form the new rotation, update the residual estimate |g_{j+1}| and
 // decide whether the cycle goes on (the final step of an iteration). Shared memory: 4 j + 3
@@ -192,11 +206,12 @@ __device__ __noinline__ void gm_rotate(GmCols C, GState* st, double* gd, GmLayou
   }
   if (threadIdx.x == 0) {
     const Dc a0 = xs[j], b0 = hs[j + 1];
-    const double d = sqrt(abs2(a0) + abs2(b0));
+    const double d = gm_sqrt(abs2(a0) + abs2(b0));
     Dc c = dc(1.0, 0.0), s = dc(0.0, 0.0);
     if (d > 0.0) {
-      c = dc(a0.re / d, -a0.im / d);  // conj(a) / d
-      s = dc(b0.re / d, -b0.im / d);  // conj(b) / d
+      const double id = gm_rcp(d);
+      c = dc(a0.re * id, -a0.im * id);  // conj(a) / d
+      s = dc(b0.re * id, -b0.im * id);  // conj(b) / d
     }
     R[2 * j] = d;
     R[2 * j + 1] = 0.0;
@@ -211,8 +226,8 @@ __device__ __noinline__ void gm_rotate(GmCols C, GState* st, double* gd, GmLayou
     gd[L.g() + 2 * j + 1] = g0.im;
     gd[L.g() + 2 * (j + 1)] = g1.re;
     gd[L.g() + 2 * (j + 1) + 1] = g1.im;
-    const double res = sqrt(abs2(g1));
-    gd[L.s() + j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    const double res = gm_sqrt(abs2(g1));
+    gd[L.s() + j + 1] = nrm > 0.0 ? gm_rcp(nrm) : 0.0;
     st->resid = res;
     st->j = j + 1;
     st->ticket = 0u;
@@ -505,7 +520,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n
   __syncthreads();
   if (threadIdx.x < 32) {
     const double u2 = warp_sum_run<VT>(gd + L.npart(), L.G, threadIdx.x);
-    if (threadIdx.x == 0) nrm_s = sqrt(u2);
+    if (threadIdx.x == 0) nrm_s = gm_sqrt(u2);
   }
   __syncthreads();
   gm_rotate(C, st, gd, L, m, j, nrm_s);
@@ -770,7 +785,7 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_fused(GmCols C, int m, int n,
       s2 = warp_sum(s2);
       u2 = fmax(u2 - s2, 0.0);
     }
-    if (threadIdx.x == 0) nrm_s = sqrt(u2);
+    if (threadIdx.x == 0) nrm_s = gm_sqrt(u2);
   }
   __syncthreads();
   gm_rotate(C, st, gd, L, m, j, nrm_s);
@@ -790,8 +805,8 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_solve(GmCols C, int m, int G)
   for (int k = jj - 1; k >= 0; k--) {
     const double* Rk = gd + L.R() + 2 * (size_t)k * m;  // column k
     if (threadIdx.x == 0) {
-      const double d = Rk[2 * k];  // real and positive
-      yk = dc(gs[k].re / d, gs[k].im / d);
+      const double id = gm_rcp(Rk[2 * k]);  // the diagonal is real and positive
+      yk = dc(gs[k].re * id, gs[k].im * id);
       const double sk = gd[L.s() + k];
       gd[L.coef() + 2 * k] = yk.re * sk;
       gd[L.coef() + 2 * k + 1] = yk.im * sk;
