@@ -218,10 +218,26 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
   H->near.alloc((size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s);
   if (prec != PREC_FP64) H->xdf.alloc((size_t)c->m->Ne * sizeof(cd), s);
   AC3D_CUDA(cudaMemsetAsync(H->near.p, 0, (size_t)std::max<int64_t>(c->m->P.near_total, 2) * cs, s));
+  // near field and ACA kernels on the low-priority assembly streams; every buffer is allocated
+  // and freed on s, which waits for them before it reads their results
+  cudaStream_t as = c->asm_s;
+  AC3D_CUDA(cudaEventRecord(c->ev_fork, s));
+  AC3D_CUDA(cudaStreamWaitEvent(as, c->ev_fork, 0));
+  // On every way out (an exception included), s waits for the assembly streams before anything
+  // frees H's buffers on s (destroyed before H: declared after it).
+  struct JoinAssembly {
+    ac3d_ctx* c;
+    ~JoinAssembly() {
+      cudaEventRecord(c->ev_join_asm, c->asm_s);
+      cudaStreamWaitEvent(c->stream, c->ev_join_asm, 0);
+      cudaEventRecord(c->ev_join, c->side);
+      cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+    }
+  } join_assembly{c};
   if (H->pool_df)
-    launch_near_assembly_df(c->m->G, c->m->DP, *H, s);
+    launch_near_assembly_df(c->m->G, c->m->DP, *H, as);
   else
-    launch_near_assembly(c->m->G, c->m->DP, *H, s);
+    launch_near_assembly(c->m->G, c->m->DP, *H, as);
   H->err.alloc(16, s);
   AC3D_CUDA(cudaMemsetAsync(H->err.p, 0, 16, s));
   H->ticket.alloc(16, s);
@@ -242,15 +258,18 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
       H->pool.alloc((size_t)cap * pool_es, s);
       H->pool_cap = cap;
       AC3D_CUDA(cudaMemsetAsync(H->pool_used.p, 0, 16, s));
-      // small blocks (one warp each) run on the side stream, concurrently with the large ones
+      // the ACA groups on the two assembly streams (the first after the near field)
       AC3D_CUDA(cudaEventRecord(c->ev_fork, s));
+      AC3D_CUDA(cudaStreamWaitEvent(as, c->ev_fork, 0));
       AC3D_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
       if (H->pool_df)
-        launch_aca_df(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, s, c->side);
+        launch_aca_df(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, as, c->side);
       else
-        launch_aca(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, s, c->side);
+        launch_aca(c->m->G, c->m->DP, *H, c->aca_tol, c->m->P.max_rows, as, c->side);
       AC3D_CUDA(cudaEventRecord(c->ev_join, c->side));
+      AC3D_CUDA(cudaEventRecord(c->ev_join_asm, as));
       AC3D_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+      AC3D_CUDA(cudaStreamWaitEvent(s, c->ev_join_asm, 0));
       unsigned long long hu[2];
       AC3D_CUDA(cudaMemcpyAsync(hu, H->pool_used.p, 16, cudaMemcpyDeviceToHost, s));
       AC3D_CUDA(cudaStreamSynchronize(s));
@@ -354,6 +373,9 @@ std::unique_ptr<DevHMat> assemble(ac3d_ctx* c, double k, int prec) {
     c->stats.max_rank = mx;
     c->stats.mean_rank = sr / na;
   } else {
+    // no admissible blocks: only the near field ran on the assembly stream
+    AC3D_CUDA(cudaEventRecord(c->ev_join_asm, as));
+    AC3D_CUDA(cudaStreamWaitEvent(s, c->ev_join_asm, 0));
     AC3D_CUDA(cudaMemsetAsync(H->t_off.p, 0, sizeof(int), s));
     H->tvec.alloc(16, s);
     H->tvec64.alloc(16, s);
@@ -1360,10 +1382,18 @@ int ac3d_create(ac3d_ctx** out, int cluster_size, double radius_factor, const do
   c->recompute = recompute_matrices != 0;
   c->Ls = hemisphere(listener_radius, listener_ds);
   int rc = guard(c, [&] {
-    AC3D_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    AC3D_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    // The context's stream at the highest priority, the assembly kernels on two streams at the
+    // lowest: when several contexts share the GPU (the request server), the latency-bound solve
+    // kernels of one request take SMs as they free up ahead of the compute-bound ACA blocks of
+    // another. Within one context the streams are ordered by events as before.
+    int prio_low = 0, prio_high = 0;
+    AC3D_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    AC3D_CUDA(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_high));
+    AC3D_CUDA(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_low));
+    AC3D_CUDA(cudaStreamCreateWithPriority(&c->asm_s, cudaStreamNonBlocking, prio_low));
     AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_join_asm, cudaEventDisableTiming));
     int dev = 0;
     AC3D_CUDA(cudaGetDevice(&dev));
     cudaMemPool_t pool;
@@ -1394,12 +1424,15 @@ void ac3d_destroy(ac3d_ctx* c) {
   for (DevBuf* b : bufs) b->release();
   c->m.reset();  // a mesh shared with other contexts stays alive until its last user goes
   c->m_dense.reset();
-  if (c->side) {
-    cudaStreamSynchronize(c->side);
-    cudaStreamDestroy(c->side);
-  }
+  for (cudaStream_t* st : {&c->side, &c->asm_s})
+    if (*st) {
+      cudaStreamSynchronize(*st);
+      cudaStreamDestroy(*st);
+      *st = nullptr;
+    }
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_join_asm) cudaEventDestroy(c->ev_join_asm);
   if (s) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);

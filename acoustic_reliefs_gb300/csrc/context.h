@@ -42,8 +42,9 @@ struct ac3d_ctx {
   bool actual = false;     // use_actual: the coefficient / gradient calls run on the exact operator
 
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;                 // concurrent assembly work
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t side = nullptr;                 // concurrent assembly work (low priority)
+  cudaStream_t asm_s = nullptr;                // assembly kernels (low priority; stream is high)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join_asm = nullptr;
   std::string err;
   ac3d_stats stats{};
 
