@@ -166,6 +166,22 @@ void build_leaf_lists(Partition& P, int maxk) {
     P.max_rows = std::max(P.max_rows, m);
     P.aca_term_cap += std::max(0, std::min(maxk, std::min(m - 1, n - 1)));
   }
+  // The low-rank blocks of a leaf's lists ordered by cluster (the blocks' row cluster for the
+  // U side, column cluster for the V side), then by block: the blocks that share a cluster occupy
+  // one run of consecutive segment columns in every leaf of that cluster, in the same order, so a
+  // pass can accumulate a cluster's terms over its leaves.
+  for (int l = 0; l < nleaf; l++) {
+    std::stable_sort(fl[l].begin(), fl[l].end(), [&](int a, int c) {
+      const int* qa = &P.approx[4 * a];
+      const int* qc = &P.approx[4 * c];
+      return qa[0] != qc[0] ? qa[0] < qc[0] : qa[1] != qc[1] ? qa[1] < qc[1] : a < c;
+    });
+    std::stable_sort(tl[l].begin(), tl[l].end(), [&](int a, int c) {
+      const int* qa = &P.approx[4 * a];
+      const int* qc = &P.approx[4 * c];
+      return qa[2] != qc[2] ? qa[2] < qc[2] : qa[3] != qc[3] ? qa[3] < qc[3] : a < c;
+    });
+  }
   csr(fn, P.fw_near_ptr, P.fw_near);
   // near storage in forward leaf order: each leaf's blocks form one R x NC column-major segment
   P.near_off.assign(nd, 0);
