@@ -518,6 +518,9 @@ GmresBufs gmres_bufs(ac3d_ctx* c, const DevHMat& H, const void* b, int nrb = 1) 
   // FP32 classical Gram-Schmidt loses orthogonality over long cycles: two passes keep the FP32
   // cycle converging like the FP64 one
   G.reorth = G.vec64 ? 0 : 1;
+  G.rot_stream = c->givens_branch ? c->rot : nullptr;
+  G.ev_gs = c->ev_gs;
+  G.ev_rot = c->ev_rot;
   if (!c->h_gstate) AC3D_CUDA(cudaMallocHost(&c->h_gstate, 2 * sizeof(GState)));
   return G;
 }
@@ -1394,6 +1397,9 @@ int ac3d_create(ac3d_ctx** out, int cluster_size, double radius_factor, const do
     AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_join_asm, cudaEventDisableTiming));
+    AC3D_CUDA(cudaStreamCreateWithPriority(&c->rot, cudaStreamNonBlocking, prio_high));
+    AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_gs, cudaEventDisableTiming));
+    AC3D_CUDA(cudaEventCreateWithFlags(&c->ev_rot, cudaEventDisableTiming));
     int dev = 0;
     AC3D_CUDA(cudaGetDevice(&dev));
     cudaMemPool_t pool;
@@ -1424,7 +1430,7 @@ void ac3d_destroy(ac3d_ctx* c) {
   for (DevBuf* b : bufs) b->release();
   c->m.reset();  // a mesh shared with other contexts stays alive until its last user goes
   c->m_dense.reset();
-  for (cudaStream_t* st : {&c->side, &c->asm_s})
+  for (cudaStream_t* st : {&c->side, &c->asm_s, &c->rot})
     if (*st) {
       cudaStreamSynchronize(*st);
       cudaStreamDestroy(*st);
@@ -1433,6 +1439,8 @@ void ac3d_destroy(ac3d_ctx* c) {
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_join_asm) cudaEventDestroy(c->ev_join_asm);
+  if (c->ev_gs) cudaEventDestroy(c->ev_gs);
+  if (c->ev_rot) cudaEventDestroy(c->ev_rot);
   if (s) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);

@@ -45,6 +45,13 @@ struct ac3d_ctx {
   cudaStream_t side = nullptr;                 // concurrent assembly work (low priority)
   cudaStream_t asm_s = nullptr;                // assembly kernels (low priority; stream is high)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join_asm = nullptr;
+  cudaStream_t rot = nullptr;                  // GMRES Givens steps beside the next matvec (high)
+  cudaEvent_t ev_gs = nullptr, ev_rot = nullptr;
+  // Run the Givens step of each GMRES iteration as its own kernel beside the next matvec (on
+  // `rot`). A request server's slots keep it inside the Gram-Schmidt kernel: there the other
+  // slots' kernels fill the GPU, and a separate one-CTA kernel waits for a free CTA slot (behind
+  // long assembly CTAs) on the solve's critical path.
+  bool givens_branch = true;
   std::string err;
   ac3d_stats stats{};
 

@@ -22,6 +22,14 @@
 // Batches: the kernels take the cycle as the grid's y index, so nrb independent cycles (one per
 // right-hand side of a block solve) run together and share each block matvec; their inputs and
 // outputs are element-major block vectors (stride nrb).
+//
+// The Givens step (norm, rotation of the new column, residual estimate, stop test) is serial work
+// of one CTA, about 10 us per iteration on the 20k relief. Where the fused cooperative kernel runs,
+// it goes either to a kernel of its own on a forked graph branch (k_gm_rotate), overlapping the
+// next matvec, which needs only V_{j+1}, and joined before the next Gram-Schmidt kernel; or, in
+// a request server's slots, to one extra CTA of the fused kernel that starts it while the element
+// CTAs run the last update. Either way the arithmetic and its order are the same, so the results
+// are bitwise the same.
 #include <algorithm>
 #include <mutex>
 
@@ -577,18 +585,28 @@ __device__ __forceinline__ bool gm_grid_barrier(GMulti* gm, unsigned total) {
   return s_ok != 0;
 }
 
+// Elements per lane per round of loads in gf_dot_partials: with FP32 vectors one round covers a
+// CTA's slice of a 20k-element vector over 152 CTAs (135 elements). (The FP32 fused kernel runs at
+// 3 CTAs per SM, 80 registers, without spills.)
+template <typename VT>
+struct GfDotRound {
+  static constexpr int E = sizeof(VT) == 4 ? 5 : 4;
+};
+
 // Per-CTA partial dots conj(V_k) . X over elements [lo, hi) (X from global memory with stride
-// xs), k = 0..j, into part[(k G + c) 2]; same ordering as gs_dot_partials.
+// xs), k = 0..j, into part[(k G + c) 2]; same ordering as gs_dot_partials: each lane takes the
+// elements lane, lane + 32, ... in that order, whatever the round width.
 template <typename VT>
 __device__ __forceinline__ void gf_dot_partials(const cplx<VT>* __restrict__ V, const cplx<VT>* X, int xs, int lo,
                                                 int len, int n, int j, double* part, int G) {
+  constexpr int kGfE = GfDotRound<VT>::E;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int kb = 4 * warp; kb <= j; kb += 4 * kGmWarps) {
     VT ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
-    for (int t0 = 0; t0 < len; t0 += 128) {
-      cplx<VT> v[4][4], x[4];
+    for (int t0 = 0; t0 < len; t0 += 32 * kGfE) {
+      cplx<VT> v[kGfE][4], x[kGfE];
 #pragma unroll
-      for (int e = 0; e < 4; e++) {
+      for (int e = 0; e < kGfE; e++) {
         const int t = t0 + 32 * e + lane;
         x[e] = t < len ? X[(size_t)(lo + t) * xs] : cplx<VT>();
 #pragma unroll
@@ -596,7 +614,7 @@ __device__ __forceinline__ void gf_dot_partials(const cplx<VT>* __restrict__ V, 
           v[e][u] = (t < len && kb + u <= j) ? V[(size_t)(kb + u) * n + lo + t] : cplx<VT>();
       }
 #pragma unroll
-      for (int e = 0; e < 4; e++)
+      for (int e = 0; e < kGfE; e++)
 #pragma unroll
         for (int u = 0; u < 4; u++) {  // conj(v) x
           ar[u] = fma(v[e][u].re, x[e].re, ar[u]);
@@ -653,38 +671,63 @@ __device__ __forceinline__ void gf_reduce(double* gd, const GmLayout& L, const d
   }
 }
 
+// Basis vectors per round of loads in gf_update (16). With FP32 vectors the last round is partial
+// (loads and products beyond j skipped), so a thread waits for ceil((j + 1) / 16) rounds, not for
+// a remainder one vector at a time; with FP64 vectors the remainder goes one vector at a time. The
+// products keep the order k = 0, 1, ... either way.
+constexpr int kGfChunk = 16;
+
 // U = sx X - sum_k coef_k V_k over [lo, hi), written to out (and to q, stride qs, if q); returns
 // this thread's |U|^2.
 template <typename VT>
 __device__ __forceinline__ VT gf_update(const cplx<VT>* __restrict__ V, const cplx<VT>* X, int xs, VT sx,
                                         const cplx<VT>* coef, int lo, int hi, int n, int j, cplx<VT>* out,
                                         cplx<VT>* q, int qs) {
+  constexpr int KC = kGfChunk;
+  constexpr bool partial_rounds = sizeof(VT) == 4;
   VT a = 0;
   for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const cplx<VT> x = X[(size_t)i * xs];
     VT ur = sx * x.re, ui = sx * x.im;
     const cplx<VT>* Vi = V + i;
     int k = 0;
-    for (; k + 16 <= j + 1; k += 16) {
-      cplx<VT> v[16];
+    if constexpr (partial_rounds) {
+      for (; k <= j; k += KC) {
+        cplx<VT> v[KC];
 #pragma unroll
-      for (int u = 0; u < 16; u++) v[u] = Vi[(size_t)(k + u) * n];
+        for (int u = 0; u < KC; u++) v[u] = k + u <= j ? Vi[(size_t)(k + u) * n] : cplx<VT>();
 #pragma unroll
-      for (int u = 0; u < 16; u++) {
-        const cplx<VT> c = coef[k + u];
-        ur = fma(-c.re, v[u].re, ur);
-        ur = fma(c.im, v[u].im, ur);
-        ui = fma(-c.re, v[u].im, ui);
-        ui = fma(-c.im, v[u].re, ui);
+        for (int u = 0; u < KC; u++) {
+          if (k + u > j) break;
+          const cplx<VT> c = coef[k + u];
+          ur = fma(-c.re, v[u].re, ur);
+          ur = fma(c.im, v[u].im, ur);
+          ui = fma(-c.re, v[u].im, ui);
+          ui = fma(-c.im, v[u].re, ui);
+        }
       }
-    }
-    for (; k <= j; k++) {
-      const cplx<VT> v = Vi[(size_t)k * n];
-      const cplx<VT> c = coef[k];
-      ur = fma(-c.re, v.re, ur);
-      ur = fma(c.im, v.im, ur);
-      ui = fma(-c.re, v.im, ui);
-      ui = fma(-c.im, v.re, ui);
+    } else {
+      for (; k + KC <= j + 1; k += KC) {
+        cplx<VT> v[KC];
+#pragma unroll
+        for (int u = 0; u < KC; u++) v[u] = Vi[(size_t)(k + u) * n];
+#pragma unroll
+        for (int u = 0; u < KC; u++) {
+          const cplx<VT> c = coef[k + u];
+          ur = fma(-c.re, v[u].re, ur);
+          ur = fma(c.im, v[u].im, ur);
+          ui = fma(-c.re, v[u].im, ui);
+          ui = fma(-c.im, v[u].re, ui);
+        }
+      }
+      for (; k <= j; k++) {
+        const cplx<VT> v = Vi[(size_t)k * n];
+        const cplx<VT> c = coef[k];
+        ur = fma(-c.re, v.re, ur);
+        ur = fma(c.im, v.im, ur);
+        ui = fma(-c.re, v.im, ui);
+        ui = fma(-c.im, v.re, ui);
+      }
     }
     const cplx<VT> u(ur, ui);
     out[i] = u;
@@ -708,75 +751,16 @@ __device__ __forceinline__ void gf_cta_sum(VT a, double* dst) {
   }
 }
 
+// |V_{j+1}| from the |U|^2 partials of G CTAs (two passes: minus the second pass's sum_k |h2_k|^2,
+// k in order), then the Givens step of gm_rotate; one CTA.
 template <typename VT>
-__global__ void __launch_bounds__(kGmThreads) k_gm_fused(GmCols C, int m, int n, int LG, cplx<VT>* V,
-                                                         const cplx<VT>* __restrict__ W, cplx<VT>* W2, cplx<VT>* q,
-                                                         int reorth) {
-  const int r = blockIdx.y, G = (int)gridDim.x;
-  const unsigned total = gridDim.x * gridDim.y;
-  GState* st = C.st + r;
-  double* gd = C.gd + r * C.gds;
-  V += r * C.Vs;
-  const cplx<VT>* X = W + r;  // the matvec output (block vectors)
-  W2 += (size_t)r * n;
-  q += r;
-  const GmLayout L{m, LG};
-  const bool run = st->done == 0;  // CTA 0 changes it only after the last barrier
-  const int j = st->j;
-  int lo, hi;
-  gm_range(n, lo, hi);
-  extern __shared__ __align__(16) unsigned char gsm[];
-  cplx<VT>* coef = reinterpret_cast<cplx<VT>*>(gsm);
-  const double sj = run ? gd[L.s() + j] : 0.0;
-  bool ok = true;
-  auto load_coef = [&]() {
-    for (int k = threadIdx.x; k <= j; k += blockDim.x)
-      coef[k] = cplx<VT>((VT)__ldcg(&gd[L.coef() + 2 * k]), (VT)__ldcg(&gd[L.coef() + 2 * k + 1]));
-    __syncthreads();
-  };
-  // 1, 2: first-pass dots and their reduction
-  if (run) gf_dot_partials<VT>(V, X, C.vs, lo, hi - lo, n, j, gd + L.part(), G);
-  ok = gm_grid_barrier(C.gm, total) && ok;
-  if (run && ok) gf_reduce<VT>(gd, L, gd + L.part(), G, j, sj, 0);
-  ok = gm_grid_barrier(C.gm, total) && ok;
-  if (run && ok) load_coef();
-  VT a = 0;
-  if (reorth) {
-    // 3: U into W2, second-pass dots of U and |U|^2
-    if (run && ok) {
-      a = gf_update<VT>(V, X, C.vs, (VT)sj, coef, lo, hi, n, j, W2, nullptr, 0);
-      __syncthreads();  // W2 of this CTA's elements is complete
-      gf_dot_partials<VT>(V, W2, 1, lo, hi - lo, n, j, gd + L.part2(), G);
-    }
-    if (run && ok) gf_cta_sum<VT>(a, gd + L.npart() + blockIdx.x);
-    ok = gm_grid_barrier(C.gm, total) && ok;
-    // 4: second-pass coefficients
-    if (run && ok) gf_reduce<VT>(gd, L, gd + L.part2(), G, j, 1.0, 1);
-    ok = gm_grid_barrier(C.gm, total) && ok;
-    // 5: V_{j+1} = U - sum_k coef_k V_k
-    if (run && ok) {
-      load_coef();
-      gf_update<VT>(V, W2, 1, (VT)1, coef, lo, hi, n, j, V + (size_t)(j + 1) * n, q, C.vs);
-    }
-  } else {
-    // 3: V_{j+1} with its |.|^2 partials
-    if (run && ok) {
-      a = gf_update<VT>(V, X, C.vs, (VT)sj, coef, lo, hi, n, j, V + (size_t)(j + 1) * n, q, C.vs);
-      gf_cta_sum<VT>(a, gd + L.npart() + blockIdx.x);
-    }
-    ok = gm_grid_barrier(C.gm, total) && ok;
-  }
-  if (blockIdx.x != 0 || !run) return;
-  if (!ok) {
-    if (threadIdx.x == 0) gm_mark_done(st, C.gm, 3);
-    return;
-  }
-  // CTA 0: the new column's norm, its rotation and the residual estimate
+__device__ __forceinline__ void gf_norm_rotate(GmCols C, GState* st, double* gd, const GmLayout& L, int m, int j,
+                                               int G, int reorth) {
   __shared__ double nrm_s;
   __syncthreads();
   if (threadIdx.x < 32) {
     double u2 = warp_sum_run<VT>(gd + L.npart(), G, threadIdx.x);
-    if (reorth) {  // |V_{j+1}|^2 = |U|^2 - sum_k |h2_k|^2 (k in order)
+    if (reorth) {
       double s2 = 0;
       for (int k = threadIdx.x; k <= j; k += 32) {
         const double hr = __ldcg(&gd[L.h2() + 2 * k]), hi2 = __ldcg(&gd[L.h2() + 2 * k + 1]);
@@ -789,6 +773,102 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_fused(GmCols C, int m, int n,
   }
   __syncthreads();
   gm_rotate(C, st, gd, L, m, j, nrm_s);
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads, sizeof(VT) == 4 ? 3 : 2) k_gm_fused(GmCols C, int m, int n, int LG, cplx<VT>* V,
+                                                         const cplx<VT>* __restrict__ W, cplx<VT>* W2, cplx<VT>* q,
+                                                         int reorth, int givens) {
+  // givens: where the Givens step runs. 0: CTA 0 after its last update; 1: k_gm_rotate after this
+  // kernel (the caller forks it); 2: one CTA more than the element CTAs (the last), right after
+  // the last grid barrier, while the others run the last update.
+  const int r = blockIdx.y, G = (int)gridDim.x - (givens == 2 ? 1 : 0);
+  const bool rot_cta = givens == 2 && (int)blockIdx.x == G;
+  // with the Givens step forked, the next matvec may start streaming its matrix during the last
+  // update (it reads V_{j+1} only after this kernel has completed). Not with the Givens CTA: inside
+  // a request server the early matvec CTAs would hold SM room that other requests' kernels need.
+  const bool early = givens == 1;
+  const unsigned total = gridDim.x * gridDim.y;
+  GState* st = C.st + r;
+  double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  const cplx<VT>* X = W + r;  // the matvec output (block vectors)
+  W2 += (size_t)r * n;
+  q += r;
+  const GmLayout L{m, LG};
+  const bool run = st->done == 0;  // changed only by the Givens step, after the last barrier
+  const bool work = run && !rot_cta;  // element work of this CTA
+  const int j = st->j;
+  int lo, hi;
+  {  // contiguous element range of this CTA among the G element CTAs (none for the Givens CTA)
+    const int per = (n + G - 1) / G;
+    lo = min(n, (int)blockIdx.x * per);
+    hi = min(n, lo + per);
+  }
+  extern __shared__ __align__(16) unsigned char gsm[];
+  cplx<VT>* coef = reinterpret_cast<cplx<VT>*>(gsm);
+  const double sj = work ? gd[L.s() + j] : 0.0;
+  bool ok = true;
+  auto load_coef = [&]() {
+    for (int k = threadIdx.x; k <= j; k += blockDim.x)
+      coef[k] = cplx<VT>((VT)__ldcg(&gd[L.coef() + 2 * k]), (VT)__ldcg(&gd[L.coef() + 2 * k + 1]));
+    __syncthreads();
+  };
+  // 1, 2: first-pass dots and their reduction
+  if (work) gf_dot_partials<VT>(V, X, C.vs, lo, hi - lo, n, j, gd + L.part(), G);
+  ok = gm_grid_barrier(C.gm, total) && ok;
+  if (work && ok) gf_reduce<VT>(gd, L, gd + L.part(), G, j, sj, 0);
+  ok = gm_grid_barrier(C.gm, total) && ok;
+  if (work && ok) load_coef();
+  VT a = 0;
+  if (reorth) {
+    // 3: U into W2, second-pass dots of U and |U|^2
+    if (work && ok) {
+      a = gf_update<VT>(V, X, C.vs, (VT)sj, coef, lo, hi, n, j, W2, nullptr, 0);
+      __syncthreads();  // W2 of this CTA's elements is complete
+      gf_dot_partials<VT>(V, W2, 1, lo, hi - lo, n, j, gd + L.part2(), G);
+    }
+    if (work && ok) gf_cta_sum<VT>(a, gd + L.npart() + blockIdx.x);
+    ok = gm_grid_barrier(C.gm, total) && ok;
+    // 4: second-pass coefficients
+    if (work && ok) gf_reduce<VT>(gd, L, gd + L.part2(), G, j, 1.0, 1);
+    ok = gm_grid_barrier(C.gm, total) && ok;
+    if (early) grid_dep_launch();
+    // 5: V_{j+1} = U - sum_k coef_k V_k
+    if (work && ok) {
+      load_coef();
+      gf_update<VT>(V, W2, 1, (VT)1, coef, lo, hi, n, j, V + (size_t)(j + 1) * n, q, C.vs);
+    }
+  } else {
+    if (early) grid_dep_launch();
+    // 3: V_{j+1} with its |.|^2 partials
+    if (work && ok) {
+      a = gf_update<VT>(V, X, C.vs, (VT)sj, coef, lo, hi, n, j, V + (size_t)(j + 1) * n, q, C.vs);
+      gf_cta_sum<VT>(a, gd + L.npart() + blockIdx.x);
+    }
+    // givens 1: k_gm_rotate reads the |.|^2 partials after this kernel has completed
+    if (givens != 1) ok = gm_grid_barrier(C.gm, total) && ok;
+  }
+  if (!run || (int)blockIdx.x != (givens == 2 ? G : 0)) return;
+  if (!ok) {
+    if (threadIdx.x == 0) gm_mark_done(st, C.gm, 3);
+    return;
+  }
+  if (givens == 1) return;
+  // the new column's norm, its rotation and the residual estimate
+  gf_norm_rotate<VT>(C, st, gd, L, m, j, G, reorth);
+}
+
+// Givens step of a fused iteration on its own (the fused kernel launched with givens = 1), one CTA
+// per cycle, after the fused kernel has completed: the same norm, rotation, residual estimate and
+// stop test as the fused kernel's CTA 0 would run, from the partials it left (G of them). A cycle
+// that has ended (or whose fused kernel gave up at a barrier) is left alone.
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_rotate(GmCols C, int m, int LG, int G, int reorth) {
+  GState* st = C.st + blockIdx.y;
+  if (st->done) return;
+  double* gd = C.gd + blockIdx.y * C.gds;
+  gf_norm_rotate<VT>(C, st, gd, GmLayout{m, LG}, m, st->j, G, reorth);
 }
 
 // y = R^{-1} g over the completed columns, then coef_k = y_k s_k (one CTA).
@@ -886,9 +966,10 @@ size_t gmres_update_smem(int m) {
   return std::max(sizeof(cplx<double>) * ((size_t)m + 1), sizeof(double) * 2 * (4 * (size_t)m + 3));
 }
 
-// The Gram-Schmidt passes of one iteration, after the matvec into B.W.
+// The Gram-Schmidt passes of one iteration, after the matvec into B.W. Returns true if the
+// Givens step was left to k_gm_rotate (a fused kernel with B.rot_stream set).
 template <typename VT>
-static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
+static bool enqueue_gs(const GmresBufs& B, cudaStream_t s) {
   const dim3 grid(gmres_grid(B.n), B.nrb);
   const size_t smem = gmres_update_smem(B.m);
   // with the static arrays, long cycles pass the 48 KB that needs no opt-in
@@ -898,16 +979,20 @@ static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
     const int sm = (int)gmres_update_smem(kGmMaxRestart);
     AC3D_CUDA(cudaFuncSetAttribute(k_gm_update<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     AC3D_CUDA(cudaFuncSetAttribute(k_gm_fused<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    AC3D_CUDA(cudaFuncSetAttribute(k_gm_rotate<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     AC3D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fused_per_sm, k_gm_fused<VT>, kGmThreads, sm));
   });
   if (B.m > kGmMaxRestart) throw Error(3, "internal: GMRES cycle longer than the update pass supports");
   // one cooperative launch when every cycle of the batch can have a CTA resident at once
   const int LG = gmres_grid(B.n);
-  const int Gc = std::min(LG, fused_per_sm * device_sm_count() / std::max(B.nrb, 1));
+  const int cap = fused_per_sm * device_sm_count();
+  const int Gc = std::min(LG, cap / std::max(B.nrb, 1));
   if (Gc >= 1 && (!B.reorth || B.W2)) {
     const GmCols C = cols(B);
+    // the Givens step: forked (rot_stream), else on one more CTA per cycle when it fits
+    const int givens = B.rot_stream ? 1 : ((Gc + 1) * B.nrb <= cap ? 2 : 0);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(Gc, B.nrb);
+    cfg.gridDim = dim3(Gc + (givens == 2 ? 1 : 0), B.nrb);
     cfg.blockDim = dim3(kGmThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
@@ -918,8 +1003,31 @@ static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
     cfg.numAttrs = 1;
     note_launch();
     AC3D_CUDA(cudaLaunchKernelEx(&cfg, k_gm_fused<VT>, C, B.m, B.n, LG, (cplx<VT>*)B.V, (const cplx<VT>*)B.W,
-                                 (cplx<VT>*)B.W2, (cplx<VT>*)B.q, B.reorth));
-    return;
+                                 (cplx<VT>*)B.W2, (cplx<VT>*)B.q, B.reorth, givens));
+    if (givens != 1) return false;
+    // the Givens step on the branch: it waits for this kernel, and the next Gram-Schmidt kernel
+    // waits for it (the caller joins the branch back)
+    AC3D_CUDA(cudaEventRecord(B.ev_gs, s));
+    AC3D_CUDA(cudaStreamWaitEvent(B.rot_stream, B.ev_gs, 0));
+    static int prio_high = [] {
+      int lo = 0, hi = 0;
+      AC3D_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      return hi;
+    }();
+    cudaLaunchConfig_t rc = {};
+    rc.gridDim = dim3(1, B.nrb);
+    rc.blockDim = dim3(kGmThreads);
+    rc.dynamicSmemBytes = smem;
+    rc.stream = B.rot_stream;
+    cudaLaunchAttribute rattr[1];
+    rattr[0].id = cudaLaunchAttributePriority;  // ahead of the matvec's waiting CTAs
+    rattr[0].val.priority = prio_high;
+    rc.attrs = rattr;
+    rc.numAttrs = 1;
+    note_launch();
+    AC3D_CUDA(cudaLaunchKernelEx(&rc, k_gm_rotate<VT>, C, B.m, LG, Gc, B.reorth));
+    AC3D_CUDA(cudaEventRecord(B.ev_rot, B.rot_stream));
+    return true;
   }
   const GmCols C = cols(B);
   launch_k(true, k_gm_dots<VT>, grid, dim3(kGmThreads), 0, s, C, B.m, B.n, (const cplx<VT>*)B.V,
@@ -934,26 +1042,35 @@ static void enqueue_gs(const GmresBufs& B, cudaStream_t s) {
     launch_k(true, k_gm_update<VT>, grid, dim3(kGmThreads), smem, s, C, B.m, B.n, (cplx<VT>*)B.V,
              (const cplx<VT>*)B.W, (cplx<VT>*)B.W2, (cplx<VT>*)B.q, 0, 1);
   }
+  return false;
+}
+
+// Waits on stream s for the Givens branch of the previous iteration, if it forked one.
+static void join_rotation(const GmresBufs& B, bool forked, cudaStream_t s) {
+  if (forked) AC3D_CUDA(cudaStreamWaitEvent(s, B.ev_rot, 0));
 }
 
 void gmres_enqueue_iterations(const GmresBufs& B, const DevPartition& DP, const DevHMat& H, bool tr, int count,
                               cudaStream_t s) {
+  bool forked = false;
   for (int i = 0; i < count; i++) {
     MatvecEpilogue ep;  // no fused dots
     launch_matvec_ex(DP, H, tr, B.vec64, B.q, B.W, nullptr, ep, &B.gm->done_all, s, nullptr, i > 0);
-    if (B.vec64)
-      enqueue_gs<double>(B, s);
-    else
-      enqueue_gs<float>(B, s);
+    join_rotation(B, forked, s);
+    forked = B.vec64 ? enqueue_gs<double>(B, s) : enqueue_gs<float>(B, s);
   }
+  join_rotation(B, forked, s);
 }
 
 void gmres_enqueue_iterations_block(const GmresBufs& B, const MultiBufs& MB, const DevPartition& DP,
                                     const DevHMat& H, int count, cudaStream_t s) {
+  bool forked = false;
   for (int i = 0; i < count; i++) {
     launch_mmatvec(DP, H, MB, B.q, B.W, nullptr, nullptr, &B.gm->done_all, s);
-    enqueue_gs<float>(B, s);
+    join_rotation(B, forked, s);
+    forked = enqueue_gs<float>(B, s);
   }
+  join_rotation(B, forked, s);
 }
 
 void gmres_enqueue_finish(const GmresBufs& B, void* x, cudaStream_t s) {

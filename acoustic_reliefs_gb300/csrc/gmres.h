@@ -47,6 +47,12 @@ struct GmresBufs {
   int reorth = 0;      // 1: two classical Gram-Schmidt passes per iteration (FP32 vectors)
   double* gd = nullptr;  // gmres_scalar_doubles(m, n) doubles
   GState* state = nullptr;
+  // Branch for the Givens step (rotation of the new Hessenberg column, residual estimate, stop
+  // test): when rot_stream is set, the iterations enqueued on a stream fork it after each fused
+  // Gram-Schmidt kernel, so that it runs beside the next matvec (which needs only V_{j+1}) and
+  // joins before the next Gram-Schmidt kernel (which needs the rotated column's scale and j).
+  cudaStream_t rot_stream = nullptr;
+  cudaEvent_t ev_gs = nullptr, ev_rot = nullptr;
 };
 
 int gmres_grid(int n);

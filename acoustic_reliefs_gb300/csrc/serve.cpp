@@ -271,6 +271,7 @@ int ac3d_server_create(ac3d_server** out, int slots, int precision, long long hb
       int r = ac3d_create(&c, 32, 2.0, &band, 1, 1, 1e-4, 1e-4, 1e-6, src, 50.0, 5.0, 0);
       if (r != AC3D_OK) throw Error(r, "cannot create a slot context");
       c->prec = precision;
+      c->givens_branch = false;
       S->slots.push_back(c);
     }
     for (int i = 0; i < slots; i++) S->workers.emplace_back(worker, S, i);
