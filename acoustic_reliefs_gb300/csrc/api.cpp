@@ -563,8 +563,11 @@ int run_gmres(ac3d_ctx* c, const DevHMat& H, const cd* b, cd* d, bool tr, double
   }
   gmres_enqueue_finish(G, d, s);
   GState st{};
+  GMulti gm{};
   AC3D_CUDA(cudaMemcpyAsync(&c->h_gstate[0], G.state, sizeof(GState), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaMemcpyAsync(&gm, G.gm, sizeof(GMulti), cudaMemcpyDeviceToHost, s));
   AC3D_CUDA(cudaStreamSynchronize(s));
+  if (gm.bar_fail) throw Error(AC3D_ERR_CUDA, "GMRES Gram-Schmidt grid barrier timed out (bounded wait)");
   st = c->h_gstate[0];
   *done = st.done;
   c->stats.matvecs += st.j;
@@ -749,8 +752,11 @@ int run_block_gmres(ac3d_ctx* c, const DevHMat& H, const MultiBufs& B, std::vect
   }
   gmres_enqueue_finish(G, B.x, s);
   std::vector<GState> st(G.nrb);
+  GMulti gmf{};
   AC3D_CUDA(cudaMemcpyAsync(st.data(), G.state, G.nrb * sizeof(GState), cudaMemcpyDeviceToHost, s));
+  AC3D_CUDA(cudaMemcpyAsync(&gmf, G.gm, sizeof(GMulti), cudaMemcpyDeviceToHost, s));
   AC3D_CUDA(cudaStreamSynchronize(s));
+  if (gmf.bar_fail) throw Error(AC3D_ERR_CUDA, "GMRES Gram-Schmidt grid barrier timed out (bounded wait)");
   done.assign(G.nrb, 0);
   int iters = 0;
   for (int j = 0; j < G.nrb; j++) {

@@ -9,15 +9,15 @@
 // that the vector the update pass writes is the next matvec's input without a normalisation pass:
 //   W = A V_j;  h_kj = s_k s_j (V_k^H W);  V_{j+1} = s_j W - sum_k (h_kj s_k) V_k;
 //   h_{j+1,j} = |V_{j+1}|,  s_{j+1} = 1 / h_{j+1,j}.
-// Per iteration: the matvec (into W), then per Gram-Schmidt pass a dot pass (the j + 1 dots,
-// per-CTA partials reduced by the last CTA in fixed order) and an update pass; with two passes the
-// first update also computes the second pass's dots. The final update writes V_{j+1} and its
-// norm, and its last CTA rotates the new Hessenberg column and updates the residual estimate
-// |g_{j+1}|. FP32 cycles take two passes (one loses orthogonality over long
-// cycles), FP64 cycles one. Vectors and their arithmetic, the dots and the norms are in the
-// solve's vector type (FP32 for the mixed-precision inner solve, FP64 for the FP64 solve); the
-// Hessenberg matrix, the rotations and the scalars are FP64. No atomics touch floating-point sums,
-// so a solve is bit-reproducible.
+// Per iteration: the matvec (into W), then the Gram-Schmidt kernel and the Givens step (rotation
+// of the new Hessenberg column, residual estimate |g_{j+1}|, stop test). FP32 cycles need a second
+// Gram-Schmidt pass (one loses orthogonality over long cycles); they run it delayed by one
+// iteration (k_gm_dcgs, below), with the basis stored normalised. FP64 cycles take one classical
+// pass (k_gm_fused). When a batch cannot have all its CTAs resident at once, separate dot and
+// update kernels with last-CTA reductions (two classical passes for FP32) run instead. Vectors and
+// their arithmetic, the dots and the norms are in the solve's vector type (FP32 for the
+// mixed-precision inner solve, FP64 for the FP64 solve); the Hessenberg matrix, the rotations and
+// the scalars are FP64. No atomics touch floating-point sums, so a solve is bit-reproducible.
 //
 // Batches: the kernels take the cycle as the grid's y index, so nrb independent cycles (one per
 // right-hand side of a block solve) run together and share each block matvec; their inputs and
@@ -74,7 +74,9 @@ struct GmLayout {
   __host__ __device__ size_t npart() const { return part() + 2 * ((size_t)m + 1) * G; }  // G
   __host__ __device__ size_t part2() const { return npart() + (size_t)G; }               // 2 (m + 1) G
   __host__ __device__ size_t h2() const { return part2() + 2 * ((size_t)m + 1) * G; }     // 2 (m + 1)
-  __host__ __device__ size_t total() const { return h2() + 2 * ((size_t)m + 1); }
+  __host__ __device__ size_t abpart() const { return h2() + 2 * ((size_t)m + 1); }      // 3 G
+  __host__ __device__ size_t ab() const { return abpart() + 3 * (size_t)G; }             // 4
+  __host__ __device__ size_t total() const { return ab() + 4; }
 };
 
 // Column r = blockIdx.y of a batch: its state, scalars and basis.
@@ -554,29 +556,28 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_update(GmCols C, int m, int n
 constexpr uint32_t kBarSpin = 1u << 22;  // polls (with a short sleep) before a barrier gives up
 
 // Grid-wide barrier over all CTAs of a cooperative launch (every CTA calls it the same number of
-// times). Returns false on every thread if this CTA's wait gave up (recorded in bar_fail).
+// times). One 64-bit arrival counter that is never reset during a cycle: arrival ticket t belongs
+// to barrier instance t / total (no CTA arrives at the next instance before all have arrived at
+// this one), which is complete when the counter reaches (t / total + 1) total. One atomic per CTA
+// and a poll, instead of a count reset and a generation bump after the last arrival. Returns
+// false on every thread if this CTA's wait gave up (recorded in bar_fail).
 __device__ __forceinline__ bool gm_grid_barrier(GMulti* gm, unsigned total) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* genp = &gm->bar_gen;
-    const unsigned g = *genp;
-    __threadfence();
+    __threadfence();  // this CTA's writes before its arrival
+    const unsigned long long t = atomicAdd(&gm->bar, 1ull);
+    const unsigned long long target = (t / total + 1) * (unsigned long long)total;
+    volatile unsigned long long* c = &gm->bar;
     int ok = 1;
-    if (atomicAdd(&gm->bar_count, 1u) == total - 1) {
-      atomicExch(&gm->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&gm->bar_gen, 1u);
-    } else {
-      uint32_t it = 0;
-      while (*genp == g) {
-        if (++it > kBarSpin) {
-          ok = 0;
-          atomicExch(&gm->bar_fail, 1);
-          break;
-        }
-        __nanosleep(32);
+    uint32_t it = 0;
+    while (*c < target) {
+      if (++it > kBarSpin) {
+        ok = 0;
+        atomicExch(&gm->bar_fail, 1);
+        break;
       }
+      __nanosleep(20);
     }
     __threadfence();
     s_ok = ok;
@@ -871,6 +872,338 @@ __global__ void __launch_bounds__(kGmThreads) k_gm_rotate(GmCols C, int m, int L
   gf_norm_rotate<VT>(C, st, gd, GmLayout{m, LG}, m, st->j, G, reorth);
 }
 
+// ------------------------------------------------------------------------------------------
+// Gram-Schmidt with delayed reorthogonalisation (FP32 cycles): one reduction per iteration.
+// After Bielich, Langou, Thomas, Swirydowicz, Yamazaki and Boman, "Low-synch Gram-Schmidt with
+// delayed reorthogonalization for Krylov solvers" (Parallel Computing, 2022), in this form:
+// the matvec input of iteration j is u_j, the first-pass result of iteration j - 1 (not yet
+// reorthogonalised, not normalised), with A q_{j-1} = Q_j h_{j-1} + u_j. With w = A u_j, one
+// pass over the basis gives the dots a = Q_j^H u_j, b = Q_j^H w, alpha = |u_j|^2 and
+// beta = u_j^H w. Then
+//   rho = sqrt(alpha - |a|^2),  q_j = (u_j - Q_j a) / rho          (the lagged second pass),
+//   column j - 1 of H: h_{j-1} + a, subdiagonal rho                   (finished now),
+//   gamma = (beta - a^H b) / rho^2,
+//   u_{j+1} = (w - gamma u_j - Q_j (b - gamma a)) / rho               (= A q_j - Q_{j+1} h_j),
+//   first-pass column j: h_kj = b_k / rho (k < j), h_jj = gamma - a_{j-1}.
+// (The exact first-pass column is (b - H a) / rho; the H a term is of the size of the lost
+// orthogonality times |H| and is left out.) Both vectors come out of one more pass over the basis,
+// so an iteration reads the basis twice and has two grid barriers, against three or four passes
+// and four barriers with two classical passes. The basis vectors q_k are stored normalised
+// (s_k = 1). The Givens step of column j - 1 runs after the reduction; the cycle's stop test
+// therefore sees column j - 1 during iteration j, and the iteration that finds convergence has
+// already run its matvec. A cycle that fills its basis ends after the reduction of iteration m,
+// which finishes column m - 1.
+// ------------------------------------------------------------------------------------------
+
+// Elements per lane per round of loads in gd_dot_partials (two dot products per basis load).
+constexpr int kGdE = 2;
+
+// Per-CTA partial dots a_k = conj(V_k) . U and b_k = conj(V_k) . X (k < j) over [lo, lo + len)
+// of the block vectors U and X (stride xs), into pa / pb[(k G + c) 2]; each lane takes the
+// elements lane, lane + 32, ... in that order.
+template <typename VT>
+__device__ __forceinline__ void gd_dot_partials(const cplx<VT>* __restrict__ V, const cplx<VT>* U,
+                                                const cplx<VT>* X, int xs, int lo, int len, int n, int j,
+                                                double* pa, double* pb, int G) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int kb = 4 * warp; kb < j; kb += 4 * kGmWarps) {
+    VT ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0}, br[4] = {0, 0, 0, 0}, bi[4] = {0, 0, 0, 0};
+    for (int t0 = 0; t0 < len; t0 += 32 * kGdE) {
+      cplx<VT> v[kGdE][4], u[kGdE], x[kGdE];
+#pragma unroll
+      for (int e = 0; e < kGdE; e++) {
+        const int t = t0 + 32 * e + lane;
+        u[e] = t < len ? U[(size_t)(lo + t) * xs] : cplx<VT>();
+        x[e] = t < len ? X[(size_t)(lo + t) * xs] : cplx<VT>();
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          v[e][q] = (t < len && kb + q < j) ? V[(size_t)(kb + q) * n + lo + t] : cplx<VT>();
+      }
+#pragma unroll
+      for (int e = 0; e < kGdE; e++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {  // conj(v) u and conj(v) x
+          ar[q] = fma(v[e][q].re, u[e].re, ar[q]);
+          ar[q] = fma(v[e][q].im, u[e].im, ar[q]);
+          ai[q] = fma(v[e][q].re, u[e].im, ai[q]);
+          ai[q] = fma(-v[e][q].im, u[e].re, ai[q]);
+          br[q] = fma(v[e][q].re, x[e].re, br[q]);
+          br[q] = fma(v[e][q].im, x[e].im, br[q]);
+          bi[q] = fma(v[e][q].re, x[e].im, bi[q]);
+          bi[q] = fma(-v[e][q].im, x[e].re, bi[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      ar[q] = warp_sum(ar[q]);
+      ai[q] = warp_sum(ai[q]);
+      br[q] = warp_sum(br[q]);
+      bi[q] = warp_sum(bi[q]);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (kb + q < j) {
+          const size_t o = ((size_t)(kb + q) * G + blockIdx.x) * 2;
+          pa[o] = (double)ar[q];
+          pa[o + 1] = (double)ai[q];
+          pb[o] = (double)br[q];
+          pb[o + 1] = (double)bi[q];
+        }
+  }
+}
+
+// Reduction of iteration j: slots 0..j-1 are a_k, j..2j-1 are b_k, 2j is (alpha, beta); this CTA
+// sums the slots c, c + G, ... (a warp each) over the G per-CTA partials in CTA order.
+template <typename VT>
+__device__ __forceinline__ void gd_reduce(double* gd, const GmLayout& L, int G, int j) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int sl = blockIdx.x + warp * G; sl <= 2 * j; sl += kGmWarps * G) {
+    if (sl == 2 * j) {
+      VT al = 0, br = 0, bi = 0;
+      for (int c = lane; c < G; c += 32) {
+        al += (VT)__ldcg(&gd[L.abpart() + 3 * c]);
+        br += (VT)__ldcg(&gd[L.abpart() + 3 * c + 1]);
+        bi += (VT)__ldcg(&gd[L.abpart() + 3 * c + 2]);
+      }
+      al = warp_sum(al);
+      br = warp_sum(br);
+      bi = warp_sum(bi);
+      if (lane == 0) {
+        gd[L.ab()] = (double)al;
+        gd[L.ab() + 1] = (double)br;
+        gd[L.ab() + 2] = (double)bi;
+      }
+      continue;
+    }
+    const bool isb = sl >= j;
+    const int k = isb ? sl - j : sl;
+    const double* part = gd + (isb ? L.part2() : L.part());
+    VT sr = 0, si = 0;
+    for (int c = lane; c < G; c += 32) {
+      sr += (VT)__ldcg(&part[((size_t)k * G + c) * 2]);
+      si += (VT)__ldcg(&part[((size_t)k * G + c) * 2 + 1]);
+    }
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (lane == 0) {
+      double* dst = gd + (isb ? L.h2() : L.coef()) + 2 * k;
+      dst[0] = (double)sr;
+      dst[1] = (double)si;
+    }
+  }
+}
+
+// rho^2 = alpha - |a|^2 and gamma = (beta - a^H b) / rho^2 from the reduced values, by the first
+// warp of the CTA (lanes over k, a fixed xor tree: every CTA gets the same bits); into sh[0..2] =
+// (rho^2, gamma.re, gamma.im).
+__device__ __forceinline__ void gd_scalars(const double* gd, const GmLayout& L, int j, double* sh) {
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  double aa = 0, abr = 0, abi = 0;
+  for (int k = lane; k < j; k += 32) {
+    const double ar = __ldcg(&gd[L.coef() + 2 * k]), ai = __ldcg(&gd[L.coef() + 2 * k + 1]);
+    const double br = __ldcg(&gd[L.h2() + 2 * k]), bi = __ldcg(&gd[L.h2() + 2 * k + 1]);
+    aa += ar * ar + ai * ai;
+    abr += ar * br + ai * bi;  // conj(a) b
+    abi += ar * bi - ai * br;
+  }
+  aa = warp_sum(aa);
+  abr = warp_sum(abr);
+  abi = warp_sum(abi);
+  if (lane == 0) {
+    const double al = __ldcg(&gd[L.ab()]), br = __ldcg(&gd[L.ab() + 1]), bi = __ldcg(&gd[L.ab() + 2]);
+    const double r2 = al - aa;
+    const double ir2 = r2 > 0.0 ? gm_rcp(r2) : 0.0;
+    sh[0] = r2;
+    sh[1] = (br - abr) * ir2;
+    sh[2] = (bi - abi) * ir2;
+  }
+}
+
+// The Givens step of iteration j (one CTA per cycle): column j - 1 finished (h_{j-1} + a,
+// subdiagonal rho) and rotated as gm_rotate does, then the first-pass column j stored for the
+// next iteration. Iteration 0 only sets g_0 = rho and the first-pass column 0.
+template <typename VT>
+__device__ __forceinline__ void gd_givens(GmCols C, GState* st, double* gd, const GmLayout& L, int m, int j) {
+  __shared__ double sh[3];
+  __shared__ int s_go;
+  gd_scalars(gd, L, j, sh);
+  __syncthreads();
+  const double r2 = sh[0];
+  const double rho = r2 > 0.0 ? gm_sqrt(r2) : 0.0;
+  const double gr = sh[1], gi = sh[2];
+  if (j > 0) {
+    for (int k = threadIdx.x; k < j; k += blockDim.x) {
+      gd[L.hcol() + 2 * k] += __ldcg(&gd[L.coef() + 2 * k]);
+      gd[L.hcol() + 2 * k + 1] += __ldcg(&gd[L.coef() + 2 * k + 1]);
+    }
+    __syncthreads();
+    gm_rotate(C, st, gd, L, m, j - 1, rho);  // st->j = j; its done test
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      gd[L.s() + j] = 1.0;  // q_j is stored normalised
+      s_go = *(volatile int*)&st->done == 0 && j < m;
+    }
+  } else if (threadIdx.x == 0) {
+    gd[L.g()] = rho;
+    gd[L.g() + 1] = 0.0;
+    gd[L.s()] = 1.0;
+    st->resid = rho;
+    s_go = rho > 0.0 && isfinite(rho);
+    if (!s_go) gm_mark_done(st, C.gm, rho == 0.0 ? 1 : 3);
+  }
+  __syncthreads();
+  if (!s_go) return;
+  // first-pass column j: b_k / rho, then gamma - a_{j-1}
+  const double ir = gm_rcp(rho);
+  for (int k = threadIdx.x; k < j; k += blockDim.x) {
+    gd[L.hcol() + 2 * k] = __ldcg(&gd[L.h2() + 2 * k]) * ir;
+    gd[L.hcol() + 2 * k + 1] = __ldcg(&gd[L.h2() + 2 * k + 1]) * ir;
+  }
+  if (threadIdx.x == 0) {
+    const double ar = j > 0 ? __ldcg(&gd[L.coef() + 2 * (j - 1)]) : 0.0;
+    const double ai = j > 0 ? __ldcg(&gd[L.coef() + 2 * (j - 1) + 1]) : 0.0;
+    gd[L.hcol() + 2 * j] = gr - ar;
+    gd[L.hcol() + 2 * j + 1] = gi - ai;
+    st->j = j + 1;
+  }
+}
+
+// Phase 3 of k_gm_dcgs over this CTA's elements [lo, hi).
+template <typename VT>
+__device__ __forceinline__ void gd_update(const double* gd, const GmLayout& L, int m, int n, int j, cplx<VT>* V,
+                                          const cplx<VT>* X, cplx<VT>* U, int vs, int lo, int hi) {
+  extern __shared__ __align__(16) unsigned char gsm[];
+  __shared__ double sh[3];
+  gd_scalars(gd, L, j, sh);
+  __syncthreads();
+  const double r2 = sh[0];
+  const double irho = r2 > 0.0 ? gm_rcp(gm_sqrt(r2)) : 0.0;
+  const double gr = sh[1], gi = sh[2];
+  cplx<VT>* ca = reinterpret_cast<cplx<VT>*>(gsm);
+  cplx<VT>* cb = ca + (m + 1);
+  for (int k = threadIdx.x; k < j; k += blockDim.x) {
+    const double ar = __ldcg(&gd[L.coef() + 2 * k]), ai = __ldcg(&gd[L.coef() + 2 * k + 1]);
+    const double br = __ldcg(&gd[L.h2() + 2 * k]), bi = __ldcg(&gd[L.h2() + 2 * k + 1]);
+    ca[k] = cplx<VT>((VT)ar, (VT)ai);
+    cb[k] = cplx<VT>((VT)(br - (gr * ar - gi * ai)), (VT)(bi - (gr * ai + gi * ar)));
+  }
+  __syncthreads();
+  const VT ir = (VT)irho, g_re = (VT)gr, g_im = (VT)gi;
+  cplx<VT>* Vj = V + (size_t)j * n;
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const cplx<VT> u = U[(size_t)i * vs], x = X[(size_t)i * vs];
+    VT pr = u.re, pi = u.im;  // u - Q a
+    VT qr = fma(-g_re, u.re, fma(g_im, u.im, x.re)), qi = fma(-g_re, u.im, fma(-g_im, u.re, x.im));  // w - gamma u
+    const cplx<VT>* Vi = V + i;
+    for (int k = 0; k < j; k += kGfChunk) {
+      cplx<VT> v[kGfChunk];
+#pragma unroll
+      for (int q = 0; q < kGfChunk; q++) v[q] = k + q < j ? Vi[(size_t)(k + q) * n] : cplx<VT>();
+#pragma unroll
+      for (int q = 0; q < kGfChunk; q++) {
+        if (k + q >= j) break;
+        const cplx<VT> a = ca[k + q], b = cb[k + q];
+        pr = fma(-a.re, v[q].re, pr);
+        pr = fma(a.im, v[q].im, pr);
+        pi = fma(-a.re, v[q].im, pi);
+        pi = fma(-a.im, v[q].re, pi);
+        qr = fma(-b.re, v[q].re, qr);
+        qr = fma(b.im, v[q].im, qr);
+        qi = fma(-b.re, v[q].im, qi);
+        qi = fma(-b.im, v[q].re, qi);
+      }
+    }
+    Vj[i] = cplx<VT>(pr * ir, pi * ir);
+    U[(size_t)i * vs] = cplx<VT>(qr * ir, qi * ir);
+  }
+}
+
+// One iteration with delayed reorthogonalisation (cooperative launch; FP32 cycles). U: the matvec
+// input u_j (block vectors; it receives u_{j+1}), W: w = A u_j. givens as in k_gm_fused (1: the
+// caller forks k_gm_dgivens; 2: the extra last CTA of each cycle).
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads, 3) k_gm_dcgs(GmCols C, int m, int n, int LG, cplx<VT>* V,
+                                                           const cplx<VT>* __restrict__ W, cplx<VT>* U, int givens) {
+  const int r = blockIdx.y, G = (int)gridDim.x - (givens == 2 ? 1 : 0);
+  const bool giv_cta = givens == 2 && (int)blockIdx.x == G;
+  const unsigned total = gridDim.x * gridDim.y;
+  GState* st = C.st + r;
+  double* gd = C.gd + r * C.gds;
+  V += r * C.Vs;
+  const cplx<VT>* X = W + r;
+  U += r;
+  const GmLayout L{m, LG};
+  const bool run = st->done == 0;  // changed only by the Givens step, after the reduction
+  const bool work = run && !giv_cta;
+  const int j = st->j;
+  int lo, hi;
+  {
+    const int per = (n + G - 1) / G;
+    lo = min(n, (int)blockIdx.x * per);
+    hi = min(n, lo + per);
+  }
+  bool ok = true;
+  // 1: dots of the basis against u_j and w; |u_j|^2 and u_j^H w
+  if (work) {
+    gd_dot_partials<VT>(V, U, X, C.vs, lo, hi - lo, n, j, gd + L.part(), gd + L.part2(), G);
+    VT al = 0, br = 0, bi = 0;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      const cplx<VT> u = U[(size_t)i * C.vs], x = X[(size_t)i * C.vs];
+      al = fma(u.re, u.re, fma(u.im, u.im, al));
+      br = fma(u.re, x.re, fma(u.im, x.im, br));
+      bi = fma(u.re, x.im, fma(-u.im, x.re, bi));
+    }
+    __shared__ VT sw[3][kGmWarps];
+    al = warp_sum(al);
+    br = warp_sum(br);
+    bi = warp_sum(bi);
+    if ((threadIdx.x & 31) == 0) {
+      sw[0][threadIdx.x >> 5] = al;
+      sw[1][threadIdx.x >> 5] = br;
+      sw[2][threadIdx.x >> 5] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      VT t = 0;
+      for (int w = 0; w < kGmWarps; w++) t += sw[threadIdx.x][w];
+      gd[L.abpart() + 3 * blockIdx.x + threadIdx.x] = (double)t;
+    }
+  }
+  ok = gm_grid_barrier(C.gm, total) && ok;
+  // 2: the sums
+  if (work && ok) gd_reduce<VT>(gd, L, G, j);
+  ok = gm_grid_barrier(C.gm, total) && ok;
+  if (givens == 1) grid_dep_launch();  // the next matvec reads u_{j+1} only after this kernel
+  if (!run) return;
+  if (!ok) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) gm_mark_done(st, C.gm, 3);
+    return;
+  }
+  if (giv_cta) {
+    gd_givens<VT>(C, st, gd, L, m, j);
+    return;
+  }
+  // 3 (not after a full basis: iteration m only finishes column m - 1):
+  // q_j = (u - Q a) / rho into V_j, u_{j+1} = (w - gamma u - Q (b - gamma a)) / rho into U
+  if (j < m) gd_update<VT>(gd, L, m, n, j, V, X, U, C.vs, lo, hi);
+  if (givens == 0 && blockIdx.x == 0) {
+    __syncthreads();
+    gd_givens<VT>(C, st, gd, L, m, j);
+  }
+}
+
+// The Givens step of a delayed-reorthogonalisation iteration on its own (k_gm_dcgs launched with
+// givens = 1), one CTA per cycle, after that kernel has completed.
+template <typename VT>
+__global__ void __launch_bounds__(kGmThreads) k_gm_dgivens(GmCols C, int m, int LG) {
+  GState* st = C.st + blockIdx.y;
+  if (st->done) return;
+  double* gd = C.gd + blockIdx.y * C.gds;
+  gd_givens<VT>(C, st, gd, GmLayout{m, LG}, m, st->j);
+}
+
 // y = R^{-1} g over the completed columns, then coef_k = y_k s_k (one CTA).
 __global__ void __launch_bounds__(kGmThreads) k_gm_solve(GmCols C, int m, int G) {
   const GmLayout L{m, G};
@@ -972,22 +1305,30 @@ template <typename VT>
 static bool enqueue_gs(const GmresBufs& B, cudaStream_t s) {
   const dim3 grid(gmres_grid(B.n), B.nrb);
   const size_t smem = gmres_update_smem(B.m);
+  // FP32 cycles with two passes: delayed reorthogonalisation (k_gm_dcgs)
+  constexpr bool fp32 = sizeof(VT) == 4;
+  const bool dcgs = fp32 && B.reorth;
   // with the static arrays, long cycles pass the 48 KB that needs no opt-in
   static std::once_flag once;
-  static int fused_per_sm = 0;  // resident CTAs per SM of the fused kernel
+  static int fused_per_sm = 0, dcgs_per_sm = 0;  // resident CTAs per SM of the cooperative kernels
   std::call_once(once, [] {
     const int sm = (int)gmres_update_smem(kGmMaxRestart);
     AC3D_CUDA(cudaFuncSetAttribute(k_gm_update<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     AC3D_CUDA(cudaFuncSetAttribute(k_gm_fused<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     AC3D_CUDA(cudaFuncSetAttribute(k_gm_rotate<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     AC3D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fused_per_sm, k_gm_fused<VT>, kGmThreads, sm));
+    if constexpr (fp32) {
+      AC3D_CUDA(cudaFuncSetAttribute(k_gm_dcgs<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+      AC3D_CUDA(cudaFuncSetAttribute(k_gm_dgivens<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+      AC3D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dcgs_per_sm, k_gm_dcgs<VT>, kGmThreads, sm));
+    }
   });
   if (B.m > kGmMaxRestart) throw Error(3, "internal: GMRES cycle longer than the update pass supports");
   // one cooperative launch when every cycle of the batch can have a CTA resident at once
   const int LG = gmres_grid(B.n);
-  const int cap = fused_per_sm * device_sm_count();
+  const int cap = (dcgs ? dcgs_per_sm : fused_per_sm) * device_sm_count();
   const int Gc = std::min(LG, cap / std::max(B.nrb, 1));
-  if (Gc >= 1 && (!B.reorth || B.W2)) {
+  if (Gc >= 1 && (dcgs || !B.reorth || B.W2)) {
     const GmCols C = cols(B);
     // the Givens step: forked (rot_stream), else on one more CTA per cycle when it fits
     const int givens = B.rot_stream ? 1 : ((Gc + 1) * B.nrb <= cap ? 2 : 0);
@@ -1002,8 +1343,14 @@ static bool enqueue_gs(const GmresBufs& B, cudaStream_t s) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     note_launch();
-    AC3D_CUDA(cudaLaunchKernelEx(&cfg, k_gm_fused<VT>, C, B.m, B.n, LG, (cplx<VT>*)B.V, (const cplx<VT>*)B.W,
-                                 (cplx<VT>*)B.W2, (cplx<VT>*)B.q, B.reorth, givens));
+    if constexpr (fp32) {
+      if (dcgs)
+        AC3D_CUDA(cudaLaunchKernelEx(&cfg, k_gm_dcgs<VT>, C, B.m, B.n, LG, (cplx<VT>*)B.V, (const cplx<VT>*)B.W,
+                                     (cplx<VT>*)B.q, givens));
+    }
+    if (!dcgs)
+      AC3D_CUDA(cudaLaunchKernelEx(&cfg, k_gm_fused<VT>, C, B.m, B.n, LG, (cplx<VT>*)B.V, (const cplx<VT>*)B.W,
+                                   (cplx<VT>*)B.W2, (cplx<VT>*)B.q, B.reorth, givens));
     if (givens != 1) return false;
     // the Givens step on the branch: it waits for this kernel, and the next Gram-Schmidt kernel
     // waits for it (the caller joins the branch back)
@@ -1025,7 +1372,10 @@ static bool enqueue_gs(const GmresBufs& B, cudaStream_t s) {
     rc.attrs = rattr;
     rc.numAttrs = 1;
     note_launch();
-    AC3D_CUDA(cudaLaunchKernelEx(&rc, k_gm_rotate<VT>, C, B.m, LG, Gc, B.reorth));
+    if constexpr (fp32) {
+      if (dcgs) AC3D_CUDA(cudaLaunchKernelEx(&rc, k_gm_dgivens<VT>, C, B.m, LG));
+    }
+    if (!dcgs) AC3D_CUDA(cudaLaunchKernelEx(&rc, k_gm_rotate<VT>, C, B.m, LG, Gc, B.reorth));
     AC3D_CUDA(cudaEventRecord(B.ev_rot, B.rot_stream));
     return true;
   }

@@ -23,8 +23,8 @@ struct GState {
 struct GMulti {
   int ndone;     // cycles that have ended
   int done_all;
-  unsigned bar_count, bar_gen;  // grid barrier of the fused Gram-Schmidt kernel (zero at init)
-  int bar_fail;                 // a grid barrier gave up waiting
+  unsigned long long bar;  // arrivals at the grid barriers of the Gram-Schmidt kernels (zero at init)
+  int bar_fail;            // a grid barrier gave up waiting
   int pad[3];
 };
 
