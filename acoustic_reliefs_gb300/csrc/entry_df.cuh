@@ -38,7 +38,7 @@ __host__ __device__ __forceinline__ cdf entry_df(df64 k, const DfPt* __restrict_
     const df64 rx = p.x - ge->yq[q][0];
     const df64 ry = p.y - ge->yq[q][1];
     const df64 rz = p.z - ge->yq[q][2];
-    const df64 r2 = df_sqr(rx) + df_sqr(ry) + df_sqr(rz);
+    const df64 r2 = df_norm2_3(rx, ry, rz);
     const df64 r = df_sqrt(r2);
     const df64 rinv = df_rcp(r);
     const df64 s = df_fma(rz, nz, df_fma(ry, ny, rx * nx));

@@ -16,22 +16,28 @@
 
 namespace ac3d {
 
-// Per leaf: K = sum of ranks of its list, padded to even; kseg = prefix of K, seg = prefix of R K.
-__global__ void leaf_scan_kernel(const int* __restrict__ rank, const int* __restrict__ leaf_start,
-                                 const int* __restrict__ ptr, const int* __restrict__ items, int nleaf, int* kseg,
-                                 long long* seg) {
+// Per leaf: K = sum of the ranks of its list, padded to even, into kseg[l] (a warp per leaf, the
+// ranks summed by lanes; integer sums, so the order does not matter).
+__global__ void leaf_k_kernel(const int* __restrict__ rank, const int* __restrict__ ptr,
+                              const int* __restrict__ items, int nleaf, int* kseg) {
+  const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (l >= nleaf) return;
+  int K = 0;
+  for (int it = ptr[l] + lane; it < ptr[l + 1]; it += 32) K += rank[items[it]];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) K += __shfl_xor_sync(0xffffffffu, K, o);
+  if (lane == 0) kseg[l] = K + (K & 1);
+}
+
+// kseg[l] (holding K of leaf l) becomes the prefix of K, seg[l] the prefix of R K (one CTA).
+__global__ void leaf_scan_kernel(const int* __restrict__ leaf_start, int nleaf, int* kseg, long long* seg) {
   __shared__ long long sk[1024], ss[1024];
   const int tid = threadIdx.x;
   const int chunk = (nleaf + 1023) / 1024;
   const int s = min(nleaf, tid * chunk), e = min(nleaf, s + chunk);
-  auto kleaf = [&](int l) {
-    int K = 0;
-    for (int it = ptr[l]; it < ptr[l + 1]; it++) K += rank[items[it]];
-    return K + (K & 1);
-  };
   long long ak = 0, as = 0;
   for (int l = s; l < e; l++) {
-    const int K = kleaf(l);
+    const int K = kseg[l];
     ak += K;
     as += (long long)K * (leaf_start[l + 1] - leaf_start[l]);
   }
@@ -47,9 +53,9 @@ __global__ void leaf_scan_kernel(const int* __restrict__ rank, const int* __rest
   }
   long long bk = tid ? sk[tid - 1] : 0, bs = tid ? ss[tid - 1] : 0;
   for (int l = s; l < e; l++) {
+    const int K = kseg[l];  // this thread's own leaf, read before it is overwritten
     kseg[l] = (int)bk;
     seg[l] = bs;
-    const int K = kleaf(l);
     bk += K;
     bs += (long long)K * (leaf_start[l + 1] - leaf_start[l]);
   }
@@ -65,37 +71,83 @@ template <typename R>
 __device__ __forceinline__ cplx<R> seg_value(const cplx<R>& v) { return v; }
 __device__ __forceinline__ cf seg_value(const cdf& v) { return cf(v.re.hi, v.im.hi); }
 
-// One CTA per leaf: copy the leaf's slices of every listed block's terms, write the segment
-// column indices (phase-1 output positions t_off[b] + q) and the first column of each entry.
+constexpr int kPackThreads = 256;
+constexpr int kPackChunk = 512;  // list entries per round of a leaf's scan
+
+// One CTA per leaf: the first segment column of every listed block (an exclusive scan of the ranks
+// in list order, a chunk of the list at a time), then a warp per list entry copies the leaf's
+// slice of the block's terms (lanes over the leaf's rows, four terms per round of loads) and
+// writes the segment column indices (phase-1 output positions t_off[b] + q) and the entry's first
+// column. The list entries' metadata loads and copies run in parallel across the warps; the
+// output is the same as copying the list in order.
 template <typename P, typename R>
-__global__ void pack_segments_kernel(const P* __restrict__ pool, const long long* __restrict__ task_off,
-                                     const int* __restrict__ t_off, const int* __restrict__ rank,
-                                     const int4* __restrict__ blocks, const int* __restrict__ leaf_start,
-                                     const int* __restrict__ ptr, const int* __restrict__ items, int cols,
-                                     const int* __restrict__ kseg, const long long* __restrict__ seg, cplx<R>* S,
-                                     int* sidx, const int* __restrict__ pos, int* kpos) {
+__global__ void __launch_bounds__(kPackThreads) pack_segments_kernel(
+    const P* __restrict__ pool, const long long* __restrict__ task_off, const int* __restrict__ t_off,
+    const int* __restrict__ rank, const int4* __restrict__ blocks, const int* __restrict__ leaf_start,
+    const int* __restrict__ ptr, const int* __restrict__ items, int cols, const int* __restrict__ kseg,
+    const long long* __restrict__ seg, cplx<R>* S, int* sidx, const int* __restrict__ pos, int* kpos) {
+  __shared__ int sb[kPackChunk], sr[kPackChunk], sbase[kPackChunk];
+  __shared__ int wsum[kPackThreads / 32];
+  __shared__ int s_total;
   const int l = blockIdx.x;
   const int ls = leaf_start[l], Rn = leaf_start[l + 1] - ls;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   cplx<R>* dst = S + seg[l];
   int* idx = sidx + kseg[l];
-  int kbase = 0;
-  for (int it = ptr[l]; it < ptr[l + 1]; it++) {
-    const int b = items[it];
-    const int r = rank[b];
-    const int4 q4 = blocks[b];
-    const int off = cols ? (q4.y - q4.x) + (ls - q4.z) : (ls - q4.x);
-    const long long* to = task_off + t_off[b];
-    for (int e = threadIdx.x; e < r * Rn; e += blockDim.x) {
-      const int q = e / Rn, row = e - q * Rn;
-      dst[(long long)(kbase + q) * Rn + row] = seg_value(pool[to[q] + off + row]);
+  const int it0 = ptr[l], nit = ptr[l + 1] - it0;
+  int base = 0;  // segment columns of the entries before this chunk
+  for (int c0 = 0; c0 < nit; c0 += kPackChunk) {
+    const int cn = min(kPackChunk, nit - c0);
+    for (int i = threadIdx.x; i < kPackChunk; i += kPackThreads) {
+      const int b = i < cn ? items[it0 + c0 + i] : 0;
+      sb[i] = b;
+      sr[i] = i < cn ? rank[b] : 0;
     }
-    for (int q = threadIdx.x; q < r; q += blockDim.x) idx[kbase + q] = t_off[b] + q;
-    if (threadIdx.x == 0) kpos[pos[it]] = kseg[l] + kbase;  // block-major order
-    kbase += r;
+    __syncthreads();
+    // exclusive scan of sr: each thread two consecutive entries, warp scan, then the warp totals
+    const int a0 = sr[2 * threadIdx.x], a1 = sr[2 * threadIdx.x + 1];
+    int v = a0 + a1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    if (lane == 31) wsum[warp] = v;
+    __syncthreads();
+    int wb = 0;
+    for (int w = 0; w < warp; w++) wb += wsum[w];
+    const int excl = base + wb + v - (a0 + a1);
+    sbase[2 * threadIdx.x] = excl;
+    sbase[2 * threadIdx.x + 1] = excl + a0;
+    if (threadIdx.x == kPackThreads - 1) s_total = wb + v;
+    __syncthreads();
+    for (int i = warp; i < cn; i += kPackThreads / 32) {
+      const int b = sb[i], r = sr[i], kb = sbase[i];
+      const int4 q4 = blocks[b];
+      const int off = cols ? (q4.y - q4.x) + (ls - q4.z) : (ls - q4.x);
+      const long long* to = task_off + t_off[b];
+      for (int q0 = 0; q0 < r; q0 += 4) {  // four terms per round of loads
+        long long src[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) src[u] = q0 + u < r ? to[q0 + u] + off : -1;
+        for (int row = lane; row < Rn; row += 32) {
+          P val[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) val[u] = pool[(src[u] >= 0 ? src[u] : src[0]) + row];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            if (src[u] >= 0) dst[(long long)(kb + q0 + u) * Rn + row] = seg_value(val[u]);
+        }
+      }
+      for (int q = lane; q < r; q += 32) idx[kb + q] = t_off[b] + q;
+      if (lane == 0) kpos[pos[it0 + c0 + i]] = kseg[l] + kb;  // block-major order
+    }
+    base += s_total;
+    __syncthreads();  // the chunk's arrays are free
   }
-  if (kbase & 1) {  // padding column
-    for (int row = threadIdx.x; row < Rn; row += blockDim.x) dst[(long long)kbase * Rn + row] = cplx<R>();
-    if (threadIdx.x == 0) idx[kbase] = -1;
+  if (base & 1) {  // padding column
+    for (int row = threadIdx.x; row < Rn; row += kPackThreads) dst[(long long)base * Rn + row] = cplx<R>();
+    if (threadIdx.x == 0) idx[base] = -1;
   }
 }
 
@@ -109,11 +161,13 @@ static void pack_side(const DevPartition& DP, DevHMat& H, bool cols, cudaStream_
   DevBuf& idx = cols ? H.vidx : H.uidx;
   DevBuf& kpos = cols ? H.kpos_t : H.kpos_f;
   note_launch();
-  leaf_scan_kernel<<<1, 1024, 0, s>>>(H.rank.as<int>(), DP.leaf_start.as<int>(), ptr, items, DP.nleaf,
-                                      kseg.as<int>(), seg.as<long long>());
+  leaf_k_kernel<<<(DP.nleaf + 7) / 8, 256, 0, s>>>(H.rank.as<int>(), ptr, items, DP.nleaf, kseg.as<int>());
   AC3D_CUDA(cudaGetLastError());
   note_launch();
-  pack_segments_kernel<P, R><<<DP.nleaf, 256, 0, s>>>(H.pool.as<P>(), H.task_off.as<long long>(),
+  leaf_scan_kernel<<<1, 1024, 0, s>>>(DP.leaf_start.as<int>(), DP.nleaf, kseg.as<int>(), seg.as<long long>());
+  AC3D_CUDA(cudaGetLastError());
+  note_launch();
+  pack_segments_kernel<P, R><<<DP.nleaf, kPackThreads, 0, s>>>(H.pool.as<P>(), H.task_off.as<long long>(),
                                                    H.t_off.as<int>(), H.rank.as<int>(), DP.blocks_a.as<int4>(),
                                                    DP.leaf_start.as<int>(), ptr, items, cols ? 1 : 0, kseg.as<int>(),
                                                    seg.as<long long>(), S.as<cplx<R>>(), idx.as<int>(),
