@@ -783,6 +783,7 @@ __global__ void __launch_bounds__(kGmThreads, sizeof(VT) == 4 ? 3 : 2) k_gm_fuse
   // givens: where the Givens step runs. 0: CTA 0 after its last update; 1: k_gm_rotate after this
   // kernel (the caller forks it); 2: one CTA more than the element CTAs (the last), right after
   // the last grid barrier, while the others run the last update.
+  if (*(volatile const int*)&C.gm->done_all) return;  // as in k_gm_dcgs
   const int r = blockIdx.y, G = (int)gridDim.x - (givens == 2 ? 1 : 0);
   const bool rot_cta = givens == 2 && (int)blockIdx.x == G;
   // with the Givens step forked, the next matvec may start streaming its matrix during the last
@@ -1126,6 +1127,9 @@ __device__ __forceinline__ void gd_update(const double* gd, const GmLayout& L, i
 template <typename VT>
 __global__ void __launch_bounds__(kGmThreads, 3) k_gm_dcgs(GmCols C, int m, int n, int LG, cplx<VT>* V,
                                                            const cplx<VT>* __restrict__ W, cplx<VT>* U, int givens) {
+  // every cycle of the batch has ended (set by a Givens step of an earlier kernel, so all CTAs read
+  // the same value): the iterations left in a captured chunk pass without their barriers
+  if (*(volatile const int*)&C.gm->done_all) return;
   const int r = blockIdx.y, G = (int)gridDim.x - (givens == 2 ? 1 : 0);
   const bool giv_cta = givens == 2 && (int)blockIdx.x == G;
   const unsigned total = gridDim.x * gridDim.y;
