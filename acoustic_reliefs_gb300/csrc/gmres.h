@@ -44,13 +44,15 @@ struct GmresBufs {
   void* q = nullptr;   // the next matvec's input (n)
   void* W = nullptr;   // the matvec's output (n)
   void* W2 = nullptr;  // the first Gram-Schmidt pass's result (n per cycle), when there are two
-  int reorth = 0;      // 1: two classical Gram-Schmidt passes per iteration (FP32 vectors)
+  int reorth = 0;      // 1: two classical Gram-Schmidt passes (FP32 vectors; the second one delayed by an
+                       // iteration in the cooperative kernel)
   double* gd = nullptr;  // gmres_scalar_doubles(m, n) doubles
   GState* state = nullptr;
   // Branch for the Givens step (rotation of the new Hessenberg column, residual estimate, stop
-  // test): when rot_stream is set, the iterations enqueued on a stream fork it after each fused
-  // Gram-Schmidt kernel, so that it runs beside the next matvec (which needs only V_{j+1}) and
-  // joins before the next Gram-Schmidt kernel (which needs the rotated column's scale and j).
+  // test): when rot_stream is set, the iterations enqueued on a stream fork it after each
+  // cooperative Gram-Schmidt kernel, so that it runs beside the next matvec (which needs only the
+  // new input vector) and joins before the next Gram-Schmidt kernel (which needs j and the
+  // Hessenberg column the Givens step leaves).
   cudaStream_t rot_stream = nullptr;
   cudaEvent_t ev_gs = nullptr, ev_rot = nullptr;
 };
