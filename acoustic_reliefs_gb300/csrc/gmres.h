@@ -1,6 +1,8 @@
 // Device-resident GMRES interface (internal).
 #pragma once
 
+#include <cstddef>
+
 #include "internal.h"
 
 namespace ac3d {
@@ -27,6 +29,8 @@ struct GMulti {
   int bar_fail;            // a grid barrier gave up waiting
   int pad[3];
 };
+static_assert(offsetof(GMulti, bar) % 8 == 0, "64-bit atomics need an aligned arrival counter");
+static_assert(sizeof(GState) % 8 == 0, "GMulti follows the cycles' states in one allocation");
 
 // Device buffers of one cycle, or of a batch of nrb independent cycles that share their matvecs
 // (column r: state st + r, scalars gd + r gds, basis V + r Vs elements; the matvec input q and
