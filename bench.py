@@ -174,6 +174,35 @@ def gradient_leg():
                     "shape-derivative terms of 16 directions per derivative evaluation (ac3d_gradient_multi)"}
 
 
+def product_call_leg():
+    """The reference pipeline's own forward call (acoustics_pipeline.py:7,11-17) on its submitted
+    0.6 m relief (the 38686-triangle mesh held in tests/golden/ref_relief_cat.npz): DiffBEM(128, 1.5,
+    17 third-octave bands 100 Hz - 4 kHz, 3 frequencies each, ACA and solver tolerances 1e-5, point
+    source at (0, 100, 0), 1297-point hemisphere of radius 50 m), every band's diffusion coefficient
+    in one values() call (51 solves), with the drop-in's defaults (mixed precision, BiCGSTAB as the
+    reference, exact receiver product) and with GMRES; timed after a one-band warm-up call."""
+    from acoustic_reliefs_gb300.acoustics3d import DiffBEM
+    g = np.load(os.path.join(ROOT, "tests", "golden", "ref_relief_cat.npz"))
+    bands = [float(b) for b in SWEEP_BANDS]
+    out = {"workload": "reference product call: DiffBEM(128, 1.5, 17 bands 100 Hz - 4 kHz, 3, 1e-5, 1e-5, 1e-5, "
+                       "(0, 100, 0), 50, 5) on the reference's submitted 0.6 m relief (38686 triangles), values()"}
+    for krylov in ("bicgstab", "gmres"):
+        bem = DiffBEM(128, 1.5, bands, 3, 1e-5, 1e-5, 1e-5, (0.0, 100.0, 0.0), 50, 5)
+        bem.silent = True
+        bem.set_krylov(krylov, RESTART)
+        bem.set_mesh(g["Ps"], g["Es"])
+        bem.band_value(1000.0)
+        t0 = time.perf_counter()
+        cs = bem.values()
+        dt = time.perf_counter() - t0
+        st = bem.stats()
+        out[krylov] = {"seconds": dt, "solves": 3 * len(bands), "solves_per_s": 3 * len(bands) / dt,
+                       "iterations": st["iterations"], "ms_assemble": st["ms_assemble"], "ms_solve": st["ms_solve"],
+                       "coef_1000": cs[bands.index(1000.0)],
+                       "coef_1000_minus_oracle": cs[bands.index(1000.0)] - float(g["coef_1000"])}
+    return out
+
+
 def block_c5_leg():
     """configs[4] at size: 0.9 m relief with a 256 x 256 heightmap (210240 triangles) at 4 kHz,
     16 plane-wave directions as one block; error against the FP64 solve of the first direction."""
@@ -717,6 +746,8 @@ def run_gpu(args):
         line["gradient_c4"] = gradient_leg()
     if not args.no_c5_leg and world == 1:
         line["block_c5"] = block_c5_leg()
+    if not args.no_product_leg and world == 1:
+        line["product_call"] = product_call_leg()
     print(json.dumps(line), flush=True)
     return 0
 
@@ -735,6 +766,10 @@ def main():
     ap.add_argument("--no-fp64-sweep", action="store_true")
     ap.add_argument("--no-gradient-leg", action="store_true", help="skip the 81k-triangle 37-angle gradient")
     ap.add_argument("--no-c5-leg", action="store_true", help="skip the 210k-triangle 16-direction block solve")
+    ap.add_argument("--no-product-leg", action="store_true",
+                    help="skip the reference pipeline's own call (17 bands on its 38686-triangle relief)")
+    ap.add_argument("--product-call-only", action="store_true",
+                    help="only the reference pipeline's own call (one JSON object)")
     ap.add_argument("--multi-rhs", type=int, default=16, help="directions of the block-solve leg (0 to skip)")
     ap.add_argument("--krylov", default="gmres", choices=["gmres", "bicgstab"],
                     help="inner solver of every GPU leg (BiCGSTAB is the reference's; a served BiCGSTAB leg is "
@@ -750,6 +785,9 @@ def main():
         return run_single_block(args)
     if args.single_context:
         return run_single(args)
+    if args.product_call_only:
+        print(json.dumps({"product_call": product_call_leg()}), flush=True)
+        return 0
     return run_gpu(args)
 
 
