@@ -747,7 +747,10 @@ def run_gpu(args):
     if not args.no_c5_leg and world == 1:
         line["block_c5"] = block_c5_leg()
     if not args.no_product_leg and world == 1:
-        line["product_call"] = product_call_leg()
+        try:
+            line["product_call"] = product_call_leg()
+        except Exception as e:  # an extra leg: its failure is reported, not fatal to the line
+            line["product_call"] = {"error": f"{type(e).__name__}: {e}"}
     print(json.dumps(line), flush=True)
     return 0
 
