@@ -143,10 +143,10 @@ def served_sweep(args, Ls):
 
 
 def gradient_leg():
-    """configs[3] at size: 0.9 m relief with a 128 x 128 heightmap (81024 triangles, 37445
-    differentiable heights), 1, 2 and 4 kHz, 37 incidence angles in the xy plane, receivers on a
-    10 m semicircle: loss = 1 - mean coefficient and its gradient in one call, timed once after a
-    small warm-up call."""
+    """The multi-incidence gradient at full size: 0.9 m relief with a 128 x 128 heightmap (81024
+    triangles, 37445 differentiable heights), 1, 2 and 4 kHz, 37 incidence angles in the xy plane,
+    receivers on a 10 m semicircle: loss = 1 - mean coefficient and its gradient in one call,
+    timed once after a small warm-up call."""
     from acoustic_reliefs_gb300 import meshes
     from acoustic_reliefs_gb300.acoustics3d import DiffBEM
     R = meshes.relief(0.9, 0.9, 0.05, 48, 7, 48, 2, meshes.smooth_heightmap(128, 0))
@@ -204,8 +204,9 @@ def product_call_leg():
 
 
 def block_c5_leg():
-    """configs[4] at size: 0.9 m relief with a 256 x 256 heightmap (210240 triangles) at 4 kHz,
-    16 plane-wave directions as one block; error against the FP64 solve of the first direction."""
+    """The large block solve: 0.9 m relief with a 256 x 256 heightmap (210240 triangles) at 4
+    kHz, 16 plane-wave directions as one block; error against the FP64 solve of the first
+    direction."""
     from acoustic_reliefs_gb300 import meshes
     from acoustic_reliefs_gb300.acoustics3d import DiffBEM
     R = meshes.relief(0.9, 0.9, 0.05, 40, 7, 40, 3, meshes.smooth_heightmap(256, 0))
