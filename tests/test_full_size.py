@@ -69,9 +69,9 @@ def test_gradient_80k_triangles(gpu_lib):
 def test_gradient_multi_80k_triangles_37_directions(gpu_lib):
     """The multi-incidence gradient at full size: the 0.9 m relief with a 128 x 128 heightmap
     (81024 triangles), 1, 2 and 4 kHz, 37 incidence angles in the xy plane, receivers on a 10 m
-    semicircle: loss = 1 - mean
-    coefficient and its gradient over all 37445 differentiable heights in one call. The
-    coefficients agree with single-direction forward solves, and the gradient is finite."""
+    semicircle: loss = 1 - mean coefficient and its gradient over all 37445 differentiable heights
+    in one call. The coefficients agree with single-direction forward solves, and the gradient is
+    finite."""
     import time
     R = meshes.relief(0.9, 0.9, 0.05, 48, 7, 48, 2, meshes.smooth_heightmap(128, 0))
     assert len(R.Es) == 81024
